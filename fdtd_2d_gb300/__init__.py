@@ -1,0 +1,378 @@
+"""GB300-native TMz FDTD time-step engine.
+
+Python mirror of the C ABI in ``include/fdtd2d.h`` (ctypes over the in-tree
+``libfdtd2d.so``).  The compute path is the CUDA library; there is no CPU
+fallback: importing this package without the built library raises, and
+creating a shot without a CUDA device raises.
+
+The objects mirror the reference's device-driver boundary
+(FDTD_2D_Full/Kernel.cuh:100-108):
+
+* :class:`Problem` -- the host-side setup the reference builds in
+  FDTD_2D_Full/FDTD_cuda.cu (from a parameter spec or from Settings.ini).
+* :class:`Shot` -- ``DevMemoryAllocation`` (constructor), the
+  ``DevFieldCalculation`` loop (:meth:`Shot.run`), detector/field read-back,
+  ``DevMemoryFree`` (:meth:`Shot.close`).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "libfdtd2d.so"
+
+# ---- status codes and enums (fdtd2d.h) ------------------------------------
+OK = 0
+ERR_INVALID, ERR_NOMEM, ERR_CUDA, ERR_NONFINITE, ERR_RANGE = -1, -2, -3, -4, -5
+ERR_IO, ERR_CONFIG, ERR_STATE, ERR_BUDGET, ERR_NODEVICE = -6, -7, -8, -9, -10
+
+MEDIUM_UNIFORM, MEDIUM_MATERIAL_ID = 0, 1
+STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
+
+FIELD_EZ, FIELD_HX, FIELD_HY, FIELD_JZ = 0, 1, 2, 3
+FIELD_PSI_EZX_1, FIELD_PSI_EZX_2, FIELD_PSI_EZY_1, FIELD_PSI_EZY_2 = 4, 5, 6, 7
+FIELD_PSI_HYX_1, FIELD_PSI_HYX_2, FIELD_PSI_HXY_1, FIELD_PSI_HXY_2 = 8, 9, 10, 11
+FIELD_NAMES = {"ez": FIELD_EZ, "hx": FIELD_HX, "hy": FIELD_HY, "jz": FIELD_JZ,
+               "psi_ezx_1": FIELD_PSI_EZX_1, "psi_ezx_2": FIELD_PSI_EZX_2,
+               "psi_ezy_1": FIELD_PSI_EZY_1, "psi_ezy_2": FIELD_PSI_EZY_2,
+               "psi_hyx_1": FIELD_PSI_HYX_1, "psi_hyx_2": FIELD_PSI_HYX_2,
+               "psi_hxy_1": FIELD_PSI_HXY_1, "psi_hxy_2": FIELD_PSI_HXY_2}
+
+
+class FdtdError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        msg = _lib().fdtd2d_strerror(status).decode() if LIB_PATH.exists() else str(status)
+        super().__init__(f"{what}: {msg} ({status})" if what else f"{msg} ({status})")
+
+
+# ---- C structs --------------------------------------------------------------
+class Point(C.Structure):
+    _fields_ = [("i", C.c_int32), ("j", C.c_int32)]
+
+
+_fp = C.POINTER(C.c_float)
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_pp = C.POINTER(Point)
+
+
+class Setup(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int32), ("ny", C.c_int32), ("npml", C.c_int32), ("n_steps", C.c_int32),
+        ("dt", C.c_double), ("dx", C.c_double), ("dy", C.c_double),
+        ("be_x_1", _fp), ("ce_x_1", _fp), ("be_x_2", _fp), ("ce_x_2", _fp),
+        ("bh_x_1", _fp), ("ch_x_1", _fp), ("bh_x_2", _fp), ("ch_x_2", _fp),
+        ("be_y_1", _fp), ("ce_y_1", _fp), ("be_y_2", _fp), ("ce_y_2", _fp),
+        ("bh_y_1", _fp), ("ch_y_1", _fp), ("bh_y_2", _fp), ("ch_y_2", _fp),
+        ("den_ex", _fp), ("den_hx", _fp), ("den_ey", _fp), ("den_hy", _fp),
+        ("medium", C.c_int32), ("ca", C.c_float), ("cb", C.c_float), ("da", C.c_float),
+        ("db", C.c_float),
+        ("ne", _fp), ("id1", _ip), ("id2", _ip), ("id3", _ip), ("n_materials", C.c_int32),
+        ("mat_ca", _fp), ("mat_cb", _fp), ("mat_da", _fp), ("mat_db", _fp), ("mat_ne", _fp),
+        ("nu", C.c_double), ("jz_coef", C.c_double),
+        ("n_src", C.c_int32), ("src", _pp), ("src_phase_deg", _dp), ("envelope", _fp),
+        ("src_scale", C.c_double), ("f0", C.c_double), ("f1", C.c_double), ("t1", C.c_double),
+        ("src_pi", C.c_double),
+        ("n_det", C.c_int32), ("det", _pp), ("n_comp", C.c_int32), ("comp", _pp),
+        ("record_traces", C.c_int32), ("dft_freq", C.c_double), ("storage", C.c_int32),
+        ("n_rc", C.c_int32), ("rc_scan_i", _ip), ("rc_max_i", _ip), ("rc_j_cut", C.c_int32),
+        ("rc_level", C.c_float), ("rc_edge0", C.c_float),
+        ("line_n", C.c_int32), ("line_i0", C.c_int32), ("line_j", C.c_int32),
+        ("line_first", C.c_int32), ("line_last", C.c_int32),
+    ]
+
+
+class Spec(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int32), ("ny", C.c_int32), ("npml", C.c_int32), ("n_steps", C.c_int32),
+        ("dx", C.c_double), ("dy", C.c_double), ("courant", C.c_double), ("dt", C.c_double),
+        ("cpml_m", C.c_double), ("cpml_ma", C.c_double), ("sigma_factor", C.c_double),
+        ("kappa_max", C.c_double), ("alpha_max", C.c_double),
+        ("profile", C.c_int32), ("ne_peak", C.c_double), ("x_lo", C.c_double),
+        ("x_hi", C.c_double), ("x_center", C.c_double), ("width", C.c_double),
+        ("grf_rms", C.c_double), ("grf_corr", C.c_double), ("seed", C.c_uint64),
+        ("nu", C.c_double),
+        ("n_elem", C.c_int32), ("src_i", C.c_int32), ("src_j", C.c_int32),
+        ("src_di", C.c_int32), ("src_dj", C.c_int32),
+        ("freq", C.c_double), ("steer_deg", C.c_double), ("amp", C.c_double),
+        ("pulse", C.c_int32), ("pulse_width", C.c_double), ("pulse_t0", C.c_double),
+        ("n_det", C.c_int32), ("det_i", C.c_int32), ("det_j", C.c_int32),
+        ("det_di", C.c_int32), ("det_dj", C.c_int32),
+        ("record_traces", C.c_int32), ("dft_freq", C.c_double), ("storage", C.c_int32),
+    ]
+
+
+_LIB = None
+
+
+def _lib():
+    """Load libfdtd2d.so (fails loudly when it has not been built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not LIB_PATH.exists():
+        raise ImportError(
+            f"{LIB_PATH} is missing: build the CUDA library first "
+            "(python -m fdtd_2d_gb300.build, or __graft_entry__.build())")
+    lib = C.CDLL(str(LIB_PATH))
+    vp = C.c_void_p
+    sig = {
+        "fdtd2d_abi_version": (C.c_int, []),
+        "fdtd2d_strerror": (C.c_char_p, [C.c_int]),
+        "fdtd2d_create": (C.c_int, [C.POINTER(Setup), C.c_int, C.POINTER(vp)]),
+        "fdtd2d_run": (C.c_int, [vp, C.c_int32, C.c_int32]),
+        "fdtd2d_synchronize": (C.c_int, [vp]),
+        "fdtd2d_current_step": (C.c_int, [vp, _ip]),
+        "fdtd2d_read_traces": (C.c_int, [vp, C.c_int32, C.c_int32, _fp, _fp, _fp, _fp]),
+        "fdtd2d_read_dft": (C.c_int, [vp, _dp, _dp]),
+        "fdtd2d_read_rc": (C.c_int, [vp, C.c_int32, C.c_int32, _ip]),
+        "fdtd2d_read_line": (C.c_int, [vp, C.c_int32, C.c_int32, _fp]),
+        "fdtd2d_read_field": (C.c_int, [vp, C.c_int, _fp]),
+        "fdtd2d_write_field": (C.c_int, [vp, C.c_int, _fp]),
+        "fdtd2d_check_finite": (C.c_int, [vp]),
+        "fdtd2d_destroy": (C.c_int, [vp]),
+        "fdtd2d_device_bytes": (C.c_int64, [C.POINTER(Setup)]),
+        "fdtd2d_launch_count": (C.c_int64, [vp]),
+        "fdtd2d_last_cuda_error": (C.c_int, [vp]),
+        "fdtd2d_spec_defaults": (None, [C.POINTER(Spec)]),
+        "fdtd2d_problem_from_spec": (C.c_int, [C.POINTER(Spec), C.POINTER(vp)]),
+        "fdtd2d_problem_from_ini": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
+        "fdtd2d_problem_setup": (C.POINTER(Setup), [vp]),
+        "fdtd2d_problem_free": (None, [vp]),
+        "fdtd2d_run_settings": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int]),
+        "fdtd2d_device_count": (C.c_int, []),
+        "fdtd2d_run_timed": (C.c_int, [vp, C.c_int32, C.c_int32, _fp]),
+        "fdtd2d_stability": (C.c_double, [C.POINTER(Setup)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)  # every declared entry point must be exported
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def lib():
+    return _lib()
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != OK:
+        raise FdtdError(rc, what)
+
+
+def default_spec(**overrides) -> Spec:
+    """The plain 512^2 workload (see fdtd2d_spec_defaults) with overrides."""
+    sp = Spec()
+    _lib().fdtd2d_spec_defaults(C.byref(sp))
+    for k, v in overrides.items():
+        if not hasattr(sp, k):
+            raise AttributeError(f"fdtd2d_spec has no field {k!r}")
+        setattr(sp, k, v)
+    return sp
+
+
+def production_spec(**overrides) -> Spec:
+    """8192^2 production shot: dx = 0.25 mm, 32-cell CPML, 20000 steps,
+    16-element array on x = 64 (pitch 5 cells, centred), CW 50 GHz steered to
+    15 degrees with a 2 ns raised-cosine ramp, tanh plasma
+    1.5e19 (1 + tanh((x - 5000)/600)) times (1 + 0.05 g) with g a seeded
+    Gaussian random field (correlation length 40 cells, seed 1001),
+    nu = 2e9 1/s, 16 co-located Ez detectors with a 50 GHz running DFT."""
+    n = 8192
+    n_elem, pitch = 16, 5
+    base = dict(nx=n, ny=n, npml=32, n_steps=20000, dx=0.25e-3, dy=0.25e-3, courant=0.99,
+                profile=3, ne_peak=3.0e19, x_center=5000.0, width=600.0, grf_rms=0.05,
+                grf_corr=40.0, seed=1001, nu=2e9,
+                n_elem=n_elem, src_i=64, src_j=n // 2 - (n_elem - 1) * pitch // 2, src_di=0,
+                src_dj=pitch, freq=50e9, steer_deg=15.0, amp=1.0, pulse=1, pulse_width=2e-9,
+                n_det=n_elem, det_i=64, det_j=n // 2 - (n_elem - 1) * pitch // 2, det_di=0,
+                det_dj=pitch, record_traces=1, dft_freq=50e9)
+    base.update(overrides)
+    return default_spec(**base)
+
+
+def field_shape(which: int, nx: int, ny: int, npml: int) -> tuple[int, int]:
+    P = npml
+    return {FIELD_EZ: (ny, nx), FIELD_JZ: (ny, nx), FIELD_HX: (ny - 1, nx), FIELD_HY: (ny, nx - 1),
+            FIELD_PSI_EZX_1: (ny, P), FIELD_PSI_EZX_2: (ny, P),
+            FIELD_PSI_HYX_1: (ny, P - 1), FIELD_PSI_HYX_2: (ny, P - 1),
+            FIELD_PSI_EZY_1: (P, nx), FIELD_PSI_EZY_2: (P, nx),
+            FIELD_PSI_HXY_1: (P - 1, nx), FIELD_PSI_HXY_2: (P - 1, nx)}[which]
+
+
+class Problem:
+    """Host-side precomputed setup; owns the arrays its fdtd2d_setup points to."""
+
+    def __init__(self, handle: int):
+        self._h = C.c_void_p(handle)
+        self.setup_ptr = _lib().fdtd2d_problem_setup(self._h)
+        self.setup = self.setup_ptr.contents
+
+    @classmethod
+    def from_spec(cls, spec: Spec | None = None, **overrides) -> "Problem":
+        sp = spec if spec is not None else default_spec(**overrides)
+        h = C.c_void_p()
+        _check(_lib().fdtd2d_problem_from_spec(C.byref(sp), C.byref(h)), "problem_from_spec")
+        return cls(h.value)
+
+    @classmethod
+    def from_ini(cls, path: str | os.PathLike) -> "Problem":
+        h = C.c_void_p()
+        _check(_lib().fdtd2d_problem_from_ini(str(path).encode(), C.byref(h)), "problem_from_ini")
+        return cls(h.value)
+
+    def close(self) -> None:
+        if self._h:
+            _lib().fdtd2d_problem_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # convenience views (copies) of the setup arrays
+    def array(self, name: str, n: int, dtype=np.float32) -> np.ndarray:
+        p = getattr(self.setup, name)
+        if not p:
+            return np.zeros(0, dtype)
+        return np.ctypeslib.as_array(p, shape=(n,)).astype(dtype, copy=True)
+
+    @property
+    def nx(self) -> int:
+        return self.setup.nx
+
+    @property
+    def ny(self) -> int:
+        return self.setup.ny
+
+    @property
+    def n_steps(self) -> int:
+        return self.setup.n_steps
+
+    def device_bytes(self) -> int:
+        return int(_lib().fdtd2d_device_bytes(self.setup_ptr))
+
+    def stability(self) -> float:
+        return float(_lib().fdtd2d_stability(self.setup_ptr))
+
+
+class Shot:
+    """One shot's device state on one GPU (one CUDA stream)."""
+
+    def __init__(self, problem: Problem, device: int = 0):
+        self.problem = problem
+        s = problem.setup
+        self.nx, self.ny, self.npml, self.n_steps = s.nx, s.ny, s.npml, s.n_steps
+        self.n_det, self.n_comp = s.n_det, s.n_comp
+        h = C.c_void_p()
+        _check(_lib().fdtd2d_create(problem.setup_ptr, device, C.byref(h)), "fdtd2d_create")
+        self._h = h
+
+    @property
+    def step(self) -> int:
+        n = C.c_int32()
+        _check(_lib().fdtd2d_current_step(self._h, C.byref(n)), "current_step")
+        return n.value
+
+    def run(self, n_first: int, n_last: int) -> None:
+        _check(_lib().fdtd2d_run(self._h, n_first, n_last), "fdtd2d_run")
+
+    def advance(self, k: int) -> None:
+        n0 = self.step + 1
+        self.run(n0, n0 + k - 1)
+
+    def run_timed(self, n_first: int, n_last: int) -> float:
+        """Run steps and return their device time (ms, CUDA events on the shot's stream)."""
+        ms = C.c_float()
+        _check(_lib().fdtd2d_run_timed(self._h, n_first, n_last, C.byref(ms)), "run_timed")
+        return float(ms.value)
+
+    def synchronize(self) -> None:
+        _check(_lib().fdtd2d_synchronize(self._h), "synchronize")
+
+    def launches(self) -> int:
+        return int(_lib().fdtd2d_launch_count(self._h))
+
+    def read_field(self, which) -> np.ndarray:
+        w = FIELD_NAMES[which] if isinstance(which, str) else which
+        out = np.empty(field_shape(w, self.nx, self.ny, self.npml), np.float32)
+        _check(_lib().fdtd2d_read_field(self._h, w, out.ctypes.data_as(_fp)), "read_field")
+        return out
+
+    def write_field(self, which, arr) -> None:
+        w = FIELD_NAMES[which] if isinstance(which, str) else which
+        a = np.ascontiguousarray(arr, dtype=np.float32)
+        if a.shape != field_shape(w, self.nx, self.ny, self.npml):
+            raise ValueError(f"field {which}: shape {a.shape} != {field_shape(w, self.nx, self.ny, self.npml)}")
+        _check(_lib().fdtd2d_write_field(self._h, w, a.ctypes.data_as(_fp)), "write_field")
+
+    def traces(self, n0: int = 1, n1: int | None = None) -> dict[str, np.ndarray]:
+        n1 = self.step if n1 is None else n1
+        rows = n1 - n0 + 1
+        det = np.zeros((rows, max(self.n_det, 0)), np.float32)
+        cez = np.zeros((rows, max(self.n_comp, 0)), np.float32)
+        chx = np.zeros_like(cez)
+        chy = np.zeros_like(cez)
+        _check(_lib().fdtd2d_read_traces(self._h, n0, n1, det.ctypes.data_as(_fp),
+                                         cez.ctypes.data_as(_fp), chx.ctypes.data_as(_fp),
+                                         chy.ctypes.data_as(_fp)), "read_traces")
+        return {"det_ez": det, "comp_ez": cez, "comp_hx": chx, "comp_hy": chy}
+
+    def dft(self) -> np.ndarray:
+        re = np.zeros(self.n_det, np.float64)
+        im = np.zeros(self.n_det, np.float64)
+        _check(_lib().fdtd2d_read_dft(self._h, re.ctypes.data_as(_dp), im.ctypes.data_as(_dp)), "read_dft")
+        return re + 1j * im
+
+    def rc(self, n0: int = 1, n1: int | None = None) -> np.ndarray:
+        n1 = self.step if n1 is None else n1
+        out = np.zeros((n1 - n0 + 1, self.problem.setup.n_rc), np.int32)
+        _check(_lib().fdtd2d_read_rc(self._h, n0, n1, out.ctypes.data_as(_ip)), "read_rc")
+        return out
+
+    def line(self, n0: int, n1: int) -> np.ndarray:
+        out = np.zeros((n1 - n0 + 1, self.problem.setup.line_n), np.float32)
+        _check(_lib().fdtd2d_read_line(self._h, n0, n1, out.ctypes.data_as(_fp)), "read_line")
+        return out
+
+    def check_finite(self) -> bool:
+        rc = _lib().fdtd2d_check_finite(self._h)
+        if rc == ERR_NONFINITE:
+            return False
+        _check(rc, "check_finite")
+        return True
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            _lib().fdtd2d_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def device_count() -> int:
+    return int(_lib().fdtd2d_device_count())
+
+
+def run_settings(ini_path, out_dir, device: int = 0) -> None:
+    """Whole reference program on the GPU: Settings.ini in, reference output files out."""
+    _check(_lib().fdtd2d_run_settings(str(ini_path).encode(), str(out_dir).encode(), device),
+           "run_settings")

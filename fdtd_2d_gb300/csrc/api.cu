@@ -1,0 +1,672 @@
+// C-ABI layer: one context = one shot's device state + one CUDA stream.
+// Replaces DevMemoryAllocation / DevFieldCalculation / DevMemoryFree
+// (FDTD_2D_Full/kernel.cu:1087-1618, 1928-2818, 2820-2987).  Unlike the
+// reference, every allocation is owned by the context (no file-scope device
+// globals), so independent contexts can coexist in one process.
+#include "../../include/fdtd2d.h"
+#include "internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+using namespace fdtd2d;
+
+struct fdtd2d_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int nx = 0, ny = 0, pitch = 0, npml = 0, n_steps = 0;
+  int n_det = 0, n_comp = 0, record = 0, medium = 0;
+  bool dft = false;
+  int32_t step = 0;
+  int last_cuda = 0;
+  int64_t launches = 0;
+  DevShot h{};              // host copy of the device descriptor
+  DevShot* d_shot = nullptr;
+  int4* d_units = nullptr;
+  int n_units = 0;
+  int grid_warps = 0;
+  int* d_flag = nullptr;
+  // wave-front tracker and line probe
+  int n_rc = 0, rc_j_cut = 0;
+  float rc_level = 0;
+  int *d_rc_scan = nullptr, *d_rc_max = nullptr, *d_spd = nullptr;
+  float* d_edge = nullptr;
+  int line_n = 0, line_i0 = 0, line_j = 0, line_first = 0, line_last = -1;
+  float* d_line = nullptr;
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+
+int fail_cuda(fdtd2d_ctx* c, cudaError_t e) {
+  if (c) c->last_cuda = (int)e;
+  return e == cudaErrorMemoryAllocation ? FDTD2D_ERR_NOMEM : FDTD2D_ERR_CUDA;
+}
+
+template <class T>
+cudaError_t dalloc(fdtd2d_ctx* c, T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return cudaSuccess;
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+  if (e != cudaSuccess) return e;
+  c->allocs.push_back(q);
+  *p = static_cast<T*>(q);
+  return cudaMemsetAsync(q, 0, count * sizeof(T), c->stream);
+}
+
+int pitch_for(int nx) { return (nx + 31) / 32 * 32; }
+
+__global__ void drive_from_density(float* kp, int64_t pitch, int nx, int ny, float beta) {
+  // kp = beta * ne in place; cells without plasma (ne <= 0) get 0.
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)ny * pitch;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % pitch);
+    const float ne = kp[t];
+    kp[t] = (i < nx && ne > 0.f) ? beta * ne : 0.f;
+  }
+}
+
+int validate(const fdtd2d_setup* s) {
+  if (!s) return FDTD2D_ERR_INVALID;
+  const int P = s->npml;
+  if (s->nx < 8 || s->ny < 8 || P < 2) return FDTD2D_ERR_INVALID;
+  if (2 * P + 2 > s->nx || 2 * P + 2 > s->ny) return FDTD2D_ERR_INVALID;
+  if (s->n_steps < 1 || !(s->dt > 0) || !(s->dx > 0) || !(s->dy > 0)) return FDTD2D_ERR_INVALID;
+  const float* tabs[] = {s->be_x_1, s->ce_x_1, s->be_x_2, s->ce_x_2, s->bh_x_1, s->ch_x_1,
+                         s->bh_x_2, s->ch_x_2, s->be_y_1, s->ce_y_1, s->be_y_2, s->ce_y_2,
+                         s->bh_y_1, s->ch_y_1, s->bh_y_2, s->ch_y_2};
+  for (const float* t : tabs)
+    if (!t) return FDTD2D_ERR_INVALID;
+  if (!s->den_ex || !s->den_hx || !s->den_ey || !s->den_hy) return FDTD2D_ERR_INVALID;
+  if (s->medium == FDTD2D_MEDIUM_MATERIAL_ID) {
+    if (!s->id1 || !s->id2 || !s->id3) return FDTD2D_ERR_INVALID;
+    if (s->n_materials < 2 || s->n_materials > 256) return FDTD2D_ERR_INVALID;
+    if (!s->mat_ca || !s->mat_cb || !s->mat_da || !s->mat_db || !s->mat_ne) return FDTD2D_ERR_INVALID;
+  } else if (s->medium != FDTD2D_MEDIUM_UNIFORM) {
+    return FDTD2D_ERR_INVALID;
+  }
+  if (s->storage != FDTD2D_STORE_F32) return FDTD2D_ERR_INVALID;  // reduced storage: batch API
+  auto interior = [&](const fdtd2d_point& p) {
+    return p.i >= 1 && p.i <= s->nx - 2 && p.j >= 1 && p.j <= s->ny - 2;
+  };
+  if (s->n_src < 0 || s->n_det < 0 || s->n_comp < 0) return FDTD2D_ERR_INVALID;
+  if (s->n_src > 0 && (!s->src || !s->src_phase_deg || !s->envelope)) return FDTD2D_ERR_INVALID;
+  if (s->n_det > 0 && !s->det) return FDTD2D_ERR_INVALID;
+  if (s->n_comp > 0 && !s->comp) return FDTD2D_ERR_INVALID;
+  for (int e = 0; e < s->n_src; ++e)
+    if (!interior(s->src[e])) return FDTD2D_ERR_RANGE;
+  for (int e = 0; e < s->n_det; ++e)
+    if (!interior(s->det[e])) return FDTD2D_ERR_RANGE;
+  for (int e = 0; e < s->n_comp; ++e)
+    if (!interior(s->comp[e])) return FDTD2D_ERR_RANGE;
+  if (s->f1 != s->f0 && !(s->t1 > 0)) return FDTD2D_ERR_INVALID;
+  if (s->n_rc < 0 || (s->n_rc > 0 && (!s->rc_scan_i || !s->rc_max_i))) return FDTD2D_ERR_INVALID;
+  for (int l = 0; l < s->n_rc; ++l)
+    if (s->rc_scan_i[l] < 0 || s->rc_scan_i[l] >= s->nx || s->rc_max_i[l] < 0 || s->rc_max_i[l] >= s->nx)
+      return FDTD2D_ERR_RANGE;
+  if (s->line_n < 0) return FDTD2D_ERR_INVALID;
+  if (s->line_n > 0 && (s->line_i0 < 0 || s->line_i0 + s->line_n > s->nx || s->line_j < 0 ||
+                        s->line_j >= s->ny || s->line_first < 1 || s->line_last > s->n_steps ||
+                        s->line_last < s->line_first))
+    return FDTD2D_ERR_RANGE;
+  return FDTD2D_OK;
+}
+
+// Split rows [0, ny-1) x column blocks into at most `warps` equal units.
+std::vector<int4> make_units(int shot, int nx, int ny, int warps) {
+  const int cb = (nx + kCols - 1) / kCols;
+  const int rows = ny - 1;
+  int strips = std::max(1, warps / cb);
+  strips = std::min(strips, std::max(1, rows / 8));
+  std::vector<int4> u;
+  u.reserve((size_t)cb * strips);
+  for (int s = 0; s < strips; ++s) {
+    const int j0 = (int)((int64_t)rows * s / strips);
+    const int j1 = (int)((int64_t)rows * (s + 1) / strips);
+    if (j1 <= j0) continue;
+    for (int c = 0; c < cb; ++c) u.push_back(make_int4(shot, c * kCols, j0, j1));
+  }
+  return u;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdtd2d_abi_version(void) { return FDTD2D_ABI_VERSION; }
+
+const char* fdtd2d_strerror(int status) {
+  switch (status) {
+    case FDTD2D_OK: return "ok";
+    case FDTD2D_ERR_INVALID: return "invalid argument or setup";
+    case FDTD2D_ERR_NOMEM: return "out of memory";
+    case FDTD2D_ERR_CUDA: return "CUDA runtime error";
+    case FDTD2D_ERR_NONFINITE: return "non-finite value in the fields";
+    case FDTD2D_ERR_RANGE: return "index or step out of range";
+    case FDTD2D_ERR_IO: return "file I/O error";
+    case FDTD2D_ERR_CONFIG: return "configuration error";
+    case FDTD2D_ERR_STATE: return "call not valid in this state";
+    case FDTD2D_ERR_BUDGET: return "request exceeds the memory budget";
+    case FDTD2D_ERR_NODEVICE: return "no CUDA device";
+    default: return "unknown error";
+  }
+}
+
+int64_t fdtd2d_device_bytes(const fdtd2d_setup* s) {
+  if (!s) return -1;
+  const int64_t pitch = pitch_for(s->nx);
+  const int64_t cells = pitch * s->ny;
+  const int64_t P = s->npml;
+  int64_t b = cells * 4 * 8;                                       // 4 fields x 2
+  b += (s->medium == FDTD2D_MEDIUM_UNIFORM) ? (s->ne ? cells * 4 : 0) : cells * 3;
+  b += 2 * 4 * (2 * (P - 1) * pitch + 2 * P * pitch + 2 * s->ny * P * 2);
+  b += 4 * (int64_t)s->n_steps * (s->record_traces ? (s->n_det + 3 * s->n_comp) : 0);
+  b += 4 * (int64_t)(s->n_steps + 1) + 16 * (int64_t)s->n_det + (1 << 20);
+  return b;
+}
+
+int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
+  if (!out) return FDTD2D_ERR_INVALID;
+  *out = nullptr;
+  int rc = validate(s);
+  if (rc) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return FDTD2D_ERR_NODEVICE;
+  if (device < 0 || device >= ndev) return FDTD2D_ERR_INVALID;
+
+  fdtd2d_ctx* c = new (std::nothrow) fdtd2d_ctx();
+  if (!c) return FDTD2D_ERR_NOMEM;
+  c->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    rc = fail_cuda(c, e);
+    fdtd2d_destroy(c);
+    return rc;
+  }
+  const int nx = s->nx, ny = s->ny, P = s->npml;
+  const int pitch = pitch_for(nx);
+  const int64_t cells = (int64_t)pitch * ny;
+  c->nx = nx; c->ny = ny; c->pitch = pitch; c->npml = P; c->n_steps = s->n_steps;
+  c->n_det = s->n_det; c->n_comp = s->n_comp; c->record = s->record_traces ? 1 : 0;
+  c->medium = s->medium;
+  c->dft = s->dft_freq > 0 && s->n_det > 0;
+
+  DevShot& h = c->h;
+  h.nx = nx; h.ny = ny; h.pitch = pitch; h.npml = P; h.n_steps = s->n_steps; h.base_n = 0;
+  const double nudt = 0.5 * s->nu * s->dt;
+  h.ja = (float)((1.0 - nudt) / (1.0 + nudt));
+  const double beta = s->jz_coef * s->dt / (1.0 + nudt);
+  h.dx = (float)s->dx; h.dy = (float)s->dy;
+
+#define CK(expr)                     \
+  do {                               \
+    cudaError_t _e = (expr);         \
+    if (_e != cudaSuccess) {         \
+      rc = fail_cuda(c, _e);         \
+      fdtd2d_destroy(c);             \
+      return rc;                     \
+    }                                \
+  } while (0)
+
+  h.cells = cells;
+  CK(dalloc(c, &h.fld, (size_t)cells * 8));
+  h.o_ezy = (int64_t)2 * (P - 1) * pitch;
+  h.o_hyx = h.o_ezy + (int64_t)2 * P * pitch;
+  h.o_ezx = h.o_hyx + (int64_t)2 * ny * P;
+  h.psi_buf = h.o_ezx + (int64_t)2 * ny * P;
+  CK(dalloc(c, &h.psi, (size_t)h.psi_buf * 2));
+
+  // medium
+  if (s->medium == FDTD2D_MEDIUM_UNIFORM) {
+    h.ca = s->ca; h.cb = s->cb; h.da = s->da; h.db = s->db;
+    if (s->ne) {
+      float* kp = nullptr;
+      CK(dalloc(c, &kp, cells));
+      CK(cudaMemcpy2DAsync(kp, pitch * sizeof(float), s->ne, nx * sizeof(float), nx * sizeof(float),
+                           ny, cudaMemcpyHostToDevice, c->stream));
+      drive_from_density<<<1024, 256, 0, c->stream>>>(kp, pitch, nx, ny, (float)beta);
+      ++c->launches;
+      CK(cudaGetLastError());
+      h.kp = kp;
+    }
+  } else {
+    std::vector<uint8_t> ids((size_t)cells * 3, 0);
+    const int32_t* src[3] = {s->id1, s->id2, s->id3};
+    for (int m = 0; m < 3; ++m) {
+      for (int j = 0; j < ny; ++j) {
+        for (int i = 0; i < nx; ++i) {
+          const int32_t v = src[m][(int64_t)j * nx + i];
+          if (v < 0 || v >= s->n_materials) {
+            fdtd2d_destroy(c);
+            return FDTD2D_ERR_RANGE;
+          }
+          ids[(size_t)m * cells + (size_t)j * pitch + i] = (uint8_t)v;
+        }
+      }
+    }
+    uint8_t* d_ids = nullptr;
+    CK(dalloc(c, &d_ids, ids.size()));
+    CK(cudaMemcpyAsync(d_ids, ids.data(), ids.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    h.id1 = d_ids; h.id2 = d_ids + cells; h.id3 = d_ids + 2 * cells;
+    std::vector<MatE> me(256);
+    std::vector<MatH> mh(256);
+    for (int m = 0; m < 256; ++m) {
+      me[m] = MatE{0.f, 0.f, 0.f, m == 1 ? 1.f : 0.f};
+      mh[m] = MatH{0.f, 0.f};
+      if (m < s->n_materials) {
+        const double ne = s->mat_ne[m];
+        me[m].ca = s->mat_ca[m];
+        me[m].cb = s->mat_cb[m];
+        me[m].kp = ne > 0 ? (float)(beta * ne) : 0.f;
+        mh[m].da = s->mat_da[m];
+        mh[m].db = s->mat_db[m];
+      }
+    }
+    MatE* d_me = nullptr;
+    MatH* d_mh = nullptr;
+    CK(dalloc(c, &d_me, 256));
+    CK(dalloc(c, &d_mh, 256));
+    CK(cudaMemcpyAsync(d_me, me.data(), 256 * sizeof(MatE), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(d_mh, mh.data(), 256 * sizeof(MatH), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    h.mat_e = d_me; h.mat_h = d_mh;
+  }
+
+  // CPML and denominator tables
+  {
+    std::vector<float> tab((size_t)kCpmlRows * P, 0.f);
+    const float* rows[kCpmlRows] = {s->be_x_1, s->ce_x_1, s->be_x_2, s->ce_x_2, s->bh_x_1, s->ch_x_1,
+                                    s->bh_x_2, s->ch_x_2, s->be_y_1, s->ce_y_1, s->be_y_2, s->ce_y_2,
+                                    s->bh_y_1, s->ch_y_1, s->bh_y_2, s->ch_y_2};
+    for (int r = 0; r < kCpmlRows; ++r) {
+      const bool hrow = (r % 8) >= 4;
+      const int len = hrow ? P - 1 : P;
+      for (int k = 0; k < len; ++k) tab[(size_t)r * P + k] = rows[r][k];
+    }
+    std::vector<float> dex(pitch, 0.f), dhx(pitch, 0.f), dey(ny, 0.f), dhy(ny, 0.f);
+    for (int i = 0; i < nx - 1; ++i) { dex[i] = s->den_ex[i]; dhx[i] = s->den_hx[i]; }
+    for (int j = 0; j < ny - 1; ++j) { dey[j] = s->den_ey[j]; dhy[j] = s->den_hy[j]; }
+    float *d_tab, *d_dex, *d_dhx, *d_dey, *d_dhy;
+    CK(dalloc(c, &d_tab, tab.size()));
+    CK(dalloc(c, &d_dex, (size_t)pitch));
+    CK(dalloc(c, &d_dhx, (size_t)pitch));
+    CK(dalloc(c, &d_dey, (size_t)ny));
+    CK(dalloc(c, &d_dhy, (size_t)ny));
+    CK(cudaMemcpyAsync(d_tab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(d_dex, dex.data(), pitch * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(d_dhx, dhx.data(), pitch * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(d_dey, dey.data(), ny * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(d_dhy, dhy.data(), ny * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    h.cpml = d_tab; h.den_ex = d_dex; h.den_hx = d_dhx; h.den_ey = d_dey; h.den_hy = d_dhy;
+  }
+
+  // points by row: sources, Ez detectors, component detectors
+  {
+    struct Pt { int j, kind, i, idx; };
+    std::vector<Pt> pts;
+    for (int e = 0; e < s->n_src; ++e) pts.push_back({s->src[e].j, kPointSource, s->src[e].i, e});
+    for (int e = 0; e < s->n_det; ++e) pts.push_back({s->det[e].j, kPointDetEz, s->det[e].i, e});
+    for (int e = 0; e < s->n_comp; ++e) pts.push_back({s->comp[e].j, kPointDetComp, s->comp[e].i, e});
+    std::stable_sort(pts.begin(), pts.end(), [](const Pt& a, const Pt& b) {
+      if (a.j != b.j) return a.j < b.j;
+      if (a.kind != b.kind) return a.kind < b.kind;
+      return a.i < b.i;
+    });
+    std::vector<int> row_start(ny + 1, 0);
+    for (const Pt& p : pts) row_start[p.j + 1]++;
+    for (int j = 0; j < ny; ++j) row_start[j + 1] += row_start[j];
+    std::vector<int4> dp(std::max<size_t>(1, pts.size()));
+    for (size_t q = 0; q < pts.size(); ++q) dp[q] = make_int4(pts[q].i, pts[q].kind, pts[q].idx, 0);
+    int* d_rs;
+    int4* d_pts;
+    CK(dalloc(c, &d_rs, row_start.size()));
+    CK(dalloc(c, &d_pts, dp.size()));
+    CK(cudaMemcpyAsync(d_rs, row_start.data(), row_start.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(d_pts, dp.data(), dp.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    h.row_start = d_rs;
+    h.pts = d_pts;
+  }
+
+  // source waveform and DFT twiddle tables (FP64 on the device, once)
+  {
+    std::vector<float> env(s->n_steps + 1, 0.f);
+    const int nsrc = std::max(1, s->n_src);
+    std::vector<double> ph(nsrc, 0.0);
+    if (s->n_src > 0) {
+      for (int n = 0; n <= s->n_steps; ++n) env[n] = s->envelope[n];
+      for (int e = 0; e < s->n_src; ++e) ph[e] = s->src_phase_deg[e] / 360.0;
+    }
+    float* d_env;
+    double* d_ph;
+    float* d_val;
+    double2* d_tw = nullptr;
+    CK(dalloc(c, &d_env, env.size()));
+    CK(dalloc(c, &d_ph, ph.size()));
+    CK(dalloc(c, &d_val, (size_t)(s->n_steps + 1) * nsrc));
+    if (c->dft) CK(dalloc(c, &d_tw, (size_t)(s->n_steps + 1)));
+    CK(cudaMemcpyAsync(d_env, env.data(), env.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(d_ph, ph.data(), ph.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    const double beta_half = (s->f1 != s->f0) ? 0.5 * (s->f1 - s->f0) / s->t1 : 0.0;
+    const double src_pi = s->src_pi > 0 ? s->src_pi : kPi;
+    CK(build_source_tables(d_val, d_tw, d_env, d_ph, nsrc, s->n_steps, s->dt, s->src_scale, s->f0,
+                           beta_half, src_pi, s->dft_freq * s->dt, c->stream));
+    ++c->launches;
+    CK(cudaStreamSynchronize(c->stream));
+    h.src_val = d_val;
+    h.twiddle = d_tw;
+    h.n_src = nsrc;
+  }
+
+  // detector outputs
+  h.n_det = s->n_det;
+  h.n_comp = s->n_comp;
+  h.record = c->record;
+  if (c->record) {
+    CK(dalloc(c, &h.trace, (size_t)s->n_steps * std::max(1, s->n_det)));
+    CK(dalloc(c, &h.ctrace, (size_t)s->n_steps * std::max(1, s->n_comp) * 3));
+  }
+  if (c->dft) CK(dalloc(c, &h.dft, (size_t)s->n_det));
+
+  // wave-front tracker and line probe
+  if (s->n_rc > 0) {
+    c->n_rc = s->n_rc;
+    c->rc_j_cut = s->rc_j_cut;
+    c->rc_level = s->rc_level;
+    CK(dalloc(c, &c->d_rc_scan, (size_t)s->n_rc));
+    CK(dalloc(c, &c->d_rc_max, (size_t)s->n_rc));
+    CK(dalloc(c, &c->d_edge, (size_t)s->n_rc));
+    CK(dalloc(c, &c->d_spd, (size_t)s->n_steps * s->n_rc));
+    std::vector<float> e0(s->n_rc, s->rc_edge0);
+    CK(cudaMemcpyAsync(c->d_rc_scan, s->rc_scan_i, s->n_rc * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_rc_max, s->rc_max_i, s->n_rc * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_edge, e0.data(), s->n_rc * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  if (s->line_n > 0) {
+    c->line_n = s->line_n; c->line_i0 = s->line_i0; c->line_j = s->line_j;
+    c->line_first = s->line_first; c->line_last = s->line_last;
+    CK(dalloc(c, &c->d_line, (size_t)(s->line_last - s->line_first + 1) * s->line_n));
+  }
+
+  CK(dalloc(c, &c->d_shot, 1));
+  CK(cudaMemcpyAsync(c->d_shot, &h, sizeof(DevShot), cudaMemcpyHostToDevice, c->stream));
+  c->grid_warps = resident_warps(c->medium, device);
+  std::vector<int4> units = make_units(0, nx, ny, c->grid_warps);
+  c->n_units = (int)units.size();
+  CK(dalloc(c, &c->d_units, units.size()));
+  CK(cudaMemcpyAsync(c->d_units, units.data(), units.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                     c->stream));
+  CK(dalloc(c, &c->d_flag, 1));
+  CK(cudaStreamSynchronize(c->stream));
+#undef CK
+  *out = c;
+  return FDTD2D_OK;
+}
+
+int fdtd2d_run(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
+  if (!c) return FDTD2D_ERR_INVALID;
+  if (n_first != c->step + 1 || n_last < n_first - 1 || n_last > c->n_steps) return FDTD2D_ERR_RANGE;
+  cudaSetDevice(c->device);
+  for (int32_t n = n_first; n <= n_last; ++n) {
+    cudaError_t e = launch_step(c->d_shot, c->d_units, c->n_units, n, c->medium, c->grid_warps, c->stream);
+    if (e != cudaSuccess) return fail_cuda(c, e);
+    ++c->launches;
+    const float* ez_now = field_ptr(c->h, kEz, n & 1);
+    if (c->n_rc > 0) {
+      e = launch_rc(ez_now, c->pitch, c->ny, c->n_rc, c->d_rc_scan, c->d_rc_max, c->rc_j_cut,
+                    c->rc_level, c->d_edge, c->d_spd + (size_t)(n - 1) * c->n_rc, c->stream);
+      if (e != cudaSuccess) return fail_cuda(c, e);
+      ++c->launches;
+    }
+    if (c->line_n > 0 && n >= c->line_first && n <= c->line_last) {
+      e = launch_line(ez_now, c->pitch, c->line_j, c->line_i0, c->line_n,
+                      c->d_line + (size_t)(n - c->line_first) * c->line_n, c->stream);
+      if (e != cudaSuccess) return fail_cuda(c, e);
+      ++c->launches;
+    }
+    c->step = n;
+  }
+  return FDTD2D_OK;
+}
+
+int fdtd2d_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int fdtd2d_run_timed(fdtd2d_ctx* c, int32_t n_first, int32_t n_last, float* elapsed_ms) {
+  if (!c || !elapsed_ms) return FDTD2D_ERR_INVALID;
+  cudaSetDevice(c->device);
+  cudaEvent_t a, b;
+  cudaError_t e = cudaEventCreate(&a);
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  e = cudaEventCreate(&b);
+  if (e != cudaSuccess) {
+    cudaEventDestroy(a);
+    return fail_cuda(c, e);
+  }
+  e = cudaEventRecord(a, c->stream);
+  int rc = (e == cudaSuccess) ? fdtd2d_run(c, n_first, n_last) : fail_cuda(c, e);
+  if (rc == FDTD2D_OK) {
+    e = cudaEventRecord(b, c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(elapsed_ms, a, b);
+    if (e != cudaSuccess) rc = fail_cuda(c, e);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return rc;
+}
+
+double fdtd2d_stability(const fdtd2d_setup* s) {
+  if (!s || !(s->dx > 0) || !(s->dy > 0)) return -1;
+  const double c0 = 2.99792458E8;
+  const double eps = 1.0 / (c0 * c0 * 4.0 * 3.14159265358979 * 1.0E-7);
+  double ne_max = 0;
+  if (s->medium == FDTD2D_MEDIUM_UNIFORM) {
+    if (s->ne)
+      for (int64_t k = 0; k < (int64_t)s->nx * s->ny; ++k) ne_max = std::max(ne_max, (double)s->ne[k]);
+  } else if (s->mat_ne) {
+    for (int m = 0; m < s->n_materials; ++m) ne_max = std::max(ne_max, (double)s->mat_ne[m]);
+  }
+  const double wp2 = s->jz_coef * ne_max / eps;
+  const double cdt = c0 * s->dt;
+  return cdt * cdt * (1.0 / (s->dx * s->dx) + 1.0 / (s->dy * s->dy)) + wp2 * s->dt * s->dt / 4.0;
+}
+
+int fdtd2d_synchronize(fdtd2d_ctx* c) {
+  if (!c) return FDTD2D_ERR_INVALID;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  return FDTD2D_OK;
+}
+
+int fdtd2d_current_step(const fdtd2d_ctx* c, int32_t* n) {
+  if (!c || !n) return FDTD2D_ERR_INVALID;
+  *n = c->step;
+  return FDTD2D_OK;
+}
+
+int fdtd2d_read_traces(fdtd2d_ctx* c, int32_t n0, int32_t n1, float* det_ez, float* comp_ez,
+                       float* comp_hx, float* comp_hy) {
+  if (!c) return FDTD2D_ERR_INVALID;
+  if (!c->record) return FDTD2D_ERR_STATE;
+  if (n0 < 1 || n1 < n0 || n1 > c->n_steps) return FDTD2D_ERR_RANGE;
+  cudaSetDevice(c->device);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  const size_t rows = (size_t)(n1 - n0 + 1);
+  if (det_ez && c->n_det > 0) {
+    e = cudaMemcpy(det_ez, c->h.trace + (size_t)(n0 - 1) * c->n_det, rows * c->n_det * 4,
+                   cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail_cuda(c, e);
+  }
+  if ((comp_ez || comp_hx || comp_hy) && c->n_comp > 0) {
+    std::vector<float> buf(rows * c->n_comp * 3);
+    e = cudaMemcpy(buf.data(), c->h.ctrace + (size_t)(n0 - 1) * c->n_comp * 3, buf.size() * 4,
+                   cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail_cuda(c, e);
+    for (size_t r = 0; r < rows * c->n_comp; ++r) {
+      if (comp_ez) comp_ez[r] = buf[r * 3 + 0];
+      if (comp_hx) comp_hx[r] = buf[r * 3 + 1];
+      if (comp_hy) comp_hy[r] = buf[r * 3 + 2];
+    }
+  }
+  return FDTD2D_OK;
+}
+
+int fdtd2d_read_dft(fdtd2d_ctx* c, double* re, double* im) {
+  if (!c || !re || !im) return FDTD2D_ERR_INVALID;
+  if (!c->dft) return FDTD2D_ERR_STATE;
+  cudaSetDevice(c->device);
+  std::vector<double2> buf(c->n_det);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(buf.data(), c->h.dft, c->n_det * sizeof(double2), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  for (int k = 0; k < c->n_det; ++k) {
+    re[k] = buf[k].x;
+    im[k] = buf[k].y;
+  }
+  return FDTD2D_OK;
+}
+
+int fdtd2d_read_rc(fdtd2d_ctx* c, int32_t n0, int32_t n1, int32_t* spd) {
+  if (!c || !spd) return FDTD2D_ERR_INVALID;
+  if (c->n_rc <= 0) return FDTD2D_ERR_STATE;
+  if (n0 < 1 || n1 < n0 || n1 > c->n_steps) return FDTD2D_ERR_RANGE;
+  cudaSetDevice(c->device);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(spd, c->d_spd + (size_t)(n0 - 1) * c->n_rc, (size_t)(n1 - n0 + 1) * c->n_rc * 4,
+                   cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  return FDTD2D_OK;
+}
+
+int fdtd2d_read_line(fdtd2d_ctx* c, int32_t n0, int32_t n1, float* out) {
+  if (!c || !out) return FDTD2D_ERR_INVALID;
+  if (c->line_n <= 0) return FDTD2D_ERR_STATE;
+  if (n0 < c->line_first || n1 < n0 || n1 > c->line_last) return FDTD2D_ERR_RANGE;
+  cudaSetDevice(c->device);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(out, c->d_line + (size_t)(n0 - c->line_first) * c->line_n,
+                   (size_t)(n1 - n0 + 1) * c->line_n * 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  return FDTD2D_OK;
+}
+
+namespace {
+
+// Device pointer + geometry of a field in the reference layout.
+struct FieldView {
+  float* base;          // device
+  int64_t dpitch;       // elements
+  int rows, cols;       // reference layout
+  int64_t hpitch;       // host row stride (elements)
+};
+
+bool field_view(fdtd2d_ctx* c, int which, int buf, FieldView* v) {
+  const int nx = c->nx, ny = c->ny, P = c->npml;
+  const int64_t pitch = c->pitch;
+  const DevShot& h = c->h;
+  switch (which) {
+    case FDTD2D_FIELD_EZ: *v = {field_ptr(h, kEz, buf), pitch, ny, nx, nx}; return true;
+    case FDTD2D_FIELD_JZ: *v = {field_ptr(h, kJz, buf), pitch, ny, nx, nx}; return true;
+    case FDTD2D_FIELD_HX: *v = {field_ptr(h, kHx, buf), pitch, ny - 1, nx, nx}; return true;
+    case FDTD2D_FIELD_HY: *v = {field_ptr(h, kHy, buf), pitch, ny, nx - 1, nx - 1}; return true;
+    default: break;
+  }
+  float* ps = h.psi + buf * h.psi_buf;
+  switch (which) {
+    case FDTD2D_FIELD_PSI_EZX_1: *v = {ps + h.o_ezx, P, ny, P, P}; return true;
+    case FDTD2D_FIELD_PSI_EZX_2: *v = {ps + h.o_ezx + (int64_t)ny * P, P, ny, P, P}; return true;
+    case FDTD2D_FIELD_PSI_HYX_1: *v = {ps + h.o_hyx, P, ny, P - 1, P - 1}; return true;
+    case FDTD2D_FIELD_PSI_HYX_2: *v = {ps + h.o_hyx + (int64_t)ny * P, P, ny, P - 1, P - 1}; return true;
+    case FDTD2D_FIELD_PSI_EZY_1: *v = {ps + h.o_ezy, pitch, P, nx, nx}; return true;
+    case FDTD2D_FIELD_PSI_EZY_2: *v = {ps + h.o_ezy + (int64_t)P * pitch, pitch, P, nx, nx}; return true;
+    case FDTD2D_FIELD_PSI_HXY_1: *v = {ps, pitch, P - 1, nx, nx}; return true;
+    case FDTD2D_FIELD_PSI_HXY_2: *v = {ps + (int64_t)(P - 1) * pitch, pitch, P - 1, nx, nx}; return true;
+    default: return false;
+  }
+}
+
+}  // namespace
+
+int fdtd2d_read_field(fdtd2d_ctx* c, int which, float* host) {
+  if (!c || !host) return FDTD2D_ERR_INVALID;
+  FieldView v;
+  if (!field_view(c, which, c->step & 1, &v)) return FDTD2D_ERR_INVALID;
+  cudaSetDevice(c->device);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2D(host, v.hpitch * 4, v.base, v.dpitch * 4, (size_t)v.cols * 4, v.rows,
+                     cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  return FDTD2D_OK;
+}
+
+int fdtd2d_write_field(fdtd2d_ctx* c, int which, const float* host) {
+  if (!c || !host) return FDTD2D_ERR_INVALID;
+  cudaSetDevice(c->device);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+    FieldView v;
+    if (!field_view(c, which, b, &v)) return FDTD2D_ERR_INVALID;
+    e = cudaMemcpy2D(v.base, v.dpitch * 4, host, v.hpitch * 4, (size_t)v.cols * 4, v.rows,
+                     cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  return FDTD2D_OK;
+}
+
+int fdtd2d_check_finite(fdtd2d_ctx* c) {
+  if (!c) return FDTD2D_ERR_INVALID;
+  cudaSetDevice(c->device);
+  const int b = c->step & 1;
+  const int64_t cells = (int64_t)c->pitch * c->ny;
+  cudaError_t e = cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream);
+  const float* arrs[4] = {field_ptr(c->h, kEz, b), field_ptr(c->h, kHx, b), field_ptr(c->h, kHy, b),
+                          field_ptr(c->h, kJz, b)};
+  for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
+    e = launch_nonfinite(arrs[k], cells, c->d_flag, c->stream);
+    ++c->launches;
+  }
+  int flag = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  return flag ? FDTD2D_ERR_NONFINITE : FDTD2D_OK;
+}
+
+int fdtd2d_destroy(fdtd2d_ctx* c) {
+  if (!c) return FDTD2D_ERR_INVALID;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return FDTD2D_OK;
+}
+
+int64_t fdtd2d_launch_count(const fdtd2d_ctx* c) { return c ? c->launches : -1; }
+
+int fdtd2d_last_cuda_error(const fdtd2d_ctx* c) { return c ? c->last_cuda : -1; }
+
+}  // extern "C"

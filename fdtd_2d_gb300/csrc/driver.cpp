@@ -1,0 +1,297 @@
+// Drop-in program driver: Settings.ini in, the reference's output files out.
+//
+// Restates main -> initlimits (FDTD_2D_Full/FDTD_cuda.cu:20, 384-441) and the
+// host side of DevFieldCalculation (FDTD_2D_Full/kernel.cu:1928-2818) on top
+// of the C ABI: the time loop runs on the GPU through fdtd2d_run, and the
+// files are written with the reference's formats:
+//
+//   Detect.txt        kernel.cu:2409-2421  "%lf\t%12lf\t%12lf\n " per step row;
+//                     the third conversion has no argument in the reference
+//                     (undefined output); this driver prints 0.
+//   detAll.txt        kernel.cu:2432-2454  time in us, 6 component sums x1000
+//   detEz/Hx/Hy.txt   kernel.cu:2456-2493  per-element samples x1000
+//   Ez.txt            kernel.cu:2173-2303  slices every TimeSieve steps
+//   FieldSaveDat.txt  kernel.cu:3041-3051
+//   SourceP.txt       FDTD_cuda.cu:3647-3650
+//   RcDet_data.txt    FDTD_cuda.cu:3492-3537
+//   deb.txt           kernel.cu:2681-2751 (ID3 map dump)
+//   iniLOG.txt, log.txt
+//
+// Sample rows follow the reference: row i of every trace file is the sample
+// taken at step i (row 0 is all zeros, the step-nMax sample is never printed).
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <ctime>
+#include <string>
+#include <vector>
+
+#include "../../include/fdtd2d.h"
+#include "problem.h"
+
+namespace fdtd2d {
+Problem* problem_internal(fdtd2d_problem* p);
+int rc_run_and_write(fdtd2d_ctx* ctx, const Problem& p, const std::string& dir, int32_t n_last,
+                     std::vector<int>* spd_rows);
+int processing_run(const Problem& p, const std::vector<std::vector<float>>& field,
+                   const std::string& dir);
+}  // namespace fdtd2d
+
+using namespace fdtd2d;
+
+namespace {
+
+struct File {
+  FILE* f = nullptr;
+  File(const std::string& path, const char* mode) { f = std::fopen(path.c_str(), mode); }
+  ~File() {
+    if (f) std::fclose(f);
+  }
+  explicit operator bool() const { return f != nullptr; }
+};
+
+std::string join(const std::string& dir, const char* name) {
+  if (dir.empty()) return name;
+  return dir + "/" + name;
+}
+
+void now_strings(char* tbuf, char* dbuf) {
+  std::time_t t = std::time(nullptr);
+  std::tm tm{};
+  localtime_r(&t, &tm);
+  std::strftime(tbuf, 64, "%H:%M:%S", &tm);
+  std::strftime(dbuf, 64, "%m/%d/%y", &tm);
+}
+
+// logINIread (FDTD_2D_Full/FDTD_cuda.cu:178-303): echo of the raw parameters.
+void write_ini_log(const std::string& dir, const IniParams& r) {
+  File f(join(dir, "iniLOG.txt"), "a");
+  if (!f) return;
+  char tb[64], db[64];
+  now_strings(tb, db);
+  std::fprintf(f.f, "Config loaded from 'Settings.ini' on time %s date %s:\nHardware:\n GPU_device=%d\nRegimes: \n SourceToDetect=%d\nGrid param: \n Use_Exp_time=%d\n Imax=%d\n Jmax=%d\n Max_time=%d\n Exp_time=%g\n ds=%g\n dt_coef=%g\n Isource=%d\n Jsource=%d\n Idetect=%d\n Jdetect=%d\n",
+               tb, db, r.gpu_device, r.s2d, r.exp_time_key, r.imax, r.jmax, r.n_max, r.exp_time, r.ds,
+               r.dt_coef, r.src_i, r.src_j, r.det_i, r.det_j);
+  std::fprintf(f.f, "AESA\n SIsize=%d\n SAutoDelta=%d\n SIdelta=%d\n SPAngle=%g\n DIsize=%d\n DAutoDelta=%d\n DIdelta=%d\nPulseParam:\n Chirp=%d\n FreqA=%g\n FreqB=%g\n Fronts=%d\n Plato=%d\n Fronts_ns=%g\n Plato_ns=%g\n Pulse_amp=%g\n2Dsave:\n From=%d\n To=%d\n TimeSieve=%d\n GridSieve=%d\nmedium:\n Build=%d\n Icen=%d\n Jcen=%d\n\n A=%g\n B=%g\n C=%g\n P=%d\n Q=%d\n N=%d\n\n Radius=%d\n Alpha=%g\n Beta=%g\n ne0=%g\n neA=%g\nmediumFluc:\n FlucBuild=%d\n FlucIcen=%d\n FlucJcen=%d\n\n FlucA=%g\n FlucB=%g\n FlucC=%g\n FlucP=%d\n FlucQ=%d\n FlucN=%d\n\n FlucAngleI=%g\n FlucAngleJ=%g\n FlucAngleK=%g\n FlucSign=%d\n\n FlucRadius=%d\n FlucAlpha=%g\n FlucBeta=%g\n FlucNe0=%g\n TorusBR=%d\nKameraConf:\n Draw2D=%d\n 2Dpreset=%d\n PatrubokL=%d\n DrawWall=%d\n WallPos=%d\n\nRC_calc:\n Iline=%d\n LIsize=%d\n LIdelta=%d\n FilterWindow=%d\n Rlevel=%g\n",
+               r.s_pi, r.s_delta_auto, r.s_di, r.s_angle, r.d_pi, r.d_delta_auto, r.d_di, r.chirp,
+               r.freq_a, r.freq_b, r.fronts, r.plato, r.fronts_ns, r.plato_ns, r.amp, r.save_from,
+               r.save_to, r.save_time_sieve, r.save_grid_sieve, r.build_medium, r.med_i, r.med_j,
+               r.sph_a, r.sph_b, r.sph_c, r.sph_p, r.sph_q, r.sph_n, r.eq_r, r.eq_alpha, r.eq_beta,
+               r.eq_ne0, r.eq_nea, r.fluc_build, r.fluc_i, r.fluc_j, r.fluc_a, r.fluc_b, r.fluc_c,
+               r.fluc_p, r.fluc_q, r.fluc_n, r.fluc_angle_i, r.fluc_angle_j, r.fluc_angle_k,
+               r.fluc_sign, r.fluc_r, r.fluc_alpha, r.fluc_beta, r.fluc_ne0, r.torus_br, r.draw2d,
+               r.preset, r.patrubok, r.draw_wall, r.wall_pos, r.rc_i, r.rc_size, r.rc_delta,
+               r.rc_window, r.rc_level);
+  std::fprintf(f.f, "\nProcessing:\n Perform=%d\n SecDer=%d\n SDFType=%d\n SDFWin=%d\n SDFRuns=%d\n CF=%d\n CFTau=%d\n CFK=%g\n ARC=%d\n ARCTau=%d\n ARCK=%g\n TauThreshold=%g\n FilterType=%d\n FilterWin=%d\n FilterRuns=%d\n SaveFiltered=%d\n SaveOriginal=%d\n PosI=%d\n PosJ=%d\n PosK=%d\n SizeI=%d\n BeginAfter=%d\n FinishAt=%d\n TimeSieve=%d\n DimSieve=%d\n SimDetect=%d\n DetSave=%d\n DetSize=%d\n DetWLoad=%d\n-----------------------------------------------------------------------------\n",
+               r.p_perform, r.p_sec_der, r.p_sdf_type, r.p_sdf_win, r.p_sdf_runs, r.p_cf, r.p_cf_tau,
+               r.p_cf_k, r.p_arc, r.p_arc_tau, r.p_arc_k, r.p_tau_threshold, r.p_filter_type,
+               r.p_filter_win, r.p_filter_runs, r.p_save_filtered, r.p_save_original, r.p_pos_i,
+               r.p_pos_j, r.p_pos_k, r.p_size_i, r.p_begin_after, r.p_finish_at, r.p_time_sieve,
+               r.p_dim_sieve, r.p_sim_detect, r.p_save_detector, r.p_detector_size,
+               r.p_load_weights);
+}
+
+}  // namespace
+
+extern "C" int fdtd2d_run_settings(const char* ini_path, const char* out_dir, int device) {
+  if (!ini_path) return FDTD2D_ERR_INVALID;
+  const std::string dir = out_dir ? out_dir : "";
+  const auto t_start = std::chrono::steady_clock::now();
+  IniParams raw;
+  std::string log;
+  int rc = parse_ini(ini_path, raw, log);
+  if (rc) return rc;
+  write_ini_log(dir, raw);
+
+  fdtd2d_problem* handle = nullptr;
+  rc = fdtd2d_problem_from_ini(ini_path, &handle);
+  if (rc) return rc;
+  Problem& p = *problem_internal(handle);
+  const IniParams& ip = p.ini;
+  const fdtd2d_setup& s = p.s;
+  const int nx = s.nx, ny = s.ny, nmax = s.n_steps;
+  if (ip.s2d == 1) {
+    // SourceToDetect runs the shot twice (vacuum, then with objects) and
+    // writes the differences; provided by the batched driver, not here.
+    fdtd2d_problem_free(handle);
+    return FDTD2D_ERR_CONFIG;
+  }
+
+  // SourceP.txt, RcDet_data.txt (written during setup by the reference)
+  {
+    File f(join(dir, "SourceP.txt"), "w");
+    if (!f) { fdtd2d_problem_free(handle); return FDTD2D_ERR_IO; }
+    for (int k = 0; k < nmax; ++k) std::fprintf(f.f, "%f\n", p.source_p[k]);
+    File r(join(dir, "RcDet_data.txt"), "w");
+    if (r) {
+      for (int v : p.rc_array_i) std::fprintf(r.f, "%d ", v);
+      std::fprintf(r.f, "\n0 ");
+    }
+  }
+
+  fdtd2d_ctx* ctx = nullptr;
+  rc = fdtd2d_create(&s, device, &ctx);
+  if (rc) {
+    fdtd2d_problem_free(handle);
+    return rc;
+  }
+
+  File pEz(join(dir, "Ez.txt"), "w");
+  File pEx(join(dir, "Ex.txt"), "wb"), pEy(join(dir, "Ey.txt"), "wb");
+  File pHx(join(dir, "Hx.txt"), "w"), pHy(join(dir, "Hy.txt"), "w"), pHz(join(dir, "Hz.txt"), "w");
+  if (!pEz) {
+    fdtd2d_destroy(ctx);
+    fdtd2d_problem_free(handle);
+    return FDTD2D_ERR_IO;
+  }
+  // Step loop with the reference's slice-save cadence (kernel.cu:2173-2303):
+  // inside [From, To] a counter runs 1..TimeSieve and a slice is written when
+  // it reaches TimeSieve.
+  std::vector<float> ez((size_t)nx * ny);
+  int save_counter = 0, save_app = 1;
+  int32_t done = 0;
+  const int sieve = ip.save_grid_sieve > 0 ? ip.save_grid_sieve : 1;
+  for (int n = 1; n <= nmax && rc == FDTD2D_OK; ++n) {
+    bool save = false;
+    if (n >= ip.save_from && n <= ip.save_to) {
+      if (save_app == ip.save_time_sieve) {
+        save = true;
+        save_app = 1;
+      } else {
+        save_app++;
+      }
+    }
+    if (!save && n < nmax) continue;
+    rc = fdtd2d_run(ctx, done + 1, n);
+    done = n;
+    if (rc || !save) continue;
+    rc = fdtd2d_read_field(ctx, FDTD2D_FIELD_EZ, ez.data());
+    if (rc) break;
+    save_counter++;
+    for (int i = 1; i < nx - 1; i += sieve) {
+      for (int j = 1; j < ny - 1; j += sieve) std::fprintf(pEz.f, "%12f ", ez[(size_t)j * nx + i]);
+      std::fputc('\n', pEx.f);
+      std::fputc('\n', pEz.f);
+      std::fputc('\n', pHx.f);
+      std::fputc('\n', pHy.f);
+      std::fputc('\n', pHz.f);
+    }
+  }
+  if (rc == FDTD2D_OK) rc = fdtd2d_synchronize(ctx);
+
+  if (rc == FDTD2D_OK) {
+    // FieldSaveDat.txt (VriteSaveParameters)
+    File f(join(dir, "FieldSaveDat.txt"), "w");
+    int count_m = 0;
+    for (int i = 1; i < nx - 1; i += sieve) count_m++;
+    if (f) std::fprintf(f.f, "%d %d", count_m, save_counter);
+  }
+
+  // Detector files.  traces are [step-1][element]; output row i = step i.
+  const int nd = s.n_det, nc = s.n_comp;
+  std::vector<float> det((size_t)nmax * nd), cez((size_t)nmax * nc), chx((size_t)nmax * nc),
+      chy((size_t)nmax * nc);
+  if (rc == FDTD2D_OK)
+    rc = fdtd2d_read_traces(ctx, 1, nmax, det.data(), cez.data(), chx.data(), chy.data());
+  if (rc == FDTD2D_OK) {
+    File pDet(join(dir, "Detect.txt"), "w");
+    File pAll(join(dir, "detAll.txt"), "w");
+    File pdEz(join(dir, "detEz.txt"), "w"), pdHx(join(dir, "detHx.txt"), "w"),
+        pdHy(join(dir, "detHy.txt"), "w"), pdP(join(dir, "detP.txt"), "w");
+    File e1(join(dir, "detEx.txt"), "w"), e2(join(dir, "detEy.txt"), "w"), e3(join(dir, "detHz.txt"), "w");
+    File e4(join(dir, "DifDetEx.txt"), "w"), e5(join(dir, "CompDetect.txt"), "w");
+    File e6(join(dir, "LineDetect.txt"), "w"), e7(join(dir, "LineDetect2.txt"), "w");
+    File e8(join(dir, "test.txt"), "w"), e9(join(dir, "SDetect.txt"), "w");
+    if (!pDet || !pAll || !pdEz || !pdHx || !pdHy) rc = FDTD2D_ERR_IO;
+    for (int i = 0; i < nmax && rc == FDTD2D_OK; ++i) {
+      double sum = 0;
+      if (i > 0)
+        for (int k = 0; k < nd; ++k) sum += det[(size_t)(i - 1) * nd + k];
+      std::fprintf(pDet.f, "%lf\t%12lf\t%12lf\n ", (s.dt * i) * 1e12, sum * 1000, 0.0);
+      double s3 = 0, s4 = 0, s5 = 0;
+      if (i > 0)
+        for (int k = 0; k < nc; ++k) {
+          s3 += cez[(size_t)(i - 1) * nc + k];
+          s4 += chx[(size_t)(i - 1) * nc + k];
+          s5 += chy[(size_t)(i - 1) * nc + k];
+        }
+      std::fprintf(pAll.f, "%lf\t%12lf\t%12lf\t%12lf\t%12lf\t%12lf\t%12lf\n ", (s.dt * i) * 1000000,
+                   0.0, 0.0, s3 * 1000, s4 * 1000, s5 * 1000, 0.0);
+      for (int k = 0; k < nc; ++k) {
+        const float vez = i > 0 ? cez[(size_t)(i - 1) * nc + k] : 0.f;
+        const float vhx = i > 0 ? chx[(size_t)(i - 1) * nc + k] : 0.f;
+        const float vhy = i > 0 ? chy[(size_t)(i - 1) * nc + k] : 0.f;
+        std::fprintf(pdEz.f, "%12lf\t", (double)vez * 1000);
+        std::fprintf(pdHx.f, "%12lf\t", (double)vhx * 1000);
+        std::fprintf(pdHy.f, "%12lf\t", (double)vhy * 1000);
+        std::fputc('\n', pdEz.f);
+        std::fputc('\n', pdHx.f);
+        std::fputc('\n', pdHy.f);
+        if (pdP) std::fputc('\n', pdP.f);
+      }
+      std::fputc('\n', pdEz.f);
+      std::fputc('\n', pdHx.f);
+      std::fputc('\n', pdHy.f);
+      if (pdP) std::fputc('\n', pdP.f);
+    }
+  }
+
+  // Wave-front tracker outputs (RC_Line.txt, TAU_Line.txt).
+  if (rc == FDTD2D_OK) rc = rc_run_and_write(ctx, p, dir, nmax, nullptr);
+  // TOF processing on the saved line (processing_core, FDTD_2D_Full/kernel.cu:2313).
+  if (rc == FDTD2D_OK && ip.p_perform) {
+    const int first = ip.p_begin_after + 1;
+    const int last = std::min(ip.p_finish_at, nmax);
+    const int times = std::max(0, last - first + 1);
+    std::vector<std::vector<float>> field(times, std::vector<float>(std::max(0, ip.p_size_i), 0.f));
+    if (s.line_n > 0) {
+      std::vector<float> buf((size_t)times * s.line_n);
+      rc = fdtd2d_read_line(ctx, s.line_first, s.line_last, buf.data());
+      for (int t = 0; t < times && rc == FDTD2D_OK; ++t)
+        for (int c = 0; c < s.line_n; ++c) field[t][p.line_offset + c] = buf[(size_t)t * s.line_n + c];
+    }
+    if (rc == FDTD2D_OK) rc = processing_run(p, field, dir);
+  }
+
+  const double secs =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  if (rc == FDTD2D_OK) {
+    File f(join(dir, "log.txt"), "a");
+    if (f) {
+      char tb[64], db[64];
+      now_strings(tb, db);
+      std::fprintf(f.f, "-------------------------------------------------------------------------\n");
+      std::fprintf(f.f, "OS date:\t\t\t\t%s\n", db);
+      std::fprintf(f.f, "OS time:\t\t\t\t%s\n", tb);
+      std::fprintf(f.f, "-------------------------------------------------------------------------\n");
+      std::fprintf(f.f,
+                   "NET PARAMETERS \n Ex(%d, %d, %d) \n Ey(%d, %d, %d) \n Ez(%d, %d, %d) \n Hx(%d, %d, %d) \n Hy(%d, %d, %d) \n Hz(%d, %d, %d)\n\n(dx ,dy, dz) - dt: (%f mm, %f mm, %f mm) - %f ns\n",
+                   nx - 1, ny, 0, nx, ny - 1, 0, nx, ny, 1, nx, ny - 1, 1, nx - 1, ny, 1, nx - 1, ny - 1, 0,
+                   ip.dx * 1000, ip.dy * 1000, ip.dz * 1000, s.dt * 1e9);
+      std::fprintf(f.f, "\nSIMULATION PARAMETERS\n Total Simulation time: %d time steps or %e seconds\n", nmax,
+                   nmax * s.dt);
+      std::fprintf(f.f,
+                   "\nSAVE DATA PARAMETER\nSlises saved: %d\nData saved from time %d to time %d \nTime sieve parameter: %d \nNet sieve parameter: %d\nData multiplier: %f\n",
+                   save_counter, ip.save_from, ip.save_to, ip.save_time_sieve, ip.save_grid_sieve, 1.0);
+      std::fprintf(f.f,
+                   "\nSORCE AND DETECTOR\n Source point: (%d, %d, %d)\n Detector point(%d, %d, %d)\n Detector size: %dx%d points",
+                   ip.src_i, ip.src_j, ip.src_k, ip.det_i, ip.det_j, ip.det_k, 10, 10);
+      std::fprintf(f.f, "\n\nCalculation on GPU\n Calculation time: %f seconds\n\n", secs);
+    }
+    // deb.txt: the Ez material map, rows i, columns j (kernel.cu:2737-2751)
+    File d(join(dir, "deb.txt"), "w");
+    File m(join(dir, "materials.txt"), "w");
+    if (d) {
+      for (int i = 1; i < nx - 1; i++) {
+        for (int j = 1; j < ny - 1; j++) std::fprintf(d.f, "%d ", p.id3[(size_t)j * nx + i]);
+        std::fprintf(d.f, "\n");
+      }
+      std::fprintf(d.f, "\n\n");
+      std::fprintf(d.f, "\n\n");
+    }
+  }
+  fdtd2d_destroy(ctx);
+  fdtd2d_problem_free(handle);
+  return rc;
+}

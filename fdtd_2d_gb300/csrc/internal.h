@@ -1,0 +1,118 @@
+// Device-side description of one shot and the launch helpers shared by the
+// step kernels and the C-ABI layer.  Host code fills DevShot once per shot and
+// keeps an array of them in device memory; the kernels read it through a
+// const pointer so one launch can advance many shots (the batched form).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fdtd2d {
+
+// Point kinds in the per-row point table.  Within a row the table is sorted
+// by (kind, column) so every source of a row is applied before any detector
+// reads the cell, matching the reference order source -> detectors
+// (FDTD_2D_Full/kernel.cu:2134, 2151-2157).
+enum PointKind : int { kPointSource = 0, kPointDetEz = 1, kPointDetComp = 2 };
+
+// Packed CPML table rows (each row has npml floats; H rows use npml-1).
+enum CpmlRow : int {
+  kBeX1 = 0, kCeX1, kBeX2, kCeX2, kBhX1, kChX1, kBhX2, kChX2,
+  kBeY1, kCeY1, kBeY2, kCeY2, kBhY1, kChY1, kBhY2, kChY2, kCpmlRows
+};
+
+// Material-ID medium: per-material coefficients for the Ez cell (ID3) and the
+// H cells (ID1 for Hx, ID2 for Hy).  kp is the Jz drive coefficient
+// beta*ne; pec marks material 1 (FDTD_2D_Full/kernel.cu:435).
+struct MatE { float ca, cb, kp, pec; };
+struct MatH { float da, db; };
+
+struct DevShot {
+  int nx, ny, pitch, npml;
+  int n_steps;
+  int base_n;                 // global step offset (batched/serving shots)
+  float ca, cb, da, db;       // uniform medium coefficients
+  float ja;                   // Jz decay (1 - nu dt/2)/(1 + nu dt/2)
+  float dx, dy;               // the float dx, dy the reference passes to the psi kernels
+
+  const float* kp;            // [ny][pitch] Jz drive beta*ne (uniform medium), may be null
+  const uint8_t* id1;         // [ny][pitch] material ids (material medium)
+  const uint8_t* id2;
+  const uint8_t* id3;
+  const MatE* mat_e;          // [256]
+  const MatH* mat_h;          // [256]
+
+  // Field slab [4 fields (Ez, Hx, Hy, Jz)][2 ping-pong buffers][ny][pitch]:
+  // field f, buffer b starts at fld + (2*f + b)*cells.
+  float* fld;
+  int64_t cells;
+  // CPML psi slab [2 ping-pong buffers][psi_buf]; within a buffer (side s = 0
+  // low edge, 1 high edge):
+  //   o_hxy: [s][r][pitch]  r in [0,P-2]   (Hx, y strips)
+  //   o_ezy: [s][r][pitch]  r in [0,P-1]   (Ez, y strips; r = 0 unused)
+  //   o_hyx: [s][j][P]      r in [0,P-2]   (Hy, x strips)
+  //   o_ezx: [s][j][P]      r in [0,P-1]   (Ez, x strips; r = 0 unused)
+  float* psi;
+  int64_t psi_buf, o_ezy, o_hyx, o_ezx;   // o_hxy = 0
+  const float* cpml;          // [kCpmlRows][P]
+  const float* den_ex;        // [pitch] (entries >= nx-1 are zero)
+  const float* den_hx;        // [pitch]
+  const float* den_ey;        // [ny]
+  const float* den_hy;        // [ny]
+
+  // sources and detectors, by row
+  const int* row_start;       // [ny+1] offsets into pts
+  const int4* pts;            // (col, kind, element index, 0)
+  // Source waveform s_e(n) and DFT twiddles are tabulated per step by
+  // build_source_tables (FP64 math, once per shot) so the step kernel does no
+  // transcendental work.
+  const float* src_val;       // [n_steps+1][n_src]
+  const double2* twiddle;     // [n_steps+1] (cos, sin)(2 pi f n dt)
+  int n_src;
+  int n_det, n_comp;
+  int record;
+  float* trace;               // [n_steps][n_det]
+  float* ctrace;              // [n_steps][n_comp][3]  (Ez, Hx, Hy)
+  double2* dft;               // [n_det]
+};
+
+enum FieldId : int { kEz = 0, kHx = 1, kHy = 2, kJz = 3 };
+
+__host__ __device__ inline float* field_ptr(const DevShot& S, int f, int b) {
+  return S.fld + (int64_t)(2 * f + b) * S.cells;
+}
+
+// A unit of work is one warp-wide column block (128 cells) of one shot over a
+// contiguous range of rows: (shot, i0, j0, j1).
+constexpr int kCols = 128;
+constexpr int kThreads = 256;
+
+// Launch the fused step for steps n (global numbering) of every shot listed
+// in `units`.  medium: 0 uniform, 1 material ids.
+cudaError_t launch_step(const DevShot* shots, const int4* units, int n_units,
+                        int n_global, int medium, int n_warps_grid,
+                        cudaStream_t stream);
+
+// Launch capacity: number of warps the step kernel keeps resident at once.
+int resident_warps(int medium, int device);
+
+// Tabulate s_e(n) = scale*env[n]*cos(2*pi_c*(beta/2 t^2 + f0 t + phase_e)),
+// t = n*dt, for n = 0..n_steps, and the DFT twiddles, in FP64.
+cudaError_t build_source_tables(float* src_val, double2* twiddle, const float* env,
+                                const double* phase_cycles, int n_src, int n_steps, double dt,
+                                double scale, double f0, double beta_half, double src_pi,
+                                double dft_fdt, cudaStream_t stream);
+
+// Wave-front tracker for one step: one CTA per line (see fdtd2d_setup.n_rc).
+cudaError_t launch_rc(const float* ez, int64_t pitch, int ny, int n_rc, const int* scan_i,
+                      const int* max_i, int j_cut, float level, float* edge, int* spd_row,
+                      cudaStream_t stream);
+
+// Copy n cells of row j starting at column i0 into dst.
+cudaError_t launch_line(const float* ez, int64_t pitch, int j, int i0, int n, float* dst,
+                        cudaStream_t stream);
+
+// Count non-finite values in n floats (atomic count into *flag).
+cudaError_t launch_nonfinite(const float* a, int64_t n, int* flag, cudaStream_t stream);
+
+}  // namespace fdtd2d

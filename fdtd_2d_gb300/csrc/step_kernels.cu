@@ -1,0 +1,582 @@
+// Fused TMz step for sm_103a: Hx/Hy (+CPML psi) -> Jz -> Ez (+CPML psi) ->
+// source -> detectors in ONE pass over HBM per step.
+//
+// The reference runs this as 8-12 launches per step (FDTD_2D_Full/kernel.cu
+// :2073-2157), each re-reading the fields: about 84 B of HBM traffic per cell
+// update.  Here each warp streams a 128-column block of one shot up a range
+// of rows.  Per row it reads Ez(j+1), Hx(j), Hy(j), Jz(j) and the plasma
+// coefficient once (float4 per lane, 512 B per warp per array, fully
+// coalesced) and writes Ez, Hx, Hy, Jz once: the 36 B/cell minimum.
+//
+// Neighbour values come from registers: Ez(j) and Hx_new(j-1) roll from the
+// previous row, Ez(i+1) and Hy_new(i-1) arrive by warp shuffle.  Only the warp
+// edges (lane 0's Hy_new(i0-1), lane 31's Ez(i0+128)) and the first row of a
+// unit (Hx_new(j0-1)) are recomputed from global memory; those reads hit L2.
+// Because a unit may recompute a neighbour-owned H value, every field is
+// ping-ponged (read buffer (n-1)&1, write n&1), so no unit ever sees a value
+// from the step it is computing.
+//
+// All update arithmetic goes through explicit-rounding intrinsics
+// (__fmaf_rn, __fmul_rn, ...), so the owner's value and a recomputed copy are
+// bit-identical whatever the surrounding code, and results do not depend on
+// how the grid is cut into units.
+#include "internal.h"
+
+#include <cstdio>
+
+namespace fdtd2d {
+
+// ---- update formulas (shared by the vector and the scalar paths) ----------
+
+// Hx = DA*Hx + DB*((Ez_a - Ez_b)*den)        FDTD_2D_Full/kernel.cu:192-193, 313-314
+__device__ __forceinline__ float upd_h(float da, float h, float db, float ea, float eb, float den) {
+  return __fmaf_rn(db, __fmul_rn(__fsub_rn(ea, eb), den), __fmul_rn(da, h));
+}
+
+// psi = b*psi + c*(a - b')/d                  FDTD_2D_Full/kernel.cu:226-227, 478-479
+__device__ __forceinline__ float upd_psi(float b, float psi, float c, float a, float a2, float d) {
+  return __fmaf_rn(b, psi, __fdiv_rn(__fmul_rn(c, __fsub_rn(a, a2)), d));
+}
+
+// Ez = CA*Ez + CB*(dHy*den_ex + dHx*den_ey - Jz)   FDTD_2D_Full/kernel.cu:444-446
+__device__ __forceinline__ float upd_e(float ca, float e, float cb, float dhy, float dex,
+                                       float dhx, float dey, float jz) {
+  const float curl = __fsub_rn(__fmaf_rn(dhy, dex, __fmul_rn(dhx, dey)), jz);
+  return __fmaf_rn(cb, curl, __fmul_rn(ca, e));
+}
+
+// Jz = ja*Jz + kp*Ez where the cell carries plasma (kp != 0), else unchanged.
+// At nu = 0, ja = 1 and kp = (e^2/m_e)*ne*dt: the reference's
+// Jz + D_CJ*Ez*NE*dt (FDTD_2D_Full/kernel.cu:156-157).
+__device__ __forceinline__ float upd_j(float ja, float jz, float kp, float ez) {
+  return kp != 0.f ? __fmaf_rn(kp, ez, __fmul_rn(ja, jz)) : jz;
+}
+
+__device__ __forceinline__ void ld4(float (&d)[4], const float* p) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+  d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+}
+__device__ __forceinline__ void ld4_nc(float (&d)[4], const float* p) {
+  // Streaming load of data read exactly once this step.
+  const float4 v = __ldcs(reinterpret_cast<const float4*>(p));
+  d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+}
+__device__ __forceinline__ void st4(float* p, const float (&d)[4]) {
+  *reinterpret_cast<float4*>(p) = make_float4(d[0], d[1], d[2], d[3]);
+}
+__device__ __forceinline__ void zero4(float (&d)[4]) { d[0] = d[1] = d[2] = d[3] = 0.f; }
+
+// Per-cell coefficients of one 4-cell row segment.  The uniform medium keeps
+// only the plasma drive per cell; everything else is a shot-wide scalar.
+template <int MEDIUM>
+struct MediumRow;
+
+template <>
+struct MediumRow<0> {
+  float da, db, ca, cb;
+  float kp[4];
+  __device__ __forceinline__ float dax(int) const { return da; }
+  __device__ __forceinline__ float dbx(int) const { return db; }
+  __device__ __forceinline__ float day(int) const { return da; }
+  __device__ __forceinline__ float dby(int) const { return db; }
+  __device__ __forceinline__ float cA(int) const { return ca; }
+  __device__ __forceinline__ float cB(int) const { return cb; }
+  __device__ __forceinline__ bool pec(int) const { return false; }
+  __device__ __forceinline__ void init(const DevShot& S) { da = S.da; db = S.db; ca = S.ca; cb = S.cb; }
+  __device__ __forceinline__ void load(const DevShot& S, const MatE*, const MatH*, int64_t off) {
+    if (S.kp) {
+      ld4_nc(kp, S.kp + off);
+    } else {
+      zero4(kp);
+    }
+  }
+};
+
+template <>
+struct MediumRow<1> {
+  float da_x[4], db_x[4], da_y[4], db_y[4], ca[4], cb[4], kp[4];
+  bool pe[4];
+  __device__ __forceinline__ float dax(int k) const { return da_x[k]; }
+  __device__ __forceinline__ float dbx(int k) const { return db_x[k]; }
+  __device__ __forceinline__ float day(int k) const { return da_y[k]; }
+  __device__ __forceinline__ float dby(int k) const { return db_y[k]; }
+  __device__ __forceinline__ float cA(int k) const { return ca[k]; }
+  __device__ __forceinline__ float cB(int k) const { return cb[k]; }
+  __device__ __forceinline__ bool pec(int k) const { return pe[k]; }
+  __device__ __forceinline__ void init(const DevShot&) {}
+  __device__ __forceinline__ void load(const DevShot& S, const MatE* mat_e, const MatH* mat_h, int64_t off) {
+    const uchar4 a = *reinterpret_cast<const uchar4*>(S.id1 + off);
+    const uchar4 b = *reinterpret_cast<const uchar4*>(S.id2 + off);
+    const uchar4 c = *reinterpret_cast<const uchar4*>(S.id3 + off);
+    const unsigned char ia[4] = {a.x, a.y, a.z, a.w};
+    const unsigned char ib[4] = {b.x, b.y, b.z, b.w};
+    const unsigned char ic[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const MatH hx = mat_h[ia[k]];
+      const MatH hy = mat_h[ib[k]];
+      const MatE e = mat_e[ic[k]];
+      da_x[k] = hx.da; db_x[k] = hx.db;
+      da_y[k] = hy.da; db_y[k] = hy.db;
+      ca[k] = e.ca; cb[k] = e.cb; kp[k] = e.kp; pe[k] = e.pec != 0.f;
+    }
+  }
+};
+
+// DB of one H cell (scalar path).
+template <int MEDIUM>
+__device__ __forceinline__ void h_coef(const DevShot& S, const MatH* mat_h, const uint8_t* ids,
+                                       int64_t off, float& da, float& db) {
+  if (MEDIUM == 0) {
+    da = S.da; db = S.db;
+  } else {
+    const MatH h = mat_h[ids[off]];
+    da = h.da; db = h.db;
+  }
+}
+
+// New Hy at one cell (c, j) from old values, CPML included.  Used for the
+// lane-0 halo value Hy_new(i0-1, j).  Reads only the old buffers.
+template <int MEDIUM>
+__device__ float hy_cell(const DevShot& S, const MatH* mat_h, int par, int c, int j,
+                         float ez_c, float ez_c1) {
+  const int64_t off = (int64_t)j * S.pitch + c;
+  float da, db;
+  h_coef<MEDIUM>(S, mat_h, S.id2, off, da, db);
+  const float hyo = field_ptr(S, kHy, par)[off];
+  float h = upd_h(da, hyo, db, ez_c1, ez_c, S.den_hx[c]);
+  const int P = S.npml;
+  int side = -1, r = 0;
+  if (c <= P - 2) { side = 0; r = c; }
+  else if (c >= S.nx - P && c <= S.nx - 2) { side = 1; r = S.nx - 2 - c; }
+  if (side >= 0) {
+    const float* tb = S.cpml + (side ? kBhX2 : kBhX1) * P;
+    const float* tc = S.cpml + (side ? kChX2 : kChX1) * P;
+    const float psi = S.psi[par * S.psi_buf + S.o_hyx + ((int64_t)side * S.ny + j) * P + r];
+    const float pn = upd_psi(tb[r], psi, tc[r], ez_c1, ez_c, S.dx);
+    h = __fmaf_rn(db, pn, h);
+  }
+  return h;
+}
+
+// One Hx row segment (i..i+3, j): bulk update + y-strip CPML.  `own` writes
+// the new psi (only the owning unit does).
+template <int MEDIUM>
+__device__ __forceinline__ void hx_row(const DevShot& S, const MediumRow<MEDIUM>& m, int par, int i, int j, const float (&ezj)[4],
+                                       const float (&ezj1)[4], const float (&hxo)[4],
+                                       float (&out)[4], bool own) {
+  const float den = S.den_hy[j];
+  const int nx = S.nx;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    out[k] = (i + k <= nx - 2) ? upd_h(m.dax(k), hxo[k], m.dbx(k), ezj[k], ezj1[k], den) : hxo[k];
+  }
+  const int P = S.npml;
+  int side = -1, r = 0;
+  if (j <= P - 2) { side = 0; r = j; }
+  else if (j >= S.ny - P) { side = 1; r = S.ny - 2 - j; }
+  if (side >= 0) {
+    const float b = S.cpml[(side ? kBhY2 : kBhY1) * P + r];
+    const float c = S.cpml[(side ? kChY2 : kChY1) * P + r];
+    const int64_t poff = ((int64_t)side * (P - 1) + r) * S.pitch + i;
+    float psi[4], pn[4];
+    ld4(psi, S.psi + par * S.psi_buf + poff);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      pn[k] = psi[k];
+      if (i + k <= nx - 2) {
+        pn[k] = upd_psi(b, psi[k], c, ezj[k], ezj1[k], S.dy);
+        out[k] = __fmaf_rn(m.dbx(k), pn[k], out[k]);
+      }
+    }
+    if (own) st4(S.psi + (par ^ 1) * S.psi_buf + poff, pn);
+  }
+}
+
+template <int MEDIUM>
+__device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e, const MatH* mat_h,
+                                             int i0, int j0, int j1, int n, int lane) {
+  const int nx = S.nx, ny = S.ny, P = S.npml;
+  const int64_t pitch = S.pitch;
+  const int par = (n - 1) & 1;
+  const float* __restrict__ ezo = field_ptr(S, kEz, par);
+  const float* __restrict__ hxo_p = field_ptr(S, kHx, par);
+  const float* __restrict__ hyo_p = field_ptr(S, kHy, par);
+  const float* __restrict__ jzo_p = field_ptr(S, kJz, par);
+  float* __restrict__ ezw = field_ptr(S, kEz, par ^ 1);
+  float* __restrict__ hxw = field_ptr(S, kHx, par ^ 1);
+  float* __restrict__ hyw = field_ptr(S, kHy, par ^ 1);
+  float* __restrict__ jzw = field_ptr(S, kJz, par ^ 1);
+  float* __restrict__ psr = S.psi + par * S.psi_buf;          // psi read buffer
+  float* __restrict__ psw = S.psi + (par ^ 1) * S.psi_buf;    // psi write buffer
+
+  const int i = i0 + 4 * lane;
+  const bool act = i < nx;
+  const int ic = act ? i : 0;  // clamp for address formation of inactive lanes
+
+  float dex[4], dhx[4];
+  ld4(dex, S.den_ex + ic);
+  ld4(dhx, S.den_hx + ic);
+
+  MediumRow<MEDIUM> m;
+  m.init(S);
+  float ezc[4], hxp[4];
+  zero4(ezc);
+  zero4(hxp);
+  if (act) ld4(ezc, ezo + (int64_t)j0 * pitch + ic);
+  if (j0 >= 1) {
+    // Hx_new(j0-1): recomputed from old values (the unit below owns it).
+    float ezp[4], hxo[4];
+    zero4(ezp); zero4(hxo);
+    if (act) {
+      ld4(ezp, ezo + (int64_t)(j0 - 1) * pitch + ic);
+      ld4(hxo, hxo_p + (int64_t)(j0 - 1) * pitch + ic);
+    }
+    m.load(S, mat_e, mat_h, (int64_t)(j0 - 1) * pitch + ic);
+    hx_row<MEDIUM>(S, m, par, ic, j0 - 1, ezp, ezc, hxo, hxp, false);
+  }
+
+  // Prefetched row j data.
+  float ezn[4], hxo[4], hyo[4], jzo[4];
+  zero4(ezn); zero4(hxo); zero4(hyo); zero4(jzo);
+  if (act) {
+    const int64_t o = (int64_t)j0 * pitch + ic;
+    ld4_nc(ezn, ezo + o + pitch);   // j0 + 1 <= ny - 1 always (units stop at ny-1)
+    ld4_nc(hxo, hxo_p + o);
+    ld4_nc(hyo, hyo_p + o);
+    ld4_nc(jzo, jzo_p + o);
+  }
+
+  for (int j = j0; j < j1; ++j) {
+    const int64_t o = (int64_t)j * pitch + ic;
+    m.load(S, mat_e, mat_h, o);
+
+    // Prefetch row j+1 (Ez of j+2) while row j is computed.
+    float ezn2[4], hxo2[4], hyo2[4], jzo2[4];
+    zero4(ezn2); zero4(hxo2); zero4(hyo2); zero4(jzo2);
+    if (act && j + 1 < j1) {
+      ld4_nc(ezn2, ezo + o + 2 * pitch);
+      ld4_nc(hxo2, hxo_p + o + pitch);
+      ld4_nc(hyo2, hyo_p + o + pitch);
+      ld4_nc(jzo2, jzo_p + o + pitch);
+    }
+
+    // ---- H update (Dev_HxCalc/Dev_HxPML_Jdir_Calc, Dev_HyCalc/Dev_HyPML_Idir_Calc)
+    float hxn[4];
+    hx_row<MEDIUM>(S, m, par, ic, j, ezc, ezn, hxo, hxn, true);
+
+    float ezr_next = __shfl_down_sync(0xffffffffu, ezc[0], 1);
+    if (lane == 31) {
+      const int c = i0 + kCols;
+      ezr_next = (c < nx) ? ezo[(int64_t)j * pitch + c] : 0.f;
+    }
+    const float ezr[4] = {ezc[1], ezc[2], ezc[3], ezr_next};
+    float hyn[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      hyn[k] = (i + k <= nx - 2) ? upd_h(m.day(k), hyo[k], m.dby(k), ezr[k], ezc[k], dhx[k]) : hyo[k];
+    }
+    // Hy x-strip CPML (edge columns only).
+    if (act && (i <= P - 2 || i + 3 >= nx - P)) {
+      float pn[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int c = i + k;
+        int side = -1, r = 0;
+        if (c <= P - 2) { side = 0; r = c; }
+        else if (c >= nx - P && c <= nx - 2) { side = 1; r = nx - 2 - c; }
+        if (side >= 0) {
+          const float b = S.cpml[(side ? kBhX2 : kBhX1) * P + r];
+          const float cc = S.cpml[(side ? kChX2 : kChX1) * P + r];
+          const int64_t po = S.o_hyx + ((int64_t)side * ny + j) * P + r;
+          pn[k] = upd_psi(b, psr[po], cc, ezr[k], ezc[k], S.dx);
+          hyn[k] = __fmaf_rn(m.dby(k), pn[k], hyn[k]);
+          psw[po] = pn[k];
+        }
+      }
+    }
+    float hyl = __shfl_up_sync(0xffffffffu, hyn[3], 1);
+    if (lane == 0) {
+      hyl = 0.f;
+      if (i0 >= 1) {
+        const float ezl = ezo[(int64_t)j * pitch + i0 - 1];
+        hyl = hy_cell<MEDIUM>(S, mat_h, par, i0 - 1, j, ezl, ezc[0]);
+      }
+    }
+
+    // ---- Jz (Dev_JzCalc) and Ez (Dev_EzCalc) on interior cells
+    const bool row_in = (j >= 1) && (j <= ny - 2);
+    const float dey = S.den_ey[j];
+    const float hyl4[4] = {hyl, hyn[0], hyn[1], hyn[2]};
+    float ezw4[4], jzw4[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int c = i + k;
+      const bool in = row_in && c >= 1 && c <= nx - 2;
+      jzw4[k] = in ? upd_j(S.ja, jzo[k], m.kp[k], ezc[k]) : jzo[k];
+      float e = ezc[k];
+      if (in) {
+        e = m.pec(k) ? 0.f
+                     : upd_e(m.cA(k), ezc[k], m.cB(k), __fsub_rn(hyn[k], hyl4[k]), dex[k],
+                             __fsub_rn(hxp[k], hxn[k]), dey, jzw4[k]);
+      }
+      ezw4[k] = e;
+    }
+    // Ez x-strip CPML (Dev_EzPML_Idir_Calc), then y-strip (Dev_EzPML_Jdir_Calc).
+    if (act && row_in && (i <= P - 1 || i + 3 >= nx - P)) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int c = i + k;
+        int side = -1, r = 0;
+        if (c >= 1 && c <= P - 1) { side = 0; r = c; }
+        else if (c >= nx - P && c <= nx - 2) { side = 1; r = nx - 1 - c; }
+        if (side >= 0) {
+          const float b = S.cpml[(side ? kBeX2 : kBeX1) * P + r];
+          const float cc = S.cpml[(side ? kCeX2 : kCeX1) * P + r];
+          const int64_t po = S.o_ezx + ((int64_t)side * ny + j) * P + r;
+          const float pn = upd_psi(b, psr[po], cc, hyn[k], hyl4[k], S.dx);
+          ezw4[k] = __fmaf_rn(m.cB(k), pn, ezw4[k]);
+          psw[po] = pn;
+        }
+      }
+    }
+    if (act && row_in && (j <= P - 1 || j >= ny - P)) {
+      const int side = (j <= P - 1) ? 0 : 1;
+      const int r = side ? (ny - 1 - j) : j;
+      const float b = S.cpml[(side ? kBeY2 : kBeY1) * P + r];
+      const float cc = S.cpml[(side ? kCeY2 : kCeY1) * P + r];
+      const int64_t po = S.o_ezy + ((int64_t)side * P + r) * pitch + ic;
+      float psi[4], pn[4];
+      ld4(psi, psr + po);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int c = i + k;
+        pn[k] = psi[k];
+        if (c >= 1 && c <= nx - 2) {
+          pn[k] = upd_psi(b, psi[k], cc, hxp[k], hxn[k], S.dy);
+          ezw4[k] = __fmaf_rn(m.cB(k), pn[k], ezw4[k]);
+        }
+      }
+      st4(psw + po, pn);
+    }
+
+    // ---- sources, then detectors, of this row (Dev_AESASourceCalc,
+    //      Dev_AESADetectorSim, Dev_AESAComponentDetector)
+    const int p0 = __ldg(S.row_start + j), p1 = __ldg(S.row_start + j + 1);
+    for (int p = p0; p < p1; ++p) {
+      const int4 pt = __ldg(S.pts + p);
+      const int k = pt.x - i;
+      if (!act || k < 0 || k > 3) continue;
+      float e = 0.f;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) if (q == k) e = ezw4[q];
+      if (pt.y == kPointSource) {
+        e = __fsub_rn(e, __ldg(S.src_val + (int64_t)n * S.n_src + pt.z));
+#pragma unroll
+        for (int q = 0; q < 4; ++q) if (q == k) ezw4[q] = e;
+      } else if (pt.y == kPointDetEz) {
+        if (S.record) S.trace[(int64_t)(n - 1) * S.n_det + pt.z] = e;
+        if (S.dft) {
+          const double2 tw = __ldg(S.twiddle + n);
+          double2 acc = S.dft[pt.z];
+          acc.x = fma((double)e, tw.x, acc.x);
+          acc.y = fma(-(double)e, tw.y, acc.y);
+          S.dft[pt.z] = acc;
+        }
+      } else {
+        float hxv = 0.f, hyv = 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) if (q == k) { hxv = hxn[q]; hyv = hyn[q]; }
+        if (S.record) {
+          float* dst = S.ctrace + ((int64_t)(n - 1) * S.n_comp + pt.z) * 3;
+          dst[0] = e; dst[1] = hxv; dst[2] = hyv;
+        }
+      }
+    }
+
+    if (act) {
+      st4(hxw + o, hxn);
+      st4(hyw + o, hyn);
+      st4(ezw + o, ezw4);
+      st4(jzw + o, jzw4);
+    }
+
+    // roll
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      hxp[k] = hxn[k];
+      ezc[k] = ezn[k];
+      ezn[k] = ezn2[k]; hxo[k] = hxo2[k]; hyo[k] = hyo2[k]; jzo[k] = jzo2[k];
+    }
+  }
+}
+
+template <int MEDIUM>
+__global__ void __launch_bounds__(kThreads, 2)
+step_stream_kernel(const DevShot* __restrict__ shots, const int4* __restrict__ units, int n_units,
+                   int n_global) {
+  __shared__ MatE s_mat_e[MEDIUM ? 256 : 1];
+  __shared__ MatH s_mat_h[MEDIUM ? 256 : 1];
+  if (MEDIUM) {
+    // Material tables are per launch (material-ID shots run one per launch).
+    for (int t = threadIdx.x; t < 256; t += blockDim.x) {
+      s_mat_e[t] = shots[0].mat_e[t];
+      s_mat_h[t] = shots[0].mat_h[t];
+    }
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31;
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int n_warps = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int u = warp; u < n_units; u += n_warps) {
+    const int4 ud = __ldg(units + u);
+    const DevShot& S = shots[ud.x];
+    const int n = n_global - S.base_n;
+    if (n < 1 || n > S.n_steps) continue;
+    process_unit<MEDIUM>(S, s_mat_e, s_mat_h, ud.y, ud.z, ud.w, n, lane);
+  }
+}
+
+cudaError_t launch_step(const DevShot* shots, const int4* units, int n_units, int n_global,
+                        int medium, int n_warps_grid, cudaStream_t stream) {
+  const int warps = n_warps_grid < n_units ? n_warps_grid : n_units;
+  const int blocks = (warps * 32 + kThreads - 1) / kThreads;
+  if (blocks <= 0) return cudaSuccess;
+  if (medium == 0) {
+    step_stream_kernel<0><<<blocks, kThreads, 0, stream>>>(shots, units, n_units, n_global);
+  } else {
+    step_stream_kernel<1><<<blocks, kThreads, 0, stream>>>(shots, units, n_units, n_global);
+  }
+  return cudaGetLastError();
+}
+
+int resident_warps(int medium, int device) {
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  if (medium == 0) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_stream_kernel<0>, kThreads, 0);
+  } else {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_stream_kernel<1>, kThreads, 0);
+  }
+  if (per_sm < 1) per_sm = 1;
+  return sms * per_sm * (kThreads / 32);
+}
+
+// Source waveform, FDTD_2D_Full/kernel.cu:653 and Dev_calculateChirp
+// (:694-698) with p = 1: amp[n]/N * cos(2*pi_c*(beta/2*t^2 + f0*t + phi/360)).
+// Computed in FP64 with t = n*dt in FP64 (the reference forms t and the phase
+// sum in FP32).  With pi_c = pi the phase is reduced modulo one cycle first.
+__global__ void source_table_kernel(float* src_val, double2* twiddle, const float* env,
+                                    const double* phase, int n_src, int n_steps, double dt,
+                                    double scale, double f0, double beta_half, double src_pi,
+                                    int exact_pi, double dft_fdt) {
+  const int64_t total = (int64_t)(n_steps + 1) * n_src;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int n = (int)(t / n_src);
+    const int e = (int)(t % n_src);
+    const double tt = (double)n * dt;
+    const double x = beta_half * tt * tt + f0 * tt + phase[e];
+    const double cs = exact_pi ? cospi(2.0 * (x - floor(x))) : cos(2.0 * src_pi * x);
+    src_val[t] = (float)(scale * (double)env[n] * cs);
+  }
+  if (twiddle) {
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n <= n_steps; n += gridDim.x * blockDim.x) {
+      double ph = dft_fdt * (double)n;
+      ph -= floor(ph);
+      double sn, cs;
+      sincospi(2.0 * ph, &sn, &cs);
+      twiddle[n] = make_double2(cs, sn);
+    }
+  }
+}
+
+cudaError_t build_source_tables(float* src_val, double2* twiddle, const float* env,
+                                const double* phase_cycles, int n_src, int n_steps, double dt,
+                                double scale, double f0, double beta_half, double src_pi,
+                                double dft_fdt, cudaStream_t stream) {
+  const int exact = (src_pi == 3.14159265358979323846) ? 1 : 0;
+  source_table_kernel<<<256, 256, 0, stream>>>(src_val, twiddle, env, phase_cycles, n_src, n_steps,
+                                               dt, scale, f0, beta_half, src_pi, exact, dft_fdt);
+  return cudaGetLastError();
+}
+
+// Dev_RCcalc (FDTD_2D_Full/kernel.cu:968-1044) as one CTA per line.  The
+// reference walks each column serially with one thread (O(ny) dependent
+// loads); here the column max and the downward scan are block reductions.
+// The scan result is the largest j in [1, ny-3] where |Ez| is not below the
+// edge level, which is where the reference's do-while from j = ny-2 stops.
+__global__ void rc_kernel(const float* __restrict__ ez, int64_t pitch, int ny,
+                          const int* __restrict__ scan_i, const int* __restrict__ max_i, int j_cut,
+                          float level, float* __restrict__ edge, int* __restrict__ spd_row) {
+  __shared__ float s_max[32];
+  __shared__ int s_best[32];
+  __shared__ float s_edge;
+  const int l = blockIdx.x;
+  const int im = max_i[l], is = scan_i[l];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  float m = -INFINITY;
+  for (int j = j_cut + (int)threadIdx.x; j < ny - 2; j += blockDim.x) m = fmaxf(m, ez[(int64_t)j * pitch + im]);
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) s_max[w] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float temp = ez[im];  // Dev_FindMax starts from row 0
+    for (int k = 0; k < nw; ++k)
+      if (s_max[k] > temp) temp = s_max[k];
+    const float cand = temp * level;
+    float e = edge[l];
+    if (cand > e) e = cand;
+    edge[l] = e;
+    s_edge = e;
+  }
+  __syncthreads();
+  const float e = s_edge;
+  int best = 0;
+  for (int j = 1 + (int)threadIdx.x; j <= ny - 3; j += blockDim.x)
+    if (!(fabsf(ez[(int64_t)j * pitch + is]) < e)) best = max(best, j);
+  for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if (lane == 0) s_best[w] = best;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int b = 0;
+    for (int k = 0; k < nw; ++k) b = max(b, s_best[k]);
+    spd_row[l] = b;
+  }
+}
+
+cudaError_t launch_rc(const float* ez, int64_t pitch, int ny, int n_rc, const int* scan_i,
+                      const int* max_i, int j_cut, float level, float* edge, int* spd_row,
+                      cudaStream_t stream) {
+  rc_kernel<<<n_rc, 256, 0, stream>>>(ez, pitch, ny, scan_i, max_i, j_cut, level, edge, spd_row);
+  return cudaGetLastError();
+}
+
+__global__ void line_kernel(const float* __restrict__ ez, int64_t pitch, int j, int i0, int n,
+                            float* __restrict__ dst) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+    dst[t] = ez[(int64_t)j * pitch + i0 + t];
+}
+
+cudaError_t launch_line(const float* ez, int64_t pitch, int j, int i0, int n, float* dst,
+                        cudaStream_t stream) {
+  line_kernel<<<(n + 255) / 256, 256, 0, stream>>>(ez, pitch, j, i0, n, dst);
+  return cudaGetLastError();
+}
+
+__global__ void nonfinite_kernel(const float* __restrict__ a, int64_t n, int* flag) {
+  int bad = 0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    bad |= !isfinite(a[t]);
+  }
+  bad = __syncthreads_or(bad);
+  if (bad && threadIdx.x == 0) atomicAdd(flag, 1);
+}
+
+cudaError_t launch_nonfinite(const float* a, int64_t n, int* flag, cudaStream_t stream) {
+  nonfinite_kernel<<<1024, 256, 0, stream>>>(a, n, flag);
+  return cudaGetLastError();
+}
+
+}  // namespace fdtd2d

@@ -1,0 +1,267 @@
+/*
+ * fdtd2d.h -- C ABI of the GB300 TMz FDTD time-step engine.
+ *
+ * This header is the drop-in boundary for the reference's device driver
+ * (FDTD_2D_Full/kernel.cu + Kernel.cuh).  The reference crosses that boundary
+ * through implicit globals (FDTD_2D_Full/Ext_kernel.cuh:8-258) and four calls:
+ *
+ *   cudaError_t DevMemoryAllocation()     FDTD_2D_Full/Kernel.cuh:100  -> fdtd2d_create
+ *   cudaError_t DevFieldCalculation()     FDTD_2D_Full/Kernel.cuh:102  -> fdtd2d_run (+ read_*)
+ *   cudaError_t DevSourceToDetect...()    FDTD_2D_Full/Kernel.cuh:101  -> two contexts, see INTEGRATION.md
+ *   cudaError_t DevMemoryFree()           FDTD_2D_Full/Kernel.cuh:106  -> fdtd2d_destroy
+ *
+ * Here the data that the reference passes in globals travels in one plain
+ * struct (fdtd2d_setup) with pointers and sizes only.  The library copies what
+ * it needs; the caller keeps ownership of every host buffer.  No C++ types and
+ * no exceptions cross this ABI.  Every entry point returns 0 on success or a
+ * negative FDTD2D_ERR_* code; fdtd2d_strerror() names it.
+ *
+ * Conventions shared with the reference (FDTD_2D_Full/kernel.cu:127-805):
+ *   - Ez lives on an nx x ny grid (Imax x Jmax), x (index i) fastest.
+ *   - Host-visible field layouts are the reference's own:
+ *       Ez, Jz : [ny][nx]        Hx : [ny-1][nx]        Hy : [ny][nx-1]
+ *   - Steps are numbered from 1 like the reference loop `for(n=1;n<=nMax;++n)`
+ *     (FDTD_2D_Full/kernel.cu:2065).
+ *   - One step = Hx, Hy (+CPML psi), Jz from Ez^n, Ez (+CPML psi), source,
+ *     detectors -- the order of FDTD_2D_Full/kernel.cu:2073-2157.
+ */
+#ifndef FDTD2D_H
+#define FDTD2D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FDTD2D_ABI_VERSION 1
+
+/* ---- status codes -------------------------------------------------------- */
+enum {
+    FDTD2D_OK            = 0,
+    FDTD2D_ERR_INVALID   = -1,  /* bad argument or inconsistent setup          */
+    FDTD2D_ERR_NOMEM     = -2,  /* device or host allocation failed            */
+    FDTD2D_ERR_CUDA      = -3,  /* CUDA runtime error (fdtd2d_last_cuda_error) */
+    FDTD2D_ERR_NONFINITE = -4,  /* NaN/Inf found in the fields                 */
+    FDTD2D_ERR_RANGE     = -5,  /* step or index range outside the run         */
+    FDTD2D_ERR_IO        = -6,  /* file could not be opened or written         */
+    FDTD2D_ERR_CONFIG    = -7,  /* Settings.ini missing or malformed           */
+    FDTD2D_ERR_STATE     = -8,  /* call not valid in the object's state        */
+    FDTD2D_ERR_BUDGET    = -9,  /* request does not fit the HBM budget         */
+    FDTD2D_ERR_NODEVICE  = -10  /* no CUDA device                              */
+};
+
+/* ---- enumerations -------------------------------------------------------- */
+enum { FDTD2D_MEDIUM_UNIFORM = 0,      /* scalar CA/CB/DA/DB + per-cell density map */
+       FDTD2D_MEDIUM_MATERIAL_ID = 1 };/* ID1/ID2/ID3 maps + material tables        */
+
+enum { FDTD2D_STORE_F32 = 0,           /* FP32 field storage (reference)            */
+       FDTD2D_STORE_F16 = 1,           /* FP16 storage, per-array 2^k scale          */
+       FDTD2D_STORE_BF16 = 2 };        /* BF16 storage                               */
+
+enum { FDTD2D_FIELD_EZ = 0, FDTD2D_FIELD_HX = 1, FDTD2D_FIELD_HY = 2, FDTD2D_FIELD_JZ = 3,
+       /* CPML auxiliary arrays in the reference's layouts (FDTD_2D_Full/kernel.cu:1160-1220) */
+       FDTD2D_FIELD_PSI_EZX_1 = 4, FDTD2D_FIELD_PSI_EZX_2 = 5,   /* [ny][P]     */
+       FDTD2D_FIELD_PSI_EZY_1 = 6, FDTD2D_FIELD_PSI_EZY_2 = 7,   /* [P][nx]     */
+       FDTD2D_FIELD_PSI_HYX_1 = 8, FDTD2D_FIELD_PSI_HYX_2 = 9,   /* [ny][P-1]   */
+       FDTD2D_FIELD_PSI_HXY_1 = 10, FDTD2D_FIELD_PSI_HXY_2 = 11  /* [P-1][nx]   */ };
+
+typedef struct fdtd2d_point { int32_t i, j; } fdtd2d_point;
+
+/*
+ * Everything one shot needs; replaces the globals of FDTD_2D_Full/Ext_kernel.cuh.
+ * Table index order is the reference's (index 0 = outer edge of each strip).
+ */
+typedef struct fdtd2d_setup {
+    int32_t nx, ny;          /* Imax, Jmax                                        */
+    int32_t npml;            /* PML_SIZE (FDTD_2D_Full/Settings.cuh:23); 2 <= P    */
+    int32_t n_steps;         /* nMax                                              */
+    double  dt, dx, dy;      /* s, m, m                                           */
+
+    /* CPML recursion tables: E tables have npml entries, H tables npml-1
+       (FDTD_2D_Full/FDTD_cuda.cu:1224-1460).                                     */
+    const float *be_x_1, *ce_x_1, *be_x_2, *ce_x_2;
+    const float *bh_x_1, *ch_x_1, *bh_x_2, *ch_x_2;
+    const float *be_y_1, *ce_y_1, *be_y_2, *ce_y_2;
+    const float *bh_y_1, *ch_y_1, *bh_y_2, *ch_y_2;
+    /* update denominators 1/(kappa*d) (FDTD_2D_Full/FDTD_cuda.cu:1466-1578)      */
+    const float *den_ex, *den_hx;           /* [nx-1] */
+    const float *den_ey, *den_hy;           /* [ny-1] */
+
+    /* medium */
+    int32_t medium;                         /* FDTD2D_MEDIUM_*                     */
+    float   ca, cb, da, db;                 /* uniform medium update coefficients  */
+    const float *ne;                        /* uniform medium: [ny][nx] electron
+                                               density at Ez cells (m^-3); NULL=none */
+    const int32_t *id1, *id2, *id3;         /* material medium: [ny][nx] maps for
+                                               Hx, Hy, Ez (values 0..255)          */
+    int32_t n_materials;                    /* material medium: table length <=256 */
+    const float *mat_ca, *mat_cb, *mat_da, *mat_db, *mat_ne;
+    double  nu;                             /* electron collision frequency, 1/s   */
+    double  jz_coef;                        /* e^2/m_e used by the Jz update
+                                               (reference D_CJ = 2.81794e-8,
+                                               FDTD_2D_Full/kernel.cu:119)         */
+
+    /* phased-array soft source: Ez(src_e) -= s_e(n) after the E update, with
+       s_e(n) = src_scale*envelope[n]*cos(2*src_pi*(beta/2*t^2 + f0*t + phase_e/360)),
+       t = n*dt, beta = (f1-f0)/t1  (FDTD_2D_Full/kernel.cu:621-659, 694-698)   */
+    int32_t n_src;
+    const fdtd2d_point *src;                /* [n_src] absolute Ez cells           */
+    const double *src_phase_deg;            /* [n_src]                             */
+    const float *envelope;                  /* [n_steps+1], index = step n         */
+    double  src_scale;                      /* reference: 1/(qantI*qantK)          */
+    double  f0, f1, t1;                     /* Hz, Hz, s (t1 > 0 when f1 != f0)    */
+    double  src_pi;                         /* pi used in the phase (reference 3.14) */
+
+    /* detectors (FDTD_2D_Full/kernel.cu:719-805)                                 */
+    int32_t n_det;  const fdtd2d_point *det;   /* Ez samples (D_detect)           */
+    int32_t n_comp; const fdtd2d_point *comp;  /* Ez/Hx/Hy samples (D_det_*)      */
+    int32_t record_traces;                  /* keep per-step samples on the GPU    */
+    double  dft_freq;                       /* running FP64 DFT of the Ez detector
+                                               samples at this frequency (0 = off) */
+    int32_t storage;                        /* FDTD2D_STORE_*                      */
+
+    /* wave-front ("RC") tracker, Dev_RCcalc (FDTD_2D_Full/kernel.cu:968-1044).
+       After each step n, for each line l:
+         edge_l = max(edge_l, rc_level * max(Ez(rc_max_i[l], 0),
+                                             max_{j in [rc_j_cut, ny-2)} Ez(rc_max_i[l], j)))
+         spd[n][l] = largest j in [1, ny-3] with !(|Ez(rc_scan_i[l], j)| < edge_l), else 0
+       with edge_l starting at rc_edge0 (reference 10.0).                         */
+    int32_t n_rc;
+    const int32_t *rc_scan_i, *rc_max_i;
+    int32_t rc_j_cut;
+    float   rc_level, rc_edge0;
+
+    /* line probe for the time-of-flight post-processing (Dev_SaveLine,
+       FDTD_2D_Full/kernel.cu:666-688): Ez(line_i0 .. line_i0+line_n-1, line_j)
+       is kept for every step in [line_first, line_last].                        */
+    int32_t line_n, line_i0, line_j, line_first, line_last;
+} fdtd2d_setup;
+
+/* ---- single shot (the reference's plain run) ------------------------------ */
+typedef struct fdtd2d_ctx fdtd2d_ctx;
+
+/* Allocate device state, upload tables/maps, zero the fields.
+   Replaces DevMemoryAllocation (FDTD_2D_Full/kernel.cu:1087-1618). */
+int fdtd2d_create(const fdtd2d_setup *setup, int device, fdtd2d_ctx **out);
+
+/* Advance steps n_first..n_last inclusive (1-based).  n_first must be the step
+   after the last one run.  Replaces the loop body of DevFieldCalculation
+   (FDTD_2D_Full/kernel.cu:2065-2309).  Asynchronous; errors surface at the
+   next synchronising call. */
+int fdtd2d_run(fdtd2d_ctx *ctx, int32_t n_first, int32_t n_last);
+
+/* Wait for queued work; returns FDTD2D_ERR_CUDA on a device-side failure. */
+int fdtd2d_synchronize(fdtd2d_ctx *ctx);
+
+/* Last completed-or-queued step number (0 before the first run). */
+int fdtd2d_current_step(const fdtd2d_ctx *ctx, int32_t *n);
+
+/* Copy per-step detector samples of steps n0..n1 (1-based) to caller buffers,
+   row-major [n1-n0+1][n_det] (ez) and [n1-n0+1][n_comp] (comp_*).  Any pointer
+   may be NULL.  Requires record_traces. */
+int fdtd2d_read_traces(fdtd2d_ctx *ctx, int32_t n0, int32_t n1, float *det_ez,
+                       float *comp_ez, float *comp_hx, float *comp_hy);
+
+/* Wave-front positions spd[n][l] of steps n0..n1 into [n1-n0+1][n_rc]. */
+int fdtd2d_read_rc(fdtd2d_ctx *ctx, int32_t n0, int32_t n1, int32_t *spd);
+
+/* Line-probe samples of steps n0..n1 (inside [line_first, line_last]) into
+   [n1-n0+1][line_n]. */
+int fdtd2d_read_line(fdtd2d_ctx *ctx, int32_t n0, int32_t n1, float *out);
+
+/* Running DFT X_e = sum_n Ez_e^n exp(-i 2 pi f n dt) per Ez detector. */
+int fdtd2d_read_dft(fdtd2d_ctx *ctx, double *re, double *im);
+
+/* Copy a field (FDTD2D_FIELD_*) in the reference layout to / from host memory. */
+int fdtd2d_read_field(fdtd2d_ctx *ctx, int which, float *host);
+int fdtd2d_write_field(fdtd2d_ctx *ctx, int which, const float *host);
+
+/* Device-side scan for NaN/Inf in Ez/Hx/Hy/Jz; FDTD2D_ERR_NONFINITE if any. */
+int fdtd2d_check_finite(fdtd2d_ctx *ctx);
+
+/* Release everything.  Replaces DevMemoryFree (FDTD_2D_Full/kernel.cu:2820-2987). */
+int fdtd2d_destroy(fdtd2d_ctx *ctx);
+
+/* Bytes of device memory one shot of this setup holds. */
+int64_t fdtd2d_device_bytes(const fdtd2d_setup *setup);
+
+/* Kernel launches issued by this context so far (for launch accounting). */
+int64_t fdtd2d_launch_count(const fdtd2d_ctx *ctx);
+
+/* Number of CUDA devices visible to this process (0 when none). */
+int fdtd2d_device_count(void);
+
+/* Run steps n_first..n_last like fdtd2d_run, bracketed by CUDA events on the
+   context's stream; *elapsed_ms receives the device time of the whole range. */
+int fdtd2d_run_timed(fdtd2d_ctx *ctx, int32_t n_first, int32_t n_last, float *elapsed_ms);
+
+/* Stability number of the explicit update with the Drude current:
+   (c dt)^2 (1/dx^2 + 1/dy^2) + (w_p,max dt / 2)^2, w_p,max from the largest
+   plasma drive of the setup.  Above 1 the scheme grows without bound. */
+double fdtd2d_stability(const fdtd2d_setup *setup);
+
+const char *fdtd2d_strerror(int status);
+int fdtd2d_last_cuda_error(const fdtd2d_ctx *ctx);   /* cudaError_t value */
+int fdtd2d_abi_version(void);
+
+/* ---- host-side setup precompute (the reference's L2 layer) ---------------- */
+typedef struct fdtd2d_problem fdtd2d_problem;   /* owns the arrays its setup points to */
+
+/* Parameterised shot (synthetic workloads): grid, CPML grading, plasma profile,
+   phased array and detectors.  Units are SI; see the design doc for each field. */
+typedef struct fdtd2d_spec {
+    int32_t nx, ny, npml, n_steps;
+    double  dx, dy;
+    double  courant;            /* dt = courant*dx/(c*sqrt(2)) when dt <= 0        */
+    double  dt;
+    /* CPML grading (FDTD_2D_Full/FDTD_cuda.cu:1206-1214 form)                     */
+    double  cpml_m, cpml_ma;    /* polynomial orders (reference 3, 1)              */
+    double  sigma_factor;       /* sigma_max = factor*0.8(m+1)/(eta0*d) (ref 0.75) */
+    double  kappa_max, alpha_max;
+    /* plasma density profile at Ez cells                                          */
+    int32_t profile;            /* 0 none, 1 linear slab, 2 tanh, 3 tanh x (1+rms*g) */
+    double  ne_peak;            /* slab: density at x_hi; tanh: 2x amplitude (n = ne_peak/2*(1+tanh)) */
+    double  x_lo, x_hi;         /* slab extent (cells)                              */
+    double  x_center, width;    /* tanh centre and width (cells)                    */
+    double  grf_rms, grf_corr;  /* random-field rms and correlation length (cells)  */
+    uint64_t seed;
+    double  nu;                 /* collision frequency (1/s)                        */
+    /* phased array: element e at (src_i + e*src_di, src_j + e*src_dj)             */
+    int32_t n_elem, src_i, src_j, src_di, src_dj;
+    double  freq;               /* carrier (Hz)                                     */
+    double  steer_deg;          /* beam steering angle from the array normal        */
+    double  amp;
+    int32_t pulse;              /* 0 Gaussian (t0, width), 1 raised-cosine ramp then CW */
+    double  pulse_width;        /* Gaussian 1/e half-width or ramp length (s)       */
+    double  pulse_t0;           /* Gaussian centre (s); <=0 -> 4 widths             */
+    /* detectors: element e at (det_i + e*det_di, det_j + e*det_dj)                */
+    int32_t n_det, det_i, det_j, det_di, det_dj;
+    int32_t record_traces;
+    double  dft_freq;           /* 0 -> freq                                        */
+    int32_t storage;
+} fdtd2d_spec;
+
+/* Fill a spec with the plain 512^2 workload defaults. */
+void fdtd2d_spec_defaults(fdtd2d_spec *spec);
+
+int fdtd2d_problem_from_spec(const fdtd2d_spec *spec, fdtd2d_problem **out);
+
+/* Reference drop-in: read Settings.ini (same sections, keys and defaults as
+   readINIparam, FDTD_2D_Full/FDTD_cuda.cu:27-176) and build the setup the
+   reference builds (FDTD_2D_Full/FDTD_cuda.cu:305-382, 1122-1579, 2602-3655). */
+int fdtd2d_problem_from_ini(const char *ini_path, fdtd2d_problem **out);
+
+const fdtd2d_setup *fdtd2d_problem_setup(const fdtd2d_problem *p);
+void fdtd2d_problem_free(fdtd2d_problem *p);
+
+/* Whole reference program on top of this ABI: Settings.ini in, the reference's
+   output files (Detect.txt, detAll.txt, detEz/Hx/Hy.txt, Ez.txt,
+   FieldSaveDat.txt, SourceP.txt, iniLOG.txt, log.txt) out in out_dir.
+   Replaces main -> initlimits (FDTD_2D_Full/FDTD_cuda.cu:20, 384-441). */
+int fdtd2d_run_settings(const char *ini_path, const char *out_dir, int device);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FDTD2D_H */

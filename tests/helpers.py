@@ -1,0 +1,63 @@
+"""Shared helpers for the parity tests: run the CUDA shot and the FP64 oracle
+on the same setup and compare fields, traces and DFTs."""
+from __future__ import annotations
+
+import numpy as np
+
+import fdtd_2d_gb300 as F
+import oracle as O
+
+FIELDS = (F.FIELD_EZ, F.FIELD_HX, F.FIELD_HY, F.FIELD_JZ)
+PSI_FIELDS = (F.FIELD_PSI_EZX_1, F.FIELD_PSI_EZX_2, F.FIELD_PSI_EZY_1, F.FIELD_PSI_EZY_2,
+              F.FIELD_PSI_HYX_1, F.FIELD_PSI_HYX_2, F.FIELD_PSI_HXY_1, F.FIELD_PSI_HXY_2)
+
+# Field tolerance: relative L2 error against the FP64 oracle (spec 1e-5).
+FIELD_TOL = 1e-5
+# Detector phase tolerance (rad).
+PHASE_TOL = 1e-4
+
+
+def rel(a, b) -> float:
+    return O.rel_l2(a, b)
+
+
+def random_state(shot_or_oracle, nx, ny, P, rng, scale=1.0, psi=True):
+    """Write the same random fields into a shot and an oracle (returns the dict)."""
+    st = {}
+    for w in FIELDS:
+        shape = F.field_shape(w, nx, ny, P)
+        a = (rng.standard_normal(shape) * scale).astype(np.float32)
+        if w == F.FIELD_HX or w == F.FIELD_HY:
+            a *= np.float32(1 / 377.0)
+        st[w] = a
+    if psi:
+        for w in PSI_FIELDS:
+            shape = F.field_shape(w, nx, ny, P)
+            st[w] = (rng.standard_normal(shape) * scale * 1e-3).astype(np.float32)
+    return st
+
+
+def load_state(targets, st):
+    for t in targets:
+        for w, a in st.items():
+            t.write_field(w, a)
+
+
+def compare_fields(shot, ref, fields=FIELDS, tol=FIELD_TOL, norms=None):
+    """Relative L2 per field; with `norms` (peak norm per field) the error is
+    normalised by the field's peak norm over the run instead of its current norm."""
+    out = {}
+    for w in fields:
+        g = shot.read_field(w).astype(np.float64)
+        c = ref.read_field(w)
+        den = norms[w] if norms else np.linalg.norm(c)
+        err = float(np.linalg.norm(g - c) / den) if den > 0 else float(np.linalg.norm(g - c))
+        out[w] = err
+    bad = {w: e for w, e in out.items() if not e <= tol}
+    assert not bad, f"fields over tolerance {tol}: {bad}"
+    return out
+
+
+def dft_phase_error(shot, ref) -> float:
+    dg, dc = shot.dft(), ref.dft()
+    return float(np.max(np.abs(np.angle(dg / dc))))

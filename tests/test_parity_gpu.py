@@ -1,0 +1,226 @@
+"""CUDA step vs the FP64 oracle, through the C ABI (fdtd2d_create/run/read_*).
+
+Tolerances: fields relative L2 <= 1e-5 (normalised by the field's peak norm
+over the run where the pulse has left the grid), detector traces relative L2
+<= 1e-5, detector DFT phase <= 1e-4 rad.
+"""
+import numpy as np
+import pytest
+
+import fdtd_2d_gb300 as F
+import oracle as O
+from helpers import (FIELD_TOL, FIELDS, PHASE_TOL, PSI_FIELDS, compare_fields, dft_phase_error,
+                     load_state, random_state, rel)
+
+pytestmark = pytest.mark.gpu
+
+
+def test_plain_512_shot_checkpoints(gpu):
+    """512^2 plain shot (linear slab plasma, point source, 4000 steps)."""
+    prob = F.Problem.from_spec()
+    assert prob.stability() < 1.0
+    ref = O.Oracle(prob.setup_ptr)
+    peaks = {w: 0.0 for w in FIELDS + PSI_FIELDS}
+    snaps = []
+    with F.Shot(prob, gpu) as shot:
+        for n in (500, 1000, 1500, 2000, 3000, 4000):
+            shot.run(shot.step + 1, n)
+            ref.run(ref.step + 1, n)
+            snap = {}
+            for w in FIELDS + PSI_FIELDS:
+                c = ref.read_field(w)
+                g = shot.read_field(w).astype(np.float64)
+                peaks[w] = max(peaks[w], float(np.linalg.norm(c)))
+                snap[w] = (float(np.linalg.norm(g - c)), float(np.linalg.norm(c)))
+            snaps.append((n, snap))
+        for n, snap in snaps:
+            for w, (d, c) in snap.items():
+                assert d / peaks[w] <= FIELD_TOL, (n, w, d / peaks[w])
+                if c >= 0.1 * peaks[w]:
+                    assert d / c <= FIELD_TOL, (n, w, d / c)
+        tg = shot.traces()["det_ez"]
+        tc = ref.traces()["det_ez"]
+        assert rel(tg, tc) <= FIELD_TOL
+        assert dft_phase_error(shot, ref) <= PHASE_TOL
+        assert shot.check_finite()
+
+
+@pytest.mark.parametrize("nx,ny,P", [(203, 157, 7), (131, 96, 4), (64, 260, 12), (40, 40, 2)])
+def test_random_state_uniform(gpu, nx, ny, P):
+    """Random fields and psi on odd grids (nx not a multiple of 4, unit edges,
+    tiny P), per-cell plasma, collisions; every code path of one step."""
+    rng = np.random.default_rng(nx * 1000 + ny)
+    prob = F.Problem.from_spec(nx=nx, ny=ny, npml=P, n_steps=60, profile=1, x_lo=nx // 3,
+                               x_hi=nx - 3, ne_peak=2e19, nu=3e9, src_i=P + 2, src_j=ny // 2,
+                               det_i=P + 4, det_j=ny // 2 + 1, n_det=1)
+    ref = O.Oracle(prob.setup_ptr)
+    with F.Shot(prob, gpu) as shot:
+        st = random_state(shot, nx, ny, P, rng)
+        load_state([shot, ref], st)
+        shot.run(1, 1)
+        ref.run(1, 1)
+        compare_fields(shot, ref, FIELDS + PSI_FIELDS, tol=1e-6)
+        shot.run(2, 60)
+        ref.run(2, 60)
+        compare_fields(shot, ref, FIELDS + PSI_FIELDS, tol=FIELD_TOL)
+
+
+def test_phased_array_traces_and_dft(gpu):
+    """Multi-element steered array with co-located detectors on a tanh x GRF
+    plasma: per-step traces and the FP64 running DFT."""
+    n_elem = 8
+    prob = F.Problem.from_spec(nx=384, ny=320, npml=16, n_steps=1500, dx=0.25e-3, dy=0.25e-3,
+                               courant=0.99, profile=3, ne_peak=3e19, x_center=250, width=40,
+                               grf_rms=0.05, grf_corr=10, seed=7, nu=2e9, n_elem=n_elem, src_i=40,
+                               src_j=140, src_dj=5, src_di=0, freq=50e9, steer_deg=15, pulse=1,
+                               pulse_width=0.2e-9, n_det=n_elem, det_i=40, det_j=140, det_dj=5,
+                               det_di=0, dft_freq=50e9)
+    assert prob.stability() < 1.0
+    ref = O.Oracle(prob.setup_ptr)
+    with F.Shot(prob, gpu) as shot:
+        shot.run(1, 1500)
+        ref.run(1, 1500)
+        tg, tc = shot.traces()["det_ez"], ref.traces()["det_ez"]
+        assert rel(tg, tc) <= FIELD_TOL
+        assert dft_phase_error(shot, ref) <= PHASE_TOL
+        dg, dc = shot.dft(), ref.dft()
+        assert np.max(np.abs(np.abs(dg) / np.abs(dc) - 1)) <= 1e-5
+
+
+def test_material_id_medium(gpu, tmp_path):
+    """Reference Settings.ini medium (sphere + fluctuation ID maps, 150-material
+    table, PEC id 1 handling) with random fields."""
+    ini = tmp_path / "Settings.ini"
+    ini.write_text(SMALL_INI)
+    prob = F.Problem.from_ini(ini)
+    s = prob.setup
+    assert s.medium == F.MEDIUM_MATERIAL_ID
+    nx, ny, P = s.nx, s.ny, s.npml
+    rng = np.random.default_rng(5)
+    ref = O.Oracle(prob.setup_ptr)
+    with F.Shot(prob, gpu) as shot:
+        st = random_state(shot, nx, ny, P, rng, scale=10.0)
+        load_state([shot, ref], st)
+        shot.run(1, 40)
+        ref.run(1, 40)
+        compare_fields(shot, ref, FIELDS + PSI_FIELDS)
+        t = shot.traces()
+        r = ref.traces()
+        for k in ("det_ez", "comp_ez", "comp_hx", "comp_hy"):
+            assert rel(t[k], r[k]) <= FIELD_TOL, k
+
+
+def test_write_read_roundtrip(gpu):
+    prob = F.Problem.from_spec(nx=100, ny=77, npml=6, n_steps=5)
+    rng = np.random.default_rng(1)
+    with F.Shot(prob, gpu) as shot:
+        for w in FIELDS + PSI_FIELDS:
+            a = rng.standard_normal(F.field_shape(w, 100, 77, 6)).astype(np.float32)
+            shot.write_field(w, a)
+            assert np.array_equal(shot.read_field(w), a)
+
+
+def test_nonfinite_detection(gpu):
+    prob = F.Problem.from_spec(nx=64, ny=64, npml=4, n_steps=3)
+    with F.Shot(prob, gpu) as shot:
+        shot.run(1, 1)
+        assert shot.check_finite()
+        ez = shot.read_field("ez")
+        ez[10, 10] = np.nan
+        shot.write_field("ez", ez)
+        assert not shot.check_finite()
+
+
+def test_run_range_errors(gpu):
+    prob = F.Problem.from_spec(nx=64, ny=64, npml=4, n_steps=10)
+    with F.Shot(prob, gpu) as shot:
+        with pytest.raises(F.FdtdError) as e:
+            shot.run(2, 3)  # must start at step 1
+        assert e.value.status == F.ERR_RANGE
+        shot.run(1, 10)
+        with pytest.raises(F.FdtdError):
+            shot.run(11, 11)  # past n_steps
+        with pytest.raises(F.FdtdError):
+            shot.traces(5, 12)
+
+
+def test_invalid_setups_rejected(gpu):
+    # detector on the PEC ring
+    prob = F.Problem.from_spec(nx=64, ny=64, npml=4, n_steps=3, det_i=0, det_j=5)
+    with pytest.raises(F.FdtdError) as e:
+        F.Shot(prob, gpu)
+    assert e.value.status == F.ERR_RANGE
+    # CPML strips overlapping
+    prob = F.Problem.from_spec(nx=20, ny=64, npml=10, n_steps=3, src_i=5, det_i=6, src_j=30,
+                               det_j=30, x_lo=8, x_hi=12)
+    with pytest.raises(F.FdtdError):
+        F.Shot(prob, gpu)
+
+
+SMALL_INI = """;config for a small drop-in run
+[hardware]
+GPU_device=0
+[regimes]
+SourceToDetect = 0
+[grid]
+Use_Exp_time = 1
+Imax = 60
+Jmax = 110
+Max_time = 400
+Exp_time = 0.25
+ds = 0.5
+dt_coef = 0.5
+Isource = 30
+Jsource = 10
+Idetect = 30
+Jdetect = 14
+[AESA]
+SIsize = 10
+SAutoDelta = 0
+SIdelta = 2
+SPAngle = 5
+DIsize = 10
+DAutoDelta = 0
+DIdelta = 2
+[PulseParam]
+Chirp=1
+FreqA=38
+FreqB=30
+Fronts_ns=0.05
+Plato_ns=0.05
+Pulse_amp = 1881
+[2Dsave]
+From=0
+To=-25
+TimeSieve=2000
+GridSieve=1
+[medium]
+Build=1
+Icen=30
+Jcen=80
+A=2
+B=1
+C=1
+P=1
+Q=1
+N=1
+Radius=25
+Alpha=2.0
+Beta=1.0
+ne0=5.5e+19
+neA=0
+[mediumFluc]
+FlucBuild=2
+FlucIcen=25
+FlucJcen=70
+FlucRadius=8
+FlucAlpha=2
+FlucBeta=1
+FlucNe0=1.028e+19
+[RC_calc]
+Iline = 30
+LIsize = 10
+LIdelta = 5
+FilterWindow = 20
+Rlevel = 0.07
+"""
