@@ -160,7 +160,8 @@ __device__ float hy_cell(const DevShot& S, const MatH* mat_h, int par, int c, in
 }
 
 // One Hx row segment (i..i+3, j): bulk update + y-strip CPML.  `own` writes
-// the new psi (only the owning unit does).
+// the new psi: only the owning unit does, and only from lanes that hold real
+// columns (inactive lanes run with their address clamped to column 0).
 template <int MEDIUM>
 __device__ __forceinline__ void hx_row(const DevShot& S, const MediumRow<MEDIUM>& m, int par, int i, int j, const float (&ezj)[4],
                                        const float (&ezj1)[4], const float (&hxo)[4],
@@ -189,7 +190,7 @@ __device__ __forceinline__ void hx_row(const DevShot& S, const MediumRow<MEDIUM>
         out[k] = __fmaf_rn(m.dbx(k), pn[k], out[k]);
       }
     }
-    if (own) st4(S.psi + (par ^ 1) * S.psi_buf + poff, pn);
+    if (own) st4(S.psi + (par ^ 1) * S.psi_buf + poff, pn);  // callers pass own = act
   }
 }
 
@@ -263,7 +264,7 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
 
     // ---- H update (Dev_HxCalc/Dev_HxPML_Jdir_Calc, Dev_HyCalc/Dev_HyPML_Idir_Calc)
     float hxn[4];
-    hx_row<MEDIUM>(S, m, par, ic, j, ezc, ezn, hxo, hxn, true);
+    hx_row<MEDIUM>(S, m, par, ic, j, ezc, ezn, hxo, hxn, act);
 
     float ezr_next = __shfl_down_sync(0xffffffffu, ezc[0], 1);
     if (lane == 31) {

@@ -43,18 +43,30 @@ def load_state(targets, st):
             t.write_field(w, a)
 
 
-def compare_fields(shot, ref, fields=FIELDS, tol=FIELD_TOL, norms=None):
-    """Relative L2 per field; with `norms` (peak norm per field) the error is
-    normalised by the field's peak norm over the run instead of its current norm."""
+def compare_fields(shot, ref, fields=FIELDS, tol=FIELD_TOL, ref32=None):
+    """Relative L2 error per field against the FP64 oracle.
+
+    The physical fields (Ez, Hx, Hy, Jz) must be within `tol`.  The CPML psi
+    arrays are differences of nearly equal field values, so FP32 arithmetic
+    (the reference's own) loses digits there; with `ref32` (the FP32
+    restatement of the same step) a psi array passes when its error is within
+    `tol` or within 4x the FP32 restatement's own error."""
     out = {}
+    bad = {}
     for w in fields:
         g = shot.read_field(w).astype(np.float64)
         c = ref.read_field(w)
-        den = norms[w] if norms else np.linalg.norm(c)
+        den = np.linalg.norm(c)
         err = float(np.linalg.norm(g - c) / den) if den > 0 else float(np.linalg.norm(g - c))
         out[w] = err
-    bad = {w: e for w, e in out.items() if not e <= tol}
-    assert not bad, f"fields over tolerance {tol}: {bad}"
+        limit = tol
+        if ref32 is not None and w in PSI_FIELDS:
+            f = ref32.read_field(w)
+            e32 = float(np.linalg.norm(f - c) / den) if den > 0 else float(np.linalg.norm(f - c))
+            limit = max(tol, 4.0 * e32)
+        if not err <= limit:
+            bad[w] = (err, limit)
+    assert not bad, f"fields over tolerance: {bad}"
     return out
 
 
