@@ -128,8 +128,16 @@ def test_material_id_medium(gpu, tmp_path):
             assert rel(t[k], r[k]) <= FIELD_TOL, k
 
 
+def small(nx, ny, P, steps, **kw):
+    """Spec for a small grid with the source and detector inside it."""
+    base = dict(nx=nx, ny=ny, npml=P, n_steps=steps, src_i=P + 2, src_j=ny // 2, det_i=P + 3,
+                det_j=ny // 2, x_lo=nx // 2, x_hi=nx - 2)
+    base.update(kw)
+    return F.Problem.from_spec(**base)
+
+
 def test_write_read_roundtrip(gpu):
-    prob = F.Problem.from_spec(nx=100, ny=77, npml=6, n_steps=5)
+    prob = small(100, 77, 6, 5)
     rng = np.random.default_rng(1)
     with F.Shot(prob, gpu) as shot:
         for w in FIELDS + PSI_FIELDS:
@@ -139,7 +147,7 @@ def test_write_read_roundtrip(gpu):
 
 
 def test_nonfinite_detection(gpu):
-    prob = F.Problem.from_spec(nx=64, ny=64, npml=4, n_steps=3)
+    prob = small(64, 64, 4, 3)
     with F.Shot(prob, gpu) as shot:
         shot.run(1, 1)
         assert shot.check_finite()
@@ -150,7 +158,7 @@ def test_nonfinite_detection(gpu):
 
 
 def test_run_range_errors(gpu):
-    prob = F.Problem.from_spec(nx=64, ny=64, npml=4, n_steps=10)
+    prob = small(64, 64, 4, 10)
     with F.Shot(prob, gpu) as shot:
         with pytest.raises(F.FdtdError) as e:
             shot.run(2, 3)  # must start at step 1
@@ -164,7 +172,7 @@ def test_run_range_errors(gpu):
 
 def test_invalid_setups_rejected(gpu):
     # detector on the PEC ring
-    prob = F.Problem.from_spec(nx=64, ny=64, npml=4, n_steps=3, det_i=0, det_j=5)
+    prob = small(64, 64, 4, 3, det_i=0, det_j=5)
     with pytest.raises(F.FdtdError) as e:
         F.Shot(prob, gpu)
     assert e.value.status == F.ERR_RANGE
