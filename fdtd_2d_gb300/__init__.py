@@ -148,6 +148,7 @@ def _lib():
         "fdtd2d_device_count": (C.c_int, []),
         "fdtd2d_run_timed": (C.c_int, [vp, C.c_int32, C.c_int32, _fp]),
         "fdtd2d_stability": (C.c_double, [C.POINTER(Setup)]),
+        "fdtd2d_check_finite_noalloc": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int64), C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)  # every declared entry point must be exported
@@ -366,6 +367,17 @@ class Shot:
             self.close()
         except Exception:
             pass
+
+
+def check_finite_noalloc(device_ptr: int, n: int, stream: int = 0) -> tuple[int, int]:
+    """Count NaN/Inf in a caller-owned device float array without allocating
+    (fdtd2d_check_finite_noalloc).  Returns (status, count): status is OK or
+    ERR_NONFINITE; other statuses raise."""
+    cnt = C.c_int64()
+    rc = _lib().fdtd2d_check_finite_noalloc(C.c_void_p(device_ptr), n, C.byref(cnt), C.c_void_p(stream))
+    if rc not in (OK, ERR_NONFINITE):
+        raise FdtdError(rc, "check_finite_noalloc")
+    return rc, int(cnt.value)
 
 
 def device_count() -> int:

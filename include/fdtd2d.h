@@ -180,6 +180,21 @@ int fdtd2d_write_field(fdtd2d_ctx *ctx, int which, const float *host);
 /* Device-side scan for NaN/Inf in Ez/Hx/Hy/Jz; FDTD2D_ERR_NONFINITE if any. */
 int fdtd2d_check_finite(fdtd2d_ctx *ctx);
 
+/* Allocation-free non-finite scan of a caller-owned device array.
+   No counterpart in the reference.  For callers that must not allocate GPU
+   memory (a host program that owns all device memory through its own pool,
+   or code whose latency budget cannot absorb a cudaMalloc/cudaFree): it
+   counts the NaN/Inf values in d_data[0..n) using a fixed 16 KiB scratch
+   array compiled into this library, so it calls no cudaMalloc or cudaFree.
+   Returns FDTD2D_OK when all values are finite, FDTD2D_ERR_NONFINITE when
+   some are not (count in *nonfinite if non-NULL), FDTD2D_ERR_RANGE when
+   n > 2^31 (the scratch covers at most 2^31 values per call).  `stream` is a
+   cudaStream_t (NULL = default stream); the call waits for it.  The first
+   call on a device resolves the scratch address for that device: make it
+   before capturing any stream into a CUDA graph.  All calls share the one
+   scratch array, so calls whose GPU work overlaps race; serialise them. */
+int fdtd2d_check_finite_noalloc(const float *d_data, int64_t n, int64_t *nonfinite, void *stream);
+
 /* Release everything.  Replaces DevMemoryFree (FDTD_2D_Full/kernel.cu:2820-2987). */
 int fdtd2d_destroy(fdtd2d_ctx *ctx);
 
