@@ -84,6 +84,7 @@ class Setup(C.Structure):
         ("rc_level", C.c_float), ("rc_edge0", C.c_float),
         ("line_n", C.c_int32), ("line_i0", C.c_int32), ("line_j", C.c_int32),
         ("line_first", C.c_int32), ("line_last", C.c_int32),
+        ("cover", C.c_int64 * 8),
     ]
 
 
@@ -146,6 +147,8 @@ def _lib():
         "fdtd2d_problem_free": (None, [vp]),
         "fdtd2d_run_settings": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int]),
         "fdtd2d_device_count": (C.c_int, []),
+        "fdtd2d_write_rc_lines": (C.c_int, [vp, _ip, C.c_int32, C.c_char_p]),
+        "fdtd2d_write_tof": (C.c_int, [vp, _fp, C.c_int32, C.c_char_p]),
         "fdtd2d_run_timed": (C.c_int, [vp, C.c_int32, C.c_int32, _fp]),
         "fdtd2d_stability": (C.c_double, [C.POINTER(Setup)]),
         "fdtd2d_check_finite_noalloc": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int64), C.c_void_p]),
@@ -260,6 +263,18 @@ class Problem:
 
     def device_bytes(self) -> int:
         return int(_lib().fdtd2d_device_bytes(self.setup_ptr))
+
+    def write_rc_lines(self, spd, out_dir) -> None:
+        """RC_Line.txt / TAU_Line.txt from wave-front rows spd[n][l] (row 0 = before step 1)."""
+        a = np.ascontiguousarray(spd, dtype=np.int32)
+        _check(_lib().fdtd2d_write_rc_lines(self._h, a.ctypes.data_as(_ip), a.shape[0], str(out_dir).encode()),
+               "write_rc_lines")
+
+    def write_tof(self, field, out_dir) -> None:
+        """Time-of-flight files from a saved Ez line field[t][i]."""
+        a = np.ascontiguousarray(field, dtype=np.float32)
+        _check(_lib().fdtd2d_write_tof(self._h, a.ctypes.data_as(_fp), a.shape[0], str(out_dir).encode()),
+               "write_tof")
 
     def stability(self) -> float:
         return float(_lib().fdtd2d_stability(self.setup_ptr))

@@ -7,6 +7,7 @@
 #include "internal.h"
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -377,6 +378,11 @@ int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
     CK(dalloc(c, &h.ctrace, (size_t)s->n_steps * std::max(1, s->n_comp) * 3));
   }
   if (c->dft) CK(dalloc(c, &h.dft, (size_t)s->n_det));
+
+  for (int k = 0; k < 8; ++k) {
+    const int64_t v = s->cover[k];
+    h.cov[k] = (s->medium != FDTD2D_MEDIUM_MATERIAL_ID || v == 0) ? INT64_MAX : (v < 0 ? 0 : v);
+  }
 
   // wave-front tracker and line probe
   if (s->n_rc > 0) {

@@ -131,6 +131,7 @@ extern "C" int fdtd2d_run_settings(const char* ini_path, const char* out_dir, in
   }
 
   fdtd2d_ctx* ctx = nullptr;
+  if (device < 0) device = ip.gpu_device;  // [hardware] GPU_device, as cudaSetDevice(GPU_device)
   rc = fdtd2d_create(&s, device, &ctx);
   if (rc) {
     fdtd2d_problem_free(handle);

@@ -601,6 +601,18 @@ int build_from_ini(const IniParams& ip, Problem& p) {
     }
   }
 
+  // Launch coverage (kernel.cu:2027-2033 with 1024-thread blocks of 512x2):
+  // the bulk grid has floor(floor(Imax*Jmax/1024)/2) x 3 blocks, the I-strip
+  // grid floor(PML_SIZE*Jmax/1024) blocks, the J-strip grid
+  // floor(Imax*PML_SIZE/1024) blocks.
+  {
+    const int64_t bulk = (int64_t)(((int64_t)nx * ny / 1024) / 2) * 3 * 1024;
+    const int64_t pml_i = (int64_t)((int64_t)P * ny / 1024) * 1024;
+    const int64_t pml_j = (int64_t)((int64_t)nx * P / 1024) * 1024;
+    const int64_t cov[8] = {bulk, pml_j, bulk, pml_i, bulk, bulk, pml_i, pml_j};
+    for (int k = 0; k < 8; ++k) p.s.cover[k] = cov[k] > 0 ? cov[k] : -1;  // -1: no thread at all
+  }
+
   build_cpml(p, nx, ny, P, ip.dx, ip.dy, dt, 0.75, 15.0, 0.24, 3, 1);
   p.s.n_rc = (int32_t)p.rc_scan.size();
   p.s.rc_scan_i = p.rc_scan.empty() ? nullptr : p.rc_scan.data();

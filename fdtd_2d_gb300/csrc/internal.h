@@ -74,6 +74,9 @@ struct DevShot {
   float* trace;               // [n_steps][n_det]
   float* ctrace;              // [n_steps][n_comp][3]  (Ez, Hx, Hy)
   double2* dft;               // [n_det]
+  // Reference launch coverage per update kernel (material medium only):
+  // a cell update with reference thread index l >= cov[k] is skipped.
+  long long cov[8];
 };
 
 enum FieldId : int { kEz = 0, kHx = 1, kHy = 2, kJz = 3 };

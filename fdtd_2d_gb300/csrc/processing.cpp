@@ -22,6 +22,7 @@
 #include "problem.h"
 
 namespace fdtd2d {
+Problem* problem_internal(fdtd2d_problem* p);
 
 namespace {
 
@@ -288,3 +289,26 @@ int rc_run_and_write(fdtd2d_ctx* ctx, const Problem& p, const std::string& dir, 
 }
 
 }  // namespace fdtd2d
+
+using namespace fdtd2d;
+
+extern "C" int fdtd2d_write_rc_lines(const fdtd2d_problem* h, const int32_t* spd, int32_t n_rows,
+                                     const char* out_dir) {
+  Problem* p = problem_internal(const_cast<fdtd2d_problem*>(h));
+  if (!p || !spd || n_rows < 1 || !p->from_ini) return FDTD2D_ERR_INVALID;
+  const int nl = p->s.n_rc;
+  if (nl <= 0) return FDTD2D_ERR_STATE;
+  std::vector<int> rows(spd, spd + (size_t)n_rows * nl);
+  return rc_post_write(*p, rows, n_rows, nl, out_dir ? out_dir : "");
+}
+
+extern "C" int fdtd2d_write_tof(const fdtd2d_problem* h, const float* field, int32_t times,
+                                const char* out_dir) {
+  Problem* p = problem_internal(const_cast<fdtd2d_problem*>(h));
+  if (!p || (!field && times > 0) || times < 0 || !p->from_ini) return FDTD2D_ERR_INVALID;
+  const int sz = p->ini.p_size_i;
+  std::vector<std::vector<float>> f(times, std::vector<float>(std::max(0, sz)));
+  for (int t = 0; t < times; ++t)
+    for (int i = 0; i < sz; ++i) f[t][i] = field[(size_t)t * sz + i];
+  return processing_run(*p, f, out_dir ? out_dir : "");
+}

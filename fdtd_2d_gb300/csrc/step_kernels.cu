@@ -123,6 +123,15 @@ struct MediumRow<1> {
   }
 };
 
+// Reference launch coverage (fdtd2d_setup.cover): only the material-ID
+// kernel, which serves the Settings.ini path, carries the checks.
+enum CoverKernel : int { kCovHx = 0, kCovHxPml, kCovHy, kCovHyPml, kCovJz, kCovEz, kCovEzPmlI, kCovEzPmlJ };
+
+template <int MEDIUM>
+__device__ __forceinline__ bool covered(const DevShot& S, int k, long long l) {
+  return MEDIUM == 0 || l < S.cov[k];
+}
+
 // DB of one H cell (scalar path).
 template <int MEDIUM>
 __device__ __forceinline__ void h_coef(const DevShot& S, const MatH* mat_h, const uint8_t* ids,
@@ -144,12 +153,13 @@ __device__ float hy_cell(const DevShot& S, const MatH* mat_h, int par, int c, in
   float da, db;
   h_coef<MEDIUM>(S, mat_h, S.id2, off, da, db);
   const float hyo = field_ptr(S, kHy, par)[off];
-  float h = upd_h(da, hyo, db, ez_c1, ez_c, S.den_hx[c]);
+  float h = covered<MEDIUM>(S, kCovHy, (long long)j * (S.nx - 1) + c)
+                ? upd_h(da, hyo, db, ez_c1, ez_c, S.den_hx[c]) : hyo;
   const int P = S.npml;
   int side = -1, r = 0;
   if (c <= P - 2) { side = 0; r = c; }
   else if (c >= S.nx - P && c <= S.nx - 2) { side = 1; r = S.nx - 2 - c; }
-  if (side >= 0) {
+  if (side >= 0 && covered<MEDIUM>(S, kCovHyPml, (long long)j * (P - 1) + r)) {
     const float* tb = S.cpml + (side ? kBhX2 : kBhX1) * P;
     const float* tc = S.cpml + (side ? kChX2 : kChX1) * P;
     const float psi = S.psi[par * S.psi_buf + S.o_hyx + ((int64_t)side * S.ny + j) * P + r];
@@ -170,7 +180,8 @@ __device__ __forceinline__ void hx_row(const DevShot& S, const MediumRow<MEDIUM>
   const int nx = S.nx;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    out[k] = (i + k <= nx - 2) ? upd_h(m.dax(k), hxo[k], m.dbx(k), ezj[k], ezj1[k], den) : hxo[k];
+    out[k] = (i + k <= nx - 2 && covered<MEDIUM>(S, kCovHx, (long long)j * (nx - 1) + i + k))
+                 ? upd_h(m.dax(k), hxo[k], m.dbx(k), ezj[k], ezj1[k], den) : hxo[k];
   }
   const int P = S.npml;
   int side = -1, r = 0;
@@ -185,7 +196,7 @@ __device__ __forceinline__ void hx_row(const DevShot& S, const MediumRow<MEDIUM>
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       pn[k] = psi[k];
-      if (i + k <= nx - 2) {
+      if (i + k <= nx - 2 && covered<MEDIUM>(S, kCovHxPml, (long long)r * (nx - 1) + i + k)) {
         pn[k] = upd_psi(b, psi[k], c, ezj[k], ezj1[k], S.dy);
         out[k] = __fmaf_rn(m.dbx(k), pn[k], out[k]);
       }
@@ -275,7 +286,8 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
     float hyn[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      hyn[k] = (i + k <= nx - 2) ? upd_h(m.day(k), hyo[k], m.dby(k), ezr[k], ezc[k], dhx[k]) : hyo[k];
+      hyn[k] = (i + k <= nx - 2 && covered<MEDIUM>(S, kCovHy, (long long)j * (nx - 1) + i + k))
+                   ? upd_h(m.day(k), hyo[k], m.dby(k), ezr[k], ezc[k], dhx[k]) : hyo[k];
     }
     // Hy x-strip CPML (edge columns only).
     if (act && (i <= P - 2 || i + 3 >= nx - P)) {
@@ -286,7 +298,7 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
         int side = -1, r = 0;
         if (c <= P - 2) { side = 0; r = c; }
         else if (c >= nx - P && c <= nx - 2) { side = 1; r = nx - 2 - c; }
-        if (side >= 0) {
+        if (side >= 0 && covered<MEDIUM>(S, kCovHyPml, (long long)j * (P - 1) + r)) {
           const float b = S.cpml[(side ? kBhX2 : kBhX1) * P + r];
           const float cc = S.cpml[(side ? kChX2 : kChX1) * P + r];
           const int64_t po = S.o_hyx + ((int64_t)side * ny + j) * P + r;
@@ -314,9 +326,10 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
     for (int k = 0; k < 4; ++k) {
       const int c = i + k;
       const bool in = row_in && c >= 1 && c <= nx - 2;
-      jzw4[k] = in ? upd_j(S.ja, jzo[k], m.kp[k], ezc[k]) : jzo[k];
+      const long long le = (long long)(j - 1) * (nx - 2) + (c - 1);
+      jzw4[k] = (in && covered<MEDIUM>(S, kCovJz, le)) ? upd_j(S.ja, jzo[k], m.kp[k], ezc[k]) : jzo[k];
       float e = ezc[k];
-      if (in) {
+      if (in && covered<MEDIUM>(S, kCovEz, le)) {
         e = m.pec(k) ? 0.f
                      : upd_e(m.cA(k), ezc[k], m.cB(k), __fsub_rn(hyn[k], hyl4[k]), dex[k],
                              __fsub_rn(hxp[k], hxn[k]), dey, jzw4[k]);
@@ -331,7 +344,7 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
         int side = -1, r = 0;
         if (c >= 1 && c <= P - 1) { side = 0; r = c; }
         else if (c >= nx - P && c <= nx - 2) { side = 1; r = nx - 1 - c; }
-        if (side >= 0) {
+        if (side >= 0 && covered<MEDIUM>(S, kCovEzPmlI, (long long)(j - 1) * (P - 1) + (r - 1))) {
           const float b = S.cpml[(side ? kBeX2 : kBeX1) * P + r];
           const float cc = S.cpml[(side ? kCeX2 : kCeX1) * P + r];
           const int64_t po = S.o_ezx + ((int64_t)side * ny + j) * P + r;
@@ -353,7 +366,7 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
       for (int k = 0; k < 4; ++k) {
         const int c = i + k;
         pn[k] = psi[k];
-        if (c >= 1 && c <= nx - 2) {
+        if (c >= 1 && c <= nx - 2 && covered<MEDIUM>(S, kCovEzPmlJ, (long long)(r - 1) * (nx - 2) + (c - 1))) {
           pn[k] = upd_psi(b, psi[k], cc, hxp[k], hxn[k], S.dy);
           ezw4[k] = __fmaf_rn(m.cB(k), pn[k], ezw4[k]);
         }

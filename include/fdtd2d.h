@@ -136,6 +136,16 @@ typedef struct fdtd2d_setup {
        FDTD_2D_Full/kernel.cu:666-688): Ez(line_i0 .. line_i0+line_n-1, line_j)
        is kept for every step in [line_first, line_last].                        */
     int32_t line_n, line_i0, line_j, line_first, line_last;
+
+    /* Launch coverage of the reference's eight update kernels, in launch
+       order: Hx, Hx y-CPML, Hy, Hy x-CPML, Jz, Ez, Ez x-CPML, Ez y-CPML
+       (FDTD_2D_Full/kernel.cu:2075-2121).  The reference sizes these grids with
+       floor divisions (kernel.cu:2027-2033), so on small grids the threads with
+       linear index l >= cover[k] do not exist and those cells are not updated.
+       A cell update whose reference thread index is >= cover[k] is skipped
+       here too; 0 means every cell is updated, a negative value none.
+       Honoured by the material-ID medium (the Settings.ini path).             */
+    int64_t cover[8];
 } fdtd2d_setup;
 
 /* ---- single shot (the reference's plain run) ------------------------------ */
@@ -269,6 +279,18 @@ int fdtd2d_problem_from_ini(const char *ini_path, fdtd2d_problem **out);
 
 const fdtd2d_setup *fdtd2d_problem_setup(const fdtd2d_problem *p);
 void fdtd2d_problem_free(fdtd2d_problem *p);
+
+/* Host post-processing of the drop-in driver, callable on its own.
+   fdtd2d_write_rc_lines: wave-front rows spd[n][l] (n = 0..n_rows-1, row 0 =
+   before step 1, as the reference's PspdLine) -> RC_Line.txt and
+   TAU_Line.txt in out_dir (RClineFilterPostTime, CalculateRCfromPwrLines,
+   CalculateTaufromPwrLines, FDTD_2D_Full/kernel.cu:3188-3270).
+   fdtd2d_write_tof: saved Ez line field[t][i] (t < times, i < SizeI) ->
+   the time-of-flight files (processing_core, FDTD_2D_Full/processing.cu:6-144).
+   Both use the Settings.ini parameters the problem was built from.          */
+int fdtd2d_write_rc_lines(const fdtd2d_problem *p, const int32_t *spd, int32_t n_rows,
+                          const char *out_dir);
+int fdtd2d_write_tof(const fdtd2d_problem *p, const float *field, int32_t times, const char *out_dir);
 
 /* Whole reference program on top of this ABI: Settings.ini in, the reference's
    output files (Detect.txt, detAll.txt, detEz/Hx/Hy.txt, Ez.txt,

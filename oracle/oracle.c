@@ -11,10 +11,12 @@
  * this library, and only as the checker / the baseline.
  *
  * Parity status: pinned against the reference program itself, compiled from
- * its own sources for the CPU by oracle/ref/build_ref.sh into oracle/_ref/
- * (its CUDA kernels run serially on the host through a launch shim); the
- * committed vectors in tests/golden/ come from that build.
+ * its own sources for the CPU by oracle/ref_build.py into oracle/_ref/ (its
+ * CUDA kernels run serially on the host through oracle/ref_shim/); the
+ * committed vectors in tests/golden/ come from that build
+ * (tests/golden/make_golden.py).
  */
+#include <limits.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>

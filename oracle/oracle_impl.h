@@ -36,6 +36,8 @@ typedef struct NAME(state) {
     float *trace, *ctrace;
     double *dft_re, *dft_im, dft_fdt;
     int dft;
+    /* reference launch coverage (fdtd2d_setup.cover), material medium only */
+    long long cov[8];
 } NAME(state);
 
 static void NAME(free_state)(NAME(state) *o) {
@@ -62,6 +64,10 @@ static NAME(state) *NAME(create)(const fdtd2d_setup *s) {
     o = (NAME(state) *)calloc(1, sizeof(*o));
     if (!o) return NULL;
     o->nx = nx; o->ny = ny; o->P = P; o->n_steps = s->n_steps; o->step = 0;
+    for (k = 0; k < 8; ++k) {
+        const long long v = s->cover[k];
+        o->cov[k] = (s->medium != FDTD2D_MEDIUM_MATERIAL_ID || v == 0) ? LLONG_MAX : (v < 0 ? 0 : v);
+    }
     o->medium = s->medium;
     o->dt = (REAL)s->dt;
     /* the psi kernels receive dx, dy as float arguments */
@@ -201,6 +207,7 @@ static void NAME(step)(NAME(state) *o, int n) {
     for (j = 0; j <= ny - 2; ++j)
         for (i = 0; i <= nx - 2; ++i) {
             const size_t c = (size_t)j * nx + i;
+            if ((long long)j * (nx - 1) + i >= o->cov[0]) continue;
             hx[c] = o->da1[c] * hx[c] + o->db1[c] * ((ez[c] - ez[c + nx]) * o->den_hy[j]);
         }
     /* Dev_HxPML_Jdir_Calc (kernel.cu:198-240): j in [0,P-2], mirror jj = ny-2-j */
@@ -209,6 +216,7 @@ static void NAME(step)(NAME(state) *o, int n) {
         for (i = 0; i <= nx - 2; ++i) {
             const int jj = ny - 2 - j;
             const size_t c1 = (size_t)j * nx + i, c2 = (size_t)jj * nx + i, p = (size_t)j * nx + i;
+            if ((long long)j * (nx - 1) + i >= o->cov[1]) continue;
             o->phxy1[p] = o->bh_y_1[j] * o->phxy1[p] + o->ch_y_1[j] * (ez[c1] - ez[c1 + nx]) / o->dy;
             hx[c1] = hx[c1] + o->db1[c1] * o->phxy1[p];
             o->phxy2[p] = o->bh_y_2[j] * o->phxy2[p] + o->ch_y_2[j] * (ez[c2] - ez[c2 + nx]) / o->dy;
@@ -219,6 +227,7 @@ static void NAME(step)(NAME(state) *o, int n) {
     for (j = 0; j <= ny - 2; ++j)
         for (i = 0; i <= nx - 2; ++i) {
             const size_t c = (size_t)j * nx + i, h = (size_t)j * hyp + i;
+            if ((long long)j * (nx - 1) + i >= o->cov[2]) continue;
             hy[h] = o->da2[c] * hy[h] + o->db2[c] * ((ez[c + 1] - ez[c]) * o->den_hx[i]);
         }
     /* Dev_HyPML_Idir_Calc (kernel.cu:321-362): i in [0,P-2], mirror ii = nx-2-i */
@@ -228,6 +237,7 @@ static void NAME(step)(NAME(state) *o, int n) {
             const int ii = nx - 2 - i;
             const size_t c1 = (size_t)j * nx + i, c2 = (size_t)j * nx + ii;
             const size_t p = (size_t)j * (P - 1) + i;
+            if ((long long)j * (P - 1) + i >= o->cov[3]) continue;
             o->phyx1[p] = o->bh_x_1[i] * o->phyx1[p] + o->ch_x_1[i] * (ez[c1 + 1] - ez[c1]) / o->dx;
             hy[(size_t)j * hyp + i] = hy[(size_t)j * hyp + i] + o->db2[c1] * o->phyx1[p];
             o->phyx2[p] = o->bh_x_2[i] * o->phyx2[p] + o->ch_x_2[i] * (ez[c2 + 1] - ez[c2]) / o->dx;
@@ -238,6 +248,7 @@ static void NAME(step)(NAME(state) *o, int n) {
     for (j = 1; j <= ny - 2; ++j)
         for (i = 1; i <= nx - 2; ++i) {
             const size_t c = (size_t)j * nx + i;
+            if ((long long)(j - 1) * (nx - 2) + (i - 1) >= o->cov[4]) continue;
             if (o->drive3[c] > 0) jz[c] = o->jz_decay * jz[c] + o->drive3[c] * ez[c];
         }
     /* Dev_EzCalc (kernel.cu:413-451) */
@@ -245,6 +256,7 @@ static void NAME(step)(NAME(state) *o, int n) {
     for (j = 1; j <= ny - 2; ++j)
         for (i = 1; i <= nx - 2; ++i) {
             const size_t c = (size_t)j * nx + i, h = (size_t)j * hyp + i;
+            if ((long long)(j - 1) * (nx - 2) + (i - 1) >= o->cov[5]) continue;
             if (o->pec3[c]) {
                 ez[c] = 0;
             } else {
@@ -260,6 +272,7 @@ static void NAME(step)(NAME(state) *o, int n) {
             const int ii = nx - 1 - i;
             const size_t c1 = (size_t)j * nx + i, c2 = (size_t)j * nx + ii, p = (size_t)j * P + i;
             const size_t h1 = (size_t)j * hyp + i, h2 = (size_t)j * hyp + ii;
+            if ((long long)(j - 1) * (P - 1) + (i - 1) >= o->cov[6]) continue;
             o->pezx1[p] = o->be_x_1[i] * o->pezx1[p] + o->ce_x_1[i] * (hy[h1] - hy[h1 - 1]) / o->dx;
             ez[c1] = ez[c1] + o->cb3[c1] * o->pezx1[p];
             o->pezx2[p] = o->be_x_2[i] * o->pezx2[p] + o->ce_x_2[i] * (hy[h2] - hy[h2 - 1]) / o->dx;
@@ -271,6 +284,7 @@ static void NAME(step)(NAME(state) *o, int n) {
         for (i = 1; i <= nx - 2; ++i) {
             const int jj = ny - 1 - j;
             const size_t c1 = (size_t)j * nx + i, c2 = (size_t)jj * nx + i, p = (size_t)j * nx + i;
+            if ((long long)(j - 1) * (nx - 2) + (i - 1) >= o->cov[7]) continue;
             o->pezy1[p] = o->be_y_1[j] * o->pezy1[p] + o->ce_y_1[j] * (hx[c1 - nx] - hx[c1]) / o->dy;
             ez[c1] = ez[c1] + o->cb3[c1] * o->pezy1[p];
             o->pezy2[p] = o->be_y_2[j] * o->pezy2[p] + o->ce_y_2[j] * (hx[c2 - nx] - hx[c2]) / o->dy;

@@ -1,0 +1,95 @@
+"""The drop-in program (fdtd2d_run_settings: Settings.ini in, the reference's
+files out) on the GPU against the reference program's own output files for
+the same Settings.ini (tests/golden/, from the reference built for the CPU).
+
+Text files are compared number by number: the reference's FP32 kernels and
+ours round differently, so values agree to ~1e-5 of each column's largest
+magnitude; step counts, indices and layouts agree exactly.
+"""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import fdtd_2d_gb300 as F
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+CASES = sorted(p.name for p in GOLDEN.iterdir() if (p / "Settings.ini").exists())
+NUM = re.compile(r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[eE][-+]?\d+)?|nan|inf")
+
+
+def numbers(path: Path) -> np.ndarray:
+    return np.array([float(x) for x in NUM.findall(path.read_text())])
+
+
+def table(path: Path) -> list[list[float]]:
+    return [[float(x) for x in NUM.findall(line)] for line in path.read_text().splitlines() if line.strip()]
+
+
+@pytest.fixture(scope="module", params=CASES)
+def run(request, tmp_path_factory, gpu):
+    case = request.param
+    out = tmp_path_factory.mktemp(case)
+    F.run_settings(GOLDEN / case / "Settings.ini", out, gpu)
+    return case, out
+
+
+def test_trace_files(run):
+    case, out = run
+    for f in ("Detect.txt", "detAll.txt", "detEz.txt", "detHx.txt", "detHy.txt"):
+        ref_f = GOLDEN / case / f
+        if not ref_f.exists():
+            continue
+        mine, ref = table(out / f), table(ref_f)
+        assert len(mine) == len(ref), f
+        m = np.array([r for r in mine if r], dtype=float)
+        r = np.array([r for r in ref if r], dtype=float)
+        if f == "Detect.txt":
+            m, r = m[:, :2], r[:, :2]   # third column: no argument in the reference's printf
+        assert m.shape == r.shape, f
+        scale = np.maximum(np.abs(r).max(axis=0), 1e-30)
+        err = np.abs(m - r).max(axis=0) / scale
+        assert np.all(err <= 2e-5), (f, err)
+        # the time column is exact up to printf rounding
+        assert np.allclose(m[:, 0], r[:, 0], rtol=0, atol=1.5e-6 * max(1.0, abs(r[:, 0]).max()))
+
+
+def test_setup_files_exact(run):
+    case, out = run
+    for f in ("SourceP.txt", "FieldSaveDat.txt"):
+        assert (out / f).read_text() == (GOLDEN / case / f).read_text(), f
+    ref = (GOLDEN / case / "RcDet_data.txt").read_text().split()
+    assert (out / "RcDet_data.txt").read_text().split() == ref
+
+
+def test_field_slices(run):
+    case, out = run
+    ref_f = GOLDEN / case / "Ez.txt"
+    if not ref_f.exists():
+        pytest.skip("case saves no slices")
+    m, r = numbers(out / "Ez.txt"), numbers(ref_f)
+    assert m.shape == r.shape
+    assert np.abs(m - r).max() <= 2e-5 * np.abs(r).max() + 2e-6
+
+
+def test_wavefront_files(run):
+    case, out = run
+    m, r = table(out / "RC_Line.txt"), table(GOLDEN / case / "RC_Line.txt")
+    assert len(m) == len(r)
+    for a, b in zip(m, r):
+        assert abs(a[0] - b[0]) <= 1 and abs(a[1] - b[1]) <= 1.0 + 1e-3 * abs(b[1])
+    assert (out / "TAU_Line.txt").read_text() == (GOLDEN / case / "TAU_Line.txt").read_text()
+
+
+def test_tof_files(run):
+    case, out = run
+    for f in ("SD.txt", "CF.txt", "ARC.txt", "det_SD.txt", "det_CF.txt", "det_ARC.txt"):
+        ref_f = GOLDEN / case / f
+        if not ref_f.exists():
+            continue
+        m, r = np.loadtxt(out / f), np.loadtxt(ref_f)
+        assert m.shape == r.shape and np.array_equal(m[:, 0], r[:, 0]), f
+        assert np.mean(np.abs(m[:, 1] - r[:, 1]) <= 1) >= 0.95, f

@@ -1,0 +1,235 @@
+"""Host-side checks that need no GPU: the C ABI library loads and exports what
+include/fdtd2d.h declares, Settings.ini parsing follows the reference's inih
+rules, the setup precompute follows the reference's formulas, and the oracle
+behaves physically (CPML absorption, plasma cutoff reflection)."""
+import math
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import fdtd_2d_gb300 as F
+import oracle as O
+
+ROOT = Path(__file__).resolve().parent.parent
+C0 = 2.99792458e8
+MU0 = 4.0 * 3.14159265358979 * 1e-7
+EPS0 = 1.0 / (C0 * C0 * MU0)
+
+
+def test_library_exports_every_declared_entry_point():
+    header = (ROOT / "include" / "fdtd2d.h").read_text()
+    declared = set(re.findall(r"\b(fdtd2d_\w+)\s*\(", header))
+    out = subprocess.run(["nm", "-D", "--defined-only", str(F.LIB_PATH)], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (fdtd2d_\w+)", out))
+    missing = declared - exported
+    assert not missing, missing
+    lib = F.lib()
+    assert lib.fdtd2d_abi_version() == 1
+    assert lib.fdtd2d_strerror(F.ERR_RANGE).decode() == "index or step out of range"
+
+
+def test_no_device_is_reported_not_faked():
+    # On a machine without a GPU creating a shot must fail loudly.
+    if F.device_count() > 0:
+        pytest.skip("a CUDA device is present")
+    p = F.Problem.from_spec(nx=64, ny=64, npml=4, n_steps=2, src_j=32, det_j=32, x_lo=30, x_hi=60)
+    with pytest.raises(F.FdtdError) as e:
+        F.Shot(p)
+    assert e.value.status == F.ERR_NODEVICE
+
+
+def write_ini(tmp_path, body):
+    f = tmp_path / "Settings.ini"
+    f.write_bytes(body.encode())
+    return f
+
+
+MINIMAL = """[grid]
+Use_Exp_time = 0
+Imax = 40
+Jmax = 50
+Max_time = 30
+ds = 0.5
+dt_coef = 0.5
+Isource = 20
+Jsource = 10
+Idetect = 20
+Jdetect = 14
+[AESA]
+SIsize = 4
+SIdelta = 2
+DIsize = 4
+DIdelta = 2
+"""
+
+
+def test_dt_pin_from_reference_sample(tmp_path):
+    """The reference ships TAU_Line.txt from one run; column 2 / column 1 of
+    its first row is 3137.27 ps / 6582 steps = dt at ds = 0.5 mm, dt_coef = 0.5
+    (FDTD_2D_Full/TAU_Line.txt, Settings.ini:17-18, FDTD_cuda.cu:350)."""
+    p = F.Problem.from_ini(write_ini(tmp_path, MINIMAL))
+    dt = p.setup.dt
+    d = 0.5e-3
+    assert dt == (0.99 / (C0 * math.sqrt(3.0 / (d * d)))) * 0.5
+    assert abs(dt * 1e12 - 3137.27 / 6582) / (3137.27 / 6582) < 2e-6
+    assert p.n_steps == 30 and (p.nx, p.ny) == (80, 100)
+
+
+def test_ini_parser_rules(tmp_path):
+    body = ("﻿; comment line\n# hash comment\n[GRID]\nuse_exp_time = 0\nIMAX = 0x28 ; hex, inline comment\n"
+            "Jmax=50;not a comment without whitespace\nMax_time : 31\nds = 0.5\ndt_coef = 0.5\n"
+            "Isource = 20\nJsource = 10\nIdetect = 20\nJdetect = 14\nthis line is malformed\n"
+            "[AESA]\nSIsize = 4\n  continued value\nSIdelta = 2\nDIsize = 4\nDIdelta = 2\n"
+            "SPAngle = 7.5\n")
+    p = F.Problem.from_ini(write_ini(tmp_path, body))
+    s = p.setup
+    assert s.nx == 80            # 0x28 = 40 mm -> 80 cells
+    assert s.ny == 100           # "50;not..." parses as 50
+    assert s.n_steps == 31       # name : value form
+    # SPAngle 7.5 deg per element on top of 90
+    assert [s.src_phase_deg[e] for e in range(s.n_src)][:2] == [90.0, 97.5]
+
+
+def test_ini_missing_file_is_a_config_error(tmp_path):
+    with pytest.raises(F.FdtdError) as e:
+        F.Problem.from_ini(tmp_path / "nope.ini")
+    assert e.value.status == F.ERR_CONFIG
+
+
+def test_ini_unsupported_chamber_drawing_rejected(tmp_path):
+    with pytest.raises(F.FdtdError) as e:
+        F.Problem.from_ini(write_ini(tmp_path, MINIMAL + "[KameraConf]\nDraw2D=1\n"))
+    assert e.value.status == F.ERR_CONFIG
+
+
+def _grade(P, smax, kmax, amax, dt, m=3, ma=1, half=False):
+    """Reference CPML grading (FDTD_cuda.cu:1224-1460), restated in numpy with
+    the reference's FP32 storage of sigma/kappa/alpha."""
+    n = P - 1 if half else P
+    i = np.arange(n, dtype=np.float64)
+    depth = (P - 1 - i - (0.5 if half else 0.0)) / (P - 1.0)
+    sig = np.float32(smax * depth ** m)
+    alp = np.float32(amax * ((i + 0.5 if half else i) / (P - 1.0)) ** ma)
+    kap = np.float32(1.0 + (kmax - 1.0) * depth ** m)
+    rate = (sig / kap + alp).astype(np.float32)
+    b = np.float32(np.exp(-rate.astype(np.float64) * dt / EPS0))
+    den = (sig + kap * alp).astype(np.float32)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        c = np.where(den == 0, 0.0, sig.astype(np.float64) * (b.astype(np.float64) - 1.0) / den / kap)
+    return b, np.float32(c), kap
+
+
+@pytest.mark.parametrize("P", [10, 16, 32])
+def test_spec_cpml_tables_follow_reference_formulas(P):
+    p = F.Problem.from_spec(nx=128, ny=128, npml=P, n_steps=2, dx=0.25e-3, dy=0.25e-3, courant=0.99,
+                            src_i=P + 2, src_j=64, det_i=P + 3, det_j=64, x_lo=70, x_hi=120)
+    s = p.setup
+    eta = math.sqrt(MU0 / EPS0)
+    smax = 0.8 * 4 / (eta * 0.25e-3)
+    be, ce, ke = _grade(P, smax, 5.0, 0.05, s.dt)
+    bh, ch, kh = _grade(P, smax, 5.0, 0.05, s.dt, half=True)
+    assert np.array_equal(p.array("be_x_1", P), be) and np.array_equal(p.array("ce_y_2", P), ce)
+    assert np.array_equal(p.array("bh_y_1", P - 1), bh) and np.array_equal(p.array("ch_x_2", P - 1), ch)
+    den_ex = p.array("den_ex", 127)
+    assert np.array_equal(den_ex[:P], np.float32(1.0 / (ke.astype(np.float64) * 0.25e-3)))
+    assert np.all(den_ex[P:128 - P] == np.float32(1 / 0.25e-3))
+    # b in (0, 1), c <= 0: the recursion is a stable low-pass of the field difference
+    assert np.all((be > 0) & (be < 1)) and np.all(ce <= 0)
+
+
+def test_spec_medium_and_stability():
+    p = F.Problem.from_spec()  # the plain 512^2 workload
+    s = p.setup
+    assert s.cb == np.float32(s.dt / EPS0) and s.db == np.float32(s.dt / MU0) and s.ca == 1 and s.da == 1
+    ne = p.array("ne", 512 * 512).reshape(512, 512)
+    assert ne[:, :256].max() == 0 and abs(ne[0, 502] - 3e19) / 3e19 < 1e-6
+    assert np.allclose(ne[:, 379], 3e19 * (379 - 256) / 246, rtol=1e-6)
+    wp2 = 2.81794e-8 * 3e19 / EPS0
+    rho = (C0 * s.dt) ** 2 * 2 / (0.5e-3) ** 2 + wp2 * s.dt ** 2 / 4
+    assert abs(p.stability() - rho) / rho < 1e-6 and rho < 1.0
+    # at Courant 0.99 the same medium is unstable
+    assert F.Problem.from_spec(courant=0.99).stability() > 1.0
+
+
+def test_gaussian_random_field_statistics():
+    """tanh x (1 + rms g): g has zero mean, unit variance and correlation
+    exp(-r^2/l^2) (l = 40 cells) in expectation."""
+    n = 512
+    kw = dict(nx=n, ny=n, npml=10, n_steps=2, profile=3, ne_peak=3e19, x_center=-1e9, width=1.0,
+              grf_rms=0.1, grf_corr=40.0, seed=1001, src_j=256, det_j=256)
+    p = F.Problem.from_spec(**kw)
+    ne = p.array("ne", n * n).reshape(n, n).astype(np.float64)
+    # x_center far left: tanh = 1, so ne = 3e19 (1 + 0.1 g); no clamping at 10 sigma
+    g = (ne / 3e19 - 1.0) / 0.1
+    assert abs(g.mean()) < 0.2 and 0.8 < g.std() < 1.2
+    gc = g - g.mean()
+    corr40 = float(np.mean(gc[:, :-40] * gc[:, 40:]) / gc.var())
+    corr0 = float(np.mean(gc[:, :-1] * gc[:, 1:]) / gc.var())
+    assert 0.2 < corr40 < 0.55 and corr0 > 0.99   # exp(-1) = 0.37 at one correlation length
+    # deterministic across runs (and across x86/Arm: no libm in the RNG)
+    assert np.array_equal(F.Problem.from_spec(**kw).array("ne", n * n), p.array("ne", n * n))
+
+
+def test_phased_array_positions_and_steering():
+    p = F.Problem.from_spec(F.production_spec(nx=1024, ny=1024, x_center=600, src_j=475, det_j=475,
+                                              n_steps=10, profile=2))
+    s = p.setup
+    js = [s.src[e].j for e in range(16)]
+    assert js == [475 + 5 * e for e in range(16)] and all(s.src[e].i == 64 for e in range(16))
+    lam = C0 / 50e9
+    dphi = -360.0 * 5 * 0.25e-3 * math.sin(math.radians(15)) / lam
+    ph = [s.src_phase_deg[e] for e in range(16)]
+    assert np.allclose(np.diff(ph), dphi) and ph[0] == 90.0
+    env = p.array("envelope", 11)
+    t = np.arange(11) * s.dt
+    assert np.allclose(env, 0.5 * (1 - np.cos(np.pi * t / 2e-9)), rtol=1e-6, atol=1e-12)
+
+
+def test_oracle_cpml_absorbs_and_fp32_tracks_fp64():
+    """Vacuum pulse: once it has left, the CPML leaves < 1e-3 of the peak
+    energy behind; the FP32 restatement stays within 1e-5 of FP64 meanwhile."""
+    p = F.Problem.from_spec(nx=200, ny=200, npml=10, n_steps=1600, profile=0, src_i=100, src_j=100,
+                            det_i=105, det_j=100, pulse_width=0.05e-9)
+    o = O.Oracle(p.setup_ptr)
+    o32 = O.Oracle(p.setup_ptr, fp32=True)
+    peak = 0.0
+    for n in range(100, 1601, 100):
+        o.run(o.step + 1, n)
+        o32.run(o32.step + 1, n)
+        ez = o.read_field(F.FIELD_EZ)
+        e = float(np.linalg.norm(ez))
+        if e >= 0.1 * peak:
+            assert O.rel_l2(o32.read_field(F.FIELD_EZ), ez) < 1e-5
+        peak = max(peak, e)
+    assert e < 1e-3 * peak
+
+
+def test_oracle_overdense_plasma_reflects():
+    """30 GHz pulse onto a slab above the cutoff density nc = eps0 m_e w^2/e^2
+    (1.1e19 m^-3): the detector in front sees a strong echo; below cutoff far
+    less comes back."""
+    dx, tau = 0.5e-3, 0.05e-9
+
+    def echo(ne_peak):
+        p = F.Problem.from_spec(nx=400, ny=120, npml=10, n_steps=2200, profile=2, ne_peak=ne_peak,
+                                x_center=250, width=4, nu=0, src_i=60, src_j=60, det_i=120, det_j=60,
+                                pulse_width=tau, courant=0.9)
+        assert p.stability() < 1.0
+        dt = p.setup.dt
+        o = O.Oracle(p.setup_ptr)
+        o.run(1, 2200)
+        tr = o.traces()["det_ez"][:, 0]
+        t = np.arange(1, 2201) * dt
+        t_direct = 4 * tau + 60 * dx / C0                   # source -> detector
+        t_echo = 4 * tau + (190 + 130) * dx / C0            # source -> slab -> detector
+        direct = np.abs(tr[np.abs(t - t_direct) < 3 * tau]).max()
+        back = np.abs(tr[np.abs(t - t_echo) < 4 * tau]).max()
+        return float(back), float(direct)
+    nc = EPS0 * 9.10938e-31 * (2 * math.pi * 30e9) ** 2 / (1.602176634e-19) ** 2
+    hi, direct = echo(2 * 4 * nc)       # tanh plateau 4 nc
+    lo, _ = echo(2 * 0.05 * nc)         # 5 % of nc
+    assert hi > 0.2 * direct and hi > 5 * lo
