@@ -29,6 +29,7 @@ LIB_PATH = _HERE / "libfdtd2d.so"
 OK = 0
 ERR_INVALID, ERR_NOMEM, ERR_CUDA, ERR_NONFINITE, ERR_RANGE = -1, -2, -3, -4, -5
 ERR_IO, ERR_CONFIG, ERR_STATE, ERR_BUDGET, ERR_NODEVICE = -6, -7, -8, -9, -10
+ERR_TIMEOUT = -11
 
 MEDIUM_UNIFORM, MEDIUM_MATERIAL_ID = 0, 1
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2

@@ -10,6 +10,7 @@
 #include <climits>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -31,6 +32,8 @@ struct fdtd2d_ctx {
   int n_units = 0;
   int grid_warps = 0;
   int* d_flag = nullptr;
+  int* d_err = nullptr;     // device error word (bounded waits)
+  bool tma = false;         // shared-memory staged kernel (uniform medium)
   // wave-front tracker and line probe
   int n_rc = 0, rc_j_cut = 0;
   float rc_level = 0;
@@ -62,15 +65,15 @@ cudaError_t dalloc(fdtd2d_ctx* c, T** p, size_t count) {
   return cudaMemsetAsync(q, 0, count * sizeof(T), c->stream);
 }
 
-int pitch_for(int nx) { return (nx + 31) / 32 * 32; }
+int pitch_for(int nx) { return row_pitch(nx); }
 
 __global__ void drive_from_density(float* kp, int64_t pitch, int nx, int ny, float beta) {
-  // kp = beta * ne in place; cells without plasma (ne <= 0) get 0.
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)ny * pitch;
+  // kp = beta * ne in place over the nx x ny cells; no plasma (ne <= 0) -> 0.
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)ny * nx;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(t % pitch);
-    const float ne = kp[t];
-    kp[t] = (i < nx && ne > 0.f) ? beta * ne : 0.f;
+    const int64_t k = (t / nx) * pitch + (t % nx);
+    const float ne = kp[k];
+    kp[k] = ne > 0.f ? beta * ne : 0.f;
   }
 }
 
@@ -120,9 +123,9 @@ int validate(const fdtd2d_setup* s) {
   return FDTD2D_OK;
 }
 
-// Split rows [0, ny-1) x column blocks into at most `warps` equal units.
-std::vector<int4> make_units(int shot, int nx, int ny, int warps) {
-  const int cb = (nx + kCols - 1) / kCols;
+// Split rows [0, ny-1) x column blocks of `cols` into at most `warps` units.
+std::vector<int4> make_units(int shot, int nx, int ny, int warps, int cols = kCols) {
+  const int cb = (nx + cols - 1) / cols;
   const int rows = ny - 1;
   int strips = std::max(1, warps / cb);
   strips = std::min(strips, std::max(1, rows / 8));
@@ -132,7 +135,7 @@ std::vector<int4> make_units(int shot, int nx, int ny, int warps) {
     const int j0 = (int)((int64_t)rows * s / strips);
     const int j1 = (int)((int64_t)rows * (s + 1) / strips);
     if (j1 <= j0) continue;
-    for (int c = 0; c < cb; ++c) u.push_back(make_int4(shot, c * kCols, j0, j1));
+    for (int c = 0; c < cb; ++c) u.push_back(make_int4(shot, c * cols, j0, j1));
   }
   return u;
 }
@@ -156,6 +159,7 @@ const char* fdtd2d_strerror(int status) {
     case FDTD2D_ERR_STATE: return "call not valid in this state";
     case FDTD2D_ERR_BUDGET: return "request exceeds the memory budget";
     case FDTD2D_ERR_NODEVICE: return "no CUDA device";
+    case FDTD2D_ERR_TIMEOUT: return "a bounded device-side wait timed out";
     default: return "unknown error";
   }
 }
@@ -163,7 +167,7 @@ const char* fdtd2d_strerror(int status) {
 int64_t fdtd2d_device_bytes(const fdtd2d_setup* s) {
   if (!s) return -1;
   const int64_t pitch = pitch_for(s->nx);
-  const int64_t cells = pitch * s->ny;
+  const int64_t cells = buffer_floats(s->nx, s->ny);
   const int64_t P = s->npml;
   int64_t b = cells * 4 * 8;                                       // 4 fields x 2
   b += (s->medium == FDTD2D_MEDIUM_UNIFORM) ? (s->ne ? cells * 4 : 0) : cells * 3;
@@ -194,7 +198,7 @@ int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
   }
   const int nx = s->nx, ny = s->ny, P = s->npml;
   const int pitch = pitch_for(nx);
-  const int64_t cells = (int64_t)pitch * ny;
+  const int64_t cells = buffer_floats(nx, ny);
   c->nx = nx; c->ny = ny; c->pitch = pitch; c->npml = P; c->n_steps = s->n_steps;
   c->n_det = s->n_det; c->n_comp = s->n_comp; c->record = s->record_traces ? 1 : 0;
   c->medium = s->medium;
@@ -223,14 +227,17 @@ int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
   h.o_hyx = h.o_ezy + (int64_t)2 * P * pitch;
   h.o_ezx = h.o_hyx + (int64_t)2 * ny * P;
   h.psi_buf = h.o_ezx + (int64_t)2 * ny * P;
-  CK(dalloc(c, &h.psi, (size_t)h.psi_buf * 2));
+  // + slack for the staged kernel's whole-band copies of the last psi_Ezy row
+  // and the 16-byte round-up of its x-strip row copies
+  CK(dalloc(c, &h.psi, (size_t)h.psi_buf * 2 + 1024));
 
   // medium
   if (s->medium == FDTD2D_MEDIUM_UNIFORM) {
     h.ca = s->ca; h.cb = s->cb; h.da = s->da; h.db = s->db;
     if (s->ne) {
-      float* kp = nullptr;
-      CK(dalloc(c, &kp, cells));
+      float* kp_buf = nullptr;
+      CK(dalloc(c, &kp_buf, cells));
+      float* kp = kp_buf + kMargin;
       CK(cudaMemcpy2DAsync(kp, pitch * sizeof(float), s->ne, nx * sizeof(float), nx * sizeof(float),
                            ny, cudaMemcpyHostToDevice, c->stream));
       drive_from_density<<<1024, 256, 0, c->stream>>>(kp, pitch, nx, ny, (float)beta);
@@ -249,7 +256,7 @@ int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
             fdtd2d_destroy(c);
             return FDTD2D_ERR_RANGE;
           }
-          ids[(size_t)m * cells + (size_t)j * pitch + i] = (uint8_t)v;
+          ids[(size_t)m * cells + kMargin + (size_t)j * pitch + i] = (uint8_t)v;
         }
       }
     }
@@ -257,7 +264,7 @@ int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
     CK(dalloc(c, &d_ids, ids.size()));
     CK(cudaMemcpyAsync(d_ids, ids.data(), ids.size(), cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    h.id1 = d_ids; h.id2 = d_ids + cells; h.id3 = d_ids + 2 * cells;
+    h.id1 = d_ids + kMargin; h.id2 = d_ids + cells + kMargin; h.id3 = d_ids + 2 * cells + kMargin;
     std::vector<MatE> me(256);
     std::vector<MatH> mh(256);
     for (int m = 0; m < 256; ++m) {
@@ -407,13 +414,28 @@ int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
 
   CK(dalloc(c, &c->d_shot, 1));
   CK(cudaMemcpyAsync(c->d_shot, &h, sizeof(DevShot), cudaMemcpyHostToDevice, c->stream));
-  c->grid_warps = resident_warps(c->medium, device);
-  std::vector<int4> units = make_units(0, nx, ny, c->grid_warps);
+  // Kernel: the shared-memory staged step for the uniform medium with a CPML
+  // of at most tma_max_pml() cells, unless FDTD2D_KERNEL=stream selects the
+  // register-streaming one; the material-ID medium (Settings.ini path) and
+  // deeper CPMLs always stream.
+  {
+    const char* k = std::getenv("FDTD2D_KERNEL");
+    c->tma = (c->medium == FDTD2D_MEDIUM_UNIFORM) && P <= tma_max_pml() && !(k && std::strcmp(k, "stream") == 0);
+  }
+  std::vector<int4> units;
+  if (c->tma) {
+    c->grid_warps = tma_resident_ctas(device);  // CTAs for this path
+    units = make_units(0, nx, ny, c->grid_warps, tma_band_cols());
+  } else {
+    c->grid_warps = resident_warps(c->medium, device);
+    units = make_units(0, nx, ny, c->grid_warps);
+  }
   c->n_units = (int)units.size();
   CK(dalloc(c, &c->d_units, units.size()));
   CK(cudaMemcpyAsync(c->d_units, units.data(), units.size() * sizeof(int4), cudaMemcpyHostToDevice,
                      c->stream));
   CK(dalloc(c, &c->d_flag, 1));
+  CK(dalloc(c, &c->d_err, 1));
   CK(cudaStreamSynchronize(c->stream));
 #undef CK
   *out = c;
@@ -425,7 +447,8 @@ int fdtd2d_run(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
   if (n_first != c->step + 1 || n_last < n_first - 1 || n_last > c->n_steps) return FDTD2D_ERR_RANGE;
   cudaSetDevice(c->device);
   for (int32_t n = n_first; n <= n_last; ++n) {
-    cudaError_t e = launch_step(c->d_shot, c->d_units, c->n_units, n, c->medium, c->grid_warps, c->stream);
+    cudaError_t e = c->tma ? launch_step_tma(c->h, c->d_units, c->n_units, n, c->grid_warps, c->d_err, c->stream)
+                           : launch_step(c->h, c->d_units, c->n_units, n, c->medium, c->grid_warps, c->stream);
     if (e != cudaSuccess) return fail_cuda(c, e);
     ++c->launches;
     const float* ez_now = field_ptr(c->h, kEz, n & 1);
@@ -474,6 +497,7 @@ int fdtd2d_run_timed(fdtd2d_ctx* c, int32_t n_first, int32_t n_last, float* elap
     if (e == cudaSuccess) e = cudaEventElapsedTime(elapsed_ms, a, b);
     if (e != cudaSuccess) rc = fail_cuda(c, e);
   }
+  if (rc == FDTD2D_OK) rc = fdtd2d_synchronize(c);
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   return rc;
@@ -497,9 +521,12 @@ double fdtd2d_stability(const fdtd2d_setup* s) {
 
 int fdtd2d_synchronize(fdtd2d_ctx* c) {
   if (!c) return FDTD2D_ERR_INVALID;
+  cudaSetDevice(c->device);
   cudaError_t e = cudaStreamSynchronize(c->stream);
+  int err = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return fail_cuda(c, e);
-  return FDTD2D_OK;
+  return err == kErrWaitTimeout ? FDTD2D_ERR_TIMEOUT : (err ? FDTD2D_ERR_CUDA : FDTD2D_OK);
 }
 
 int fdtd2d_current_step(const fdtd2d_ctx* c, int32_t* n) {
@@ -646,10 +673,10 @@ int fdtd2d_check_finite(fdtd2d_ctx* c) {
   if (!c) return FDTD2D_ERR_INVALID;
   cudaSetDevice(c->device);
   const int b = c->step & 1;
-  const int64_t cells = (int64_t)c->pitch * c->ny;
+  const int64_t cells = c->h.cells;  // whole buffers, margins included (they stay 0)
   cudaError_t e = cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream);
-  const float* arrs[4] = {field_ptr(c->h, kEz, b), field_ptr(c->h, kHx, b), field_ptr(c->h, kHy, b),
-                          field_ptr(c->h, kJz, b)};
+  const float* arrs[4] = {field_ptr(c->h, kEz, b) - kMargin, field_ptr(c->h, kHx, b) - kMargin,
+                          field_ptr(c->h, kHy, b) - kMargin, field_ptr(c->h, kJz, b) - kMargin};
   for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
     e = launch_nonfinite(arrs[k], cells, c->d_flag, c->stream);
     ++c->launches;

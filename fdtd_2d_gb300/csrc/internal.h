@@ -42,8 +42,10 @@ struct DevShot {
   const MatE* mat_e;          // [256]
   const MatH* mat_h;          // [256]
 
-  // Field slab [4 fields (Ez, Hx, Hy, Jz)][2 ping-pong buffers][ny][pitch]:
-  // field f, buffer b starts at fld + (2*f + b)*cells.
+  // Field slab [4 fields (Ez, Hx, Hy, Jz)][2 ping-pong buffers][cells]: each
+  // buffer holds ny rows of `pitch` floats; column 0 of row 0 sits kMargin
+  // floats into the buffer, so every row has a zero margin on both sides that
+  // bulk row copies may read as halo.  field_ptr() points at column 0.
   float* fld;
   int64_t cells;
   // CPML psi slab [2 ping-pong buffers][psi_buf]; within a buffer (side s = 0
@@ -81,23 +83,45 @@ struct DevShot {
 
 enum FieldId : int { kEz = 0, kHx = 1, kHy = 2, kJz = 3 };
 
+// Left margin of every field row (floats); also the right margin pitch adds.
+constexpr int kMargin = 32;
+
 __host__ __device__ inline float* field_ptr(const DevShot& S, int f, int b) {
-  return S.fld + (int64_t)(2 * f + b) * S.cells;
+  return S.fld + (int64_t)(2 * f + b) * S.cells + kMargin;
 }
+
+// Row pitch (floats) for nx columns: 128-byte rows with kMargin on each side.
+inline int row_pitch(int nx) { return (nx + 31) / 32 * 32 + 2 * kMargin; }
+
+// Floats per field buffer: ny rows plus slack so that a bulk copy of a row
+// segment that runs past the last row's margin stays inside the allocation.
+inline int64_t buffer_floats(int nx, int ny) { return (int64_t)(ny + 2) * row_pitch(nx) + 1024; }
 
 // A unit of work is one warp-wide column block (128 cells) of one shot over a
 // contiguous range of rows: (shot, i0, j0, j1).
 constexpr int kCols = 128;
 constexpr int kThreads = 256;
 
-// Launch the fused step for steps n (global numbering) of every shot listed
-// in `units`.  medium: 0 uniform, 1 material ids.
-cudaError_t launch_step(const DevShot* shots, const int4* units, int n_units,
+// Launch the fused register-streaming step for step n_global (minus the
+// shot's base_n) of one shot over its `units`.  medium: 0 uniform, 1 ids.
+cudaError_t launch_step(const DevShot& shot, const int4* units, int n_units,
                         int n_global, int medium, int n_warps_grid,
                         cudaStream_t stream);
 
 // Launch capacity: number of warps the step kernel keeps resident at once.
 int resident_warps(int medium, int device);
+
+// Device error codes written by kernels with bounded waits.
+enum DeviceError : int { kErrNone = 0, kErrWaitTimeout = 1 };
+
+// Shared-memory staged step (step_tma.cu), uniform medium: one CTA per unit
+// of kBand columns.
+int tma_band_cols();
+int tma_max_pml();   // largest CPML depth the staged kernel takes
+size_t tma_smem_bytes();
+int tma_resident_ctas(int device);
+cudaError_t launch_step_tma(const DevShot& shot, const int4* units, int n_units, int n_global, int max_ctas,
+                            int* err, cudaStream_t stream);
 
 // Tabulate s_e(n) = scale*env[n]*cos(2*pi_c*(beta/2 t^2 + f0 t + phase_e)),
 // t = n*dt, for n = 0..n_steps, and the DFT twiddles, in FP64.

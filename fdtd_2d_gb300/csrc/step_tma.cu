@@ -1,0 +1,497 @@
+// Fused TMz step, shared-memory staged with bulk asynchronous copies (TMA).
+//
+// Same arithmetic and the same ping-pong buffers as step_stream_kernel, but
+// the rows reach the warps through shared memory: a CTA of kTmaWarps warps
+// owns a 512-column band of one shot and walks a range of rows; one thread
+// keeps a ring of kStages row stages filled with cp.async.bulk copies
+// (Ez(j+1), Hx(j), Hy(j), Jz(j), plasma drive (j), each the 520-float row
+// segment [c0-4, c0+516), halo included, in one copy), completion tracked by
+// an mbarrier per stage.  Bytes in flight per SM are then set by the ring
+// depth (3 stages x 10.4 KB per CTA, 4 CTAs per SM) instead of by registers
+// per warp, and the warp-edge neighbours (Ez(c0-1), Ez(c0+512), Hy(c0-1))
+// come from shared memory instead of dependent global loads.
+//
+// Every wait is bounded: after kSpinLimit failed polls the kernel records
+// kErrWaitTimeout in the shot's error word, waits (bounded) for the copies it
+// issued, and returns; the host reports FDTD2D_ERR_TIMEOUT.
+#include "internal.h"
+#include "step_common.cuh"
+
+namespace fdtd2d {
+
+namespace {
+
+constexpr int kTmaWarps = 4;
+constexpr int kTmaThreads = kTmaWarps * 32;
+constexpr int kBand = kTmaWarps * kCols;       // 512 columns per CTA
+constexpr int kSeg = kBand + 8;                // staged floats per array row
+constexpr int kArrays = 5;                     // Ez(j+1), Hx, Hy, Jz, drive
+constexpr int kStages = 3;
+// A stage holds one row j of the band: the 5 field segments; the psi_Hxy and
+// psi_Ezy rows of the band (CPML y-strip rows only); and the row's x-strip
+// psi rows (psi_Hyx side 0/1, psi_Ezx side 0/1; bands touching a strip only),
+// each copied from its 16-byte-aligned start, kXSlot floats reserved.
+constexpr int kPsiOff = kArrays * kSeg;
+constexpr int kXOff = kPsiOff + 2 * kBand;
+constexpr int kXSlot = 128;
+constexpr int kStageFloats = kXOff + 4 * kXSlot;
+constexpr uint32_t kSegBytes = kSeg * 4;
+constexpr uint32_t kPsiBytes = kBand * 4;
+static_assert(kPsiOff % 4 == 0 && kXOff % 4 == 0 && kStageFloats % 4 == 0, "16-byte aligned stage slots");
+constexpr int kSpinLimit = 1 << 20;
+constexpr int kTmaMaxPml = kXSlot - 8;         // x-strip rows fit their stage slot
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Poll the barrier's phase `parity` at most kSpinLimit times.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (int it = 0; it < kSpinLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void bulk_copy(float* dst, const float* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void lds4(float (&d)[4], const float* p) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+}
+
+__device__ __forceinline__ void stcs4(float* p, const float (&d)[4]) {
+  __stcs(reinterpret_cast<float4*>(p), make_float4(d[0], d[1], d[2], d[3]));
+}
+
+struct Ring {
+  float* stage;          // kStages * kStageFloats
+  uint64_t* full;        // completion of a stage's copies
+  uint64_t* empty;       // all warps done reading a stage
+  uint32_t issued = 0;   // rows issued into the ring (producer thread only)
+  uint32_t used = 0;     // rows consumed (every thread)
+};
+
+// CPML y-strip rows: psi_Hxy row (side, r) for Hx at row j and psi_Ezy row
+// for Ez at row j, or -1 when row j is outside that strip.
+__device__ __forceinline__ int hxy_row(const DevShot& S, int j) {
+  const int P = S.npml;
+  if (j <= P - 2) return j;
+  if (j >= S.ny - P) return (P - 1) + (S.ny - 2 - j);
+  return -1;
+}
+__device__ __forceinline__ int ezy_row(const DevShot& S, int j) {
+  const int P = S.npml;
+  if (j >= 1 && j <= P - 1) return j;
+  if (j >= S.ny - P && j <= S.ny - 2) return P + (S.ny - 1 - j);
+  return -1;
+}
+
+// x-strip sides a band reads: bit 0 = side 0 (columns < P), bit 1 = side 1
+// (columns >= nx - P), including the Hy halo column c0 - 1.  With P below
+// kTmaMaxPml only the first band reaches side 0.
+__device__ __forceinline__ int band_x_sides(const DevShot& S, int c0) {
+  return (c0 == 0 ? 1 : 0) | (c0 + kBand - 1 >= S.nx - S.npml ? 2 : 0);
+}
+
+// Float offset, within S.psi, of x-strip row (side, j) of the array at `o`.
+__device__ __forceinline__ int64_t xstrip_off(const DevShot& S, int par, int64_t o, int side, int j) {
+  return par * S.psi_buf + o + ((int64_t)side * S.ny + j) * S.npml;
+}
+
+// Producer: copy row `j` of the unit (band starting at c0) into the next stage.
+__device__ bool issue_row(Ring& R, const DevShot& S, int par, int c0, int j, bool has_kp, int xs) {
+  const uint32_t g = R.issued++;
+  const int s = g % kStages;
+  if (g >= (uint32_t)kStages && !mbar_wait(&R.empty[s], ((g / kStages) - 1) & 1)) return false;
+  const int64_t row = (int64_t)j * S.pitch + c0 - 4;
+  float* dst = R.stage + s * kStageFloats;
+  const int rh = hxy_row(S, j), re = ezy_row(S, j);
+  uint32_t xbytes[4] = {0, 0, 0, 0};
+  int64_t xa[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int side = q & 1;
+    if (!((xs >> side) & 1)) continue;
+    const int64_t off = xstrip_off(S, par, (q >> 1) ? S.o_ezx : S.o_hyx, side, j);
+    xa[q] = off & ~(int64_t)3;
+    xbytes[q] = (uint32_t)((((off + S.npml + 3) & ~(int64_t)3) - xa[q]) * 4);
+  }
+  mbar_expect_tx(&R.full[s], kSegBytes * (has_kp ? 5 : 4) + (rh >= 0 ? kPsiBytes : 0) + (re >= 0 ? kPsiBytes : 0) +
+                                 xbytes[0] + xbytes[1] + xbytes[2] + xbytes[3]);
+  const float* psr = S.psi + par * S.psi_buf;
+  if (rh >= 0) bulk_copy(dst + kPsiOff, psr + (int64_t)rh * S.pitch + c0, kPsiBytes, &R.full[s]);
+  if (re >= 0) bulk_copy(dst + kPsiOff + kBand, psr + S.o_ezy + (int64_t)re * S.pitch + c0, kPsiBytes, &R.full[s]);
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (xbytes[q]) bulk_copy(dst + kXOff + q * kXSlot, S.psi + xa[q], xbytes[q], &R.full[s]);
+  bulk_copy(dst + 0 * kSeg, field_ptr(S, kEz, par) + row + S.pitch, kSegBytes, &R.full[s]);
+  bulk_copy(dst + 1 * kSeg, field_ptr(S, kHx, par) + row, kSegBytes, &R.full[s]);
+  bulk_copy(dst + 2 * kSeg, field_ptr(S, kHy, par) + row, kSegBytes, &R.full[s]);
+  bulk_copy(dst + 3 * kSeg, field_ptr(S, kJz, par) + row, kSegBytes, &R.full[s]);
+  if (has_kp) bulk_copy(dst + 4 * kSeg, S.kp + row, kSegBytes, &R.full[s]);
+  return true;
+}
+
+// After a timed-out wait: wait (bounded) for every copy still in flight.
+__device__ void drain(Ring& R) {
+  for (uint32_t g = R.used; g < R.issued; ++g) mbar_wait(&R.full[g % kStages], (g / kStages) & 1);
+}
+
+__device__ void process_band(const DevShot& S, Ring& R, int c0, int j0, int j1, int n, int* err) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nx = S.nx, ny = S.ny, P = S.npml;
+  const int64_t pitch = S.pitch;
+  const int par = (n - 1) & 1;
+  const bool has_kp = S.kp != nullptr;
+  const int xs = band_x_sides(S, c0);
+  const float* __restrict__ ezo = field_ptr(S, kEz, par);
+  const float* __restrict__ hxo_p = field_ptr(S, kHx, par);
+  float* __restrict__ ezw = field_ptr(S, kEz, par ^ 1);
+  float* __restrict__ hxw = field_ptr(S, kHx, par ^ 1);
+  float* __restrict__ hyw = field_ptr(S, kHy, par ^ 1);
+  float* __restrict__ jzw = field_ptr(S, kJz, par ^ 1);
+  float* __restrict__ psw = S.psi + (par ^ 1) * S.psi_buf;
+
+  const int i0 = c0 + warp * kCols;            // this warp's first column
+  const int i = i0 + 4 * lane;
+  const bool act = i < nx;
+  const int ic = act ? i : 0;
+  const int sl = 4 + warp * kCols + 4 * lane;  // lane's float4 in a staged segment
+  const int rows = j1 - j0;
+
+  // Fill the ring.
+  if (tid == 0) {
+    for (int r = 0; r < rows && r < kStages; ++r)
+      if (!issue_row(R, S, par, c0, j0 + r, has_kp, xs)) {
+        atomicExch(err, kErrWaitTimeout);
+        drain(R);
+        return;
+      }
+  }
+
+  MediumRow<0> m;
+  m.init(S);
+  float dex[4], dhx[4];
+  ld4(dex, S.den_ex + ic);
+  ld4(dhx, S.den_hx + ic);
+  const float dhx_left = i0 >= 1 ? __ldg(S.den_hx + i0 - 1) : 0.f;  // lane 0's halo column
+
+  // Row j0 state from global memory: Ez(j0) (+ the band-edge halo values the
+  // lane needs) and Hx_new(j0-1), recomputed from the old buffers.
+  float ezc[4], hxp[4];
+  zero4(ezc);
+  zero4(hxp);
+  if (act) ld4(ezc, ezo + (int64_t)j0 * pitch + ic);
+  float ezl = (lane == 0 && i0 >= 1) ? ezo[(int64_t)j0 * pitch + i0 - 1] : 0.f;  // Ez(i0-1, j)
+  float ezr = (lane == 31 && i0 + kCols < nx) ? ezo[(int64_t)j0 * pitch + i0 + kCols] : 0.f;
+  if (j0 >= 1) {
+    float ezp[4], hxo[4];
+    zero4(ezp);
+    zero4(hxo);
+    if (act) {
+      ld4(ezp, ezo + (int64_t)(j0 - 1) * pitch + ic);
+      ld4(hxo, hxo_p + (int64_t)(j0 - 1) * pitch + ic);
+    }
+    hx_row<0>(S, m, par, ic, j0 - 1, ezp, ezc, hxo, hxp, false);
+  }
+
+  // Per-row scalars (denominators, point range), loaded one row ahead.
+  float dhy = __ldg(S.den_hy + j0), dey = __ldg(S.den_ey + j0);
+  int p0 = __ldg(S.row_start + j0), p1 = __ldg(S.row_start + j0 + 1);
+
+  for (int j = j0; j < j1; ++j) {
+    const int jn = j + 1 < j1 ? j + 1 : j;
+    const float dhy_n = __ldg(S.den_hy + jn), dey_n = __ldg(S.den_ey + jn);
+    const int p1_n = __ldg(S.row_start + jn + 1);
+
+    const uint32_t g = R.used;
+    const int s = g % kStages;
+    if (!mbar_wait(&R.full[s], (g / kStages) & 1)) {
+      atomicExch(err, kErrWaitTimeout);
+      if (tid == 0) drain(R);
+      return;
+    }
+    const float* st = R.stage + s * kStageFloats;
+    float ezn[4], hxo[4], hyo[4], jzo[4];
+    lds4(ezn, st + 0 * kSeg + sl);
+    lds4(hxo, st + 1 * kSeg + sl);
+    lds4(hyo, st + 2 * kSeg + sl);
+    lds4(jzo, st + 3 * kSeg + sl);
+    if (has_kp) {
+      lds4(m.kp, st + 4 * kSeg + sl);
+    } else {
+      zero4(m.kp);
+    }
+    // halo values of row j+1 for the next iteration, and Hy_old(i0-1, j)
+    const float ezl_next = st[0 * kSeg + 4 + warp * kCols - 1];
+    const float ezr_next = st[0 * kSeg + 4 + warp * kCols + kCols];
+    const float hyo_left = st[2 * kSeg + 4 + warp * kCols - 1];
+    // staged x-strip rows (psi_Hyx, psi_Ezx; side 0, 1): value r at x..[r]
+    const float* xh0 = st + kXOff + 0 * kXSlot + (int)(xstrip_off(S, 0, S.o_hyx, 0, j) & 3);
+    const float* xh1 = st + kXOff + 1 * kXSlot + (int)(xstrip_off(S, 0, S.o_hyx, 1, j) & 3);
+    const float* xe0 = st + kXOff + 2 * kXSlot + (int)(xstrip_off(S, 0, S.o_ezx, 0, j) & 3);
+    const float* xe1 = st + kXOff + 3 * kXSlot + (int)(xstrip_off(S, 0, S.o_ezx, 1, j) & 3);
+
+    // ---- H update: Hx bulk + y-strip CPML (psi from the stage)
+    const int rh = hxy_row(S, j), re = ezy_row(S, j);
+    float hxn[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      hxn[k] = (i + k <= nx - 2) ? upd_h(S.da, hxo[k], S.db, ezc[k], ezn[k], dhy) : hxo[k];
+    if (rh >= 0) {
+      const int side = rh >= P - 1, r = side ? rh - (P - 1) : rh;
+      const float b = S.cpml[(side ? kBhY2 : kBhY1) * P + r];
+      const float cc = S.cpml[(side ? kChY2 : kChY1) * P + r];
+      float psh[4], pn[4];
+      lds4(psh, st + kPsiOff + warp * kCols + 4 * lane);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        pn[k] = psh[k];
+        if (i + k <= nx - 2) {
+          pn[k] = upd_psi(b, psh[k], cc, ezc[k], ezn[k], S.dy);
+          hxn[k] = __fmaf_rn(S.db, pn[k], hxn[k]);
+        }
+      }
+      if (act) st4(psw + (int64_t)rh * pitch + ic, pn);
+    }
+    float ezr_k = __shfl_down_sync(0xffffffffu, ezc[0], 1);
+    if (lane == 31) ezr_k = ezr;
+    const float ezr4[4] = {ezc[1], ezc[2], ezc[3], ezr_k};
+    float hyn[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      hyn[k] = (i + k <= nx - 2) ? upd_h(m.day(k), hyo[k], m.dby(k), ezr4[k], ezc[k], dhx[k]) : hyo[k];
+    if (act && (i <= P - 2 || i + 3 >= nx - P)) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int c = i + k;
+        int side = -1, r = 0;
+        if (c <= P - 2) { side = 0; r = c; }
+        else if (c >= nx - P && c <= nx - 2) { side = 1; r = nx - 2 - c; }
+        if (side >= 0) {
+          const float b = S.cpml[(side ? kBhX2 : kBhX1) * P + r];
+          const float cc = S.cpml[(side ? kChX2 : kChX1) * P + r];
+          const float pn = upd_psi(b, (side ? xh1 : xh0)[r], cc, ezr4[k], ezc[k], S.dx);
+          hyn[k] = __fmaf_rn(m.dby(k), pn, hyn[k]);
+          psw[S.o_hyx + ((int64_t)side * ny + j) * P + r] = pn;
+        }
+      }
+    }
+    // Hy_new(i-1): lane 0 recomputes the band/warp-edge value from staged data.
+    float hyl = __shfl_up_sync(0xffffffffu, hyn[3], 1);
+    if (lane == 0) {
+      hyl = 0.f;
+      if (i0 >= 1) {
+        const int c = i0 - 1;
+        float h = upd_h(S.da, hyo_left, S.db, ezc[0], ezl, dhx_left);
+        int side = -1, r = 0;
+        if (c <= P - 2) { side = 0; r = c; }
+        else if (c >= nx - P && c <= nx - 2) { side = 1; r = nx - 2 - c; }
+        if (side >= 0) {
+          const float b = S.cpml[(side ? kBhX2 : kBhX1) * P + r];
+          const float cc = S.cpml[(side ? kChX2 : kChX1) * P + r];
+          const float pn = upd_psi(b, (side ? xh1 : xh0)[r], cc, ezc[0], ezl, S.dx);
+          h = __fmaf_rn(S.db, pn, h);
+        }
+        hyl = h;
+      }
+    }
+
+    // ---- Jz, Ez
+    const bool row_in = (j >= 1) && (j <= ny - 2);
+    const float hyl4[4] = {hyl, hyn[0], hyn[1], hyn[2]};
+    float ezw4[4], jzw4[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int c = i + k;
+      const bool in = row_in && c >= 1 && c <= nx - 2;
+      jzw4[k] = in ? upd_j(S.ja, jzo[k], m.kp[k], ezc[k]) : jzo[k];
+      ezw4[k] = in ? upd_e(S.ca, ezc[k], S.cb, __fsub_rn(hyn[k], hyl4[k]), dex[k], __fsub_rn(hxp[k], hxn[k]),
+                           dey, jzw4[k])
+                   : ezc[k];
+    }
+    if (act && row_in && (i <= P - 1 || i + 3 >= nx - P)) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int c = i + k;
+        int side = -1, r = 0;
+        if (c >= 1 && c <= P - 1) { side = 0; r = c; }
+        else if (c >= nx - P && c <= nx - 2) { side = 1; r = nx - 1 - c; }
+        if (side >= 0) {
+          const float b = S.cpml[(side ? kBeX2 : kBeX1) * P + r];
+          const float cc = S.cpml[(side ? kCeX2 : kCeX1) * P + r];
+          const float pn = upd_psi(b, (side ? xe1 : xe0)[r], cc, hyn[k], hyl4[k], S.dx);
+          ezw4[k] = __fmaf_rn(S.cb, pn, ezw4[k]);
+          psw[S.o_ezx + ((int64_t)side * ny + j) * P + r] = pn;
+        }
+      }
+    }
+    if (act && re >= 0) {
+      const int side = re >= P, r = side ? re - P : re;
+      const float b = S.cpml[(side ? kBeY2 : kBeY1) * P + r];
+      const float cc = S.cpml[(side ? kCeY2 : kCeY1) * P + r];
+      float pse[4], pn[4];
+      lds4(pse, st + kPsiOff + kBand + warp * kCols + 4 * lane);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        pn[k] = pse[k];
+        if (i + k >= 1 && i + k <= nx - 2) {
+          pn[k] = upd_psi(b, pse[k], cc, hxp[k], hxn[k], S.dy);
+          ezw4[k] = __fmaf_rn(S.cb, pn[k], ezw4[k]);
+        }
+      }
+      st4(psw + S.o_ezy + (int64_t)re * pitch + ic, pn);
+    }
+    // Every read of this stage is done: release it to the producer.
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&R.empty[s]);
+    R.used++;
+
+    // ---- sources, then detectors, of this row
+    for (int p = p0; p < p1; ++p) {
+      const int4 pt = __ldg(S.pts + p);
+      const int k = pt.x - i;
+      if (!act || k < 0 || k > 3) continue;
+      float e = 0.f;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) if (q == k) e = ezw4[q];
+      if (pt.y == kPointSource) {
+        e = __fsub_rn(e, __ldg(S.src_val + (int64_t)n * S.n_src + pt.z));
+#pragma unroll
+        for (int q = 0; q < 4; ++q) if (q == k) ezw4[q] = e;
+      } else if (pt.y == kPointDetEz) {
+        if (S.record) S.trace[(int64_t)(n - 1) * S.n_det + pt.z] = e;
+        if (S.dft) {
+          const double2 tw = __ldg(S.twiddle + n);
+          double2 acc = S.dft[pt.z];
+          acc.x = fma((double)e, tw.x, acc.x);
+          acc.y = fma(-(double)e, tw.y, acc.y);
+          S.dft[pt.z] = acc;
+        }
+      } else {
+        float hxv = 0.f, hyv = 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) if (q == k) { hxv = hxn[q]; hyv = hyn[q]; }
+        if (S.record) {
+          float* dst = S.ctrace + ((int64_t)(n - 1) * S.n_comp + pt.z) * 3;
+          dst[0] = e; dst[1] = hxv; dst[2] = hyv;
+        }
+      }
+    }
+
+    if (act) {
+      const int64_t o = (int64_t)j * pitch + ic;
+      stcs4(hxw + o, hxn);
+      stcs4(hyw + o, hyn);
+      stcs4(ezw + o, ezw4);
+      stcs4(jzw + o, jzw4);
+    }
+
+    // Producer: refill this stage with row j + kStages.
+    if (tid == 0 && j + kStages < j1) {
+      if (!issue_row(R, S, par, c0, j + kStages, has_kp, xs)) {
+        atomicExch(err, kErrWaitTimeout);
+        drain(R);
+        return;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      hxp[k] = hxn[k];
+      ezc[k] = ezn[k];
+    }
+    ezl = ezl_next;
+    ezr = ezr_next;
+    dhy = dhy_n;
+    dey = dey_n;
+    p0 = p1;
+    p1 = p1_n;
+  }
+}
+
+// The shot descriptor is a __grid_constant__ parameter: its fields are read
+// through the constant cache, and the compiler need not reload them after the
+// kernel's global stores (a descriptor in global memory could alias them).
+__global__ void __launch_bounds__(kTmaThreads, 4)
+step_tma_kernel(const __grid_constant__ DevShot S, const int4* __restrict__ units, int n_units, int n_global,
+                int* err) {
+  extern __shared__ __align__(128) float smem[];
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages];
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kTmaWarps);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  Ring R;
+  R.stage = smem;
+  R.full = full;
+  R.empty = empty;
+  const int n = n_global - S.base_n;
+  if (n < 1 || n > S.n_steps) return;
+  for (int u = blockIdx.x; u < n_units; u += gridDim.x) {
+    const int4 ud = __ldg(units + u);
+    process_band(S, R, ud.y, ud.z, ud.w, n, err);
+    if (*(volatile int*)err) return;
+  }
+}
+
+}  // namespace
+
+int tma_band_cols() { return kBand; }
+
+int tma_max_pml() { return kTmaMaxPml; }
+
+size_t tma_smem_bytes() { return (size_t)kStages * kStageFloats * sizeof(float); }
+
+cudaError_t launch_step_tma(const DevShot& shot, const int4* units, int n_units, int n_global, int max_ctas,
+                            int* err, cudaStream_t stream) {
+  const int ctas = max_ctas < n_units ? max_ctas : n_units;
+  if (ctas <= 0) return cudaSuccess;
+  step_tma_kernel<<<ctas, kTmaThreads, tma_smem_bytes(), stream>>>(shot, units, n_units, n_global, err);
+  return cudaGetLastError();
+}
+
+int tma_resident_ctas(int device) {
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(step_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tma_smem_bytes());
+    configured = true;
+  }
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_tma_kernel, kTmaThreads, tma_smem_bytes());
+  if (per_sm < 1) per_sm = 1;
+  return sms * per_sm;
+}
+
+}  // namespace fdtd2d

@@ -48,7 +48,8 @@ enum {
     FDTD2D_ERR_CONFIG    = -7,  /* Settings.ini missing or malformed           */
     FDTD2D_ERR_STATE     = -8,  /* call not valid in the object's state        */
     FDTD2D_ERR_BUDGET    = -9,  /* request does not fit the HBM budget         */
-    FDTD2D_ERR_NODEVICE  = -10  /* no CUDA device                              */
+    FDTD2D_ERR_NODEVICE  = -10, /* no CUDA device                              */
+    FDTD2D_ERR_TIMEOUT   = -11  /* a bounded device-side wait gave up          */
 };
 
 /* ---- enumerations -------------------------------------------------------- */

@@ -14,8 +14,21 @@ from helpers import (FIELD_TOL, FIELDS, PHASE_TOL, PSI_FIELDS, compare_fields, d
 
 pytestmark = pytest.mark.gpu
 
+# Uniform-medium shots run on the shared-memory staged kernel by default;
+# FDTD2D_KERNEL=stream selects the register-streaming kernel.  Both are checked.
+KERNELS = ["tma", "stream"]
 
-def test_plain_512_shot_checkpoints(gpu):
+
+@pytest.fixture(params=KERNELS)
+def kernel(request, monkeypatch):
+    if request.param == "stream":
+        monkeypatch.setenv("FDTD2D_KERNEL", "stream")
+    else:
+        monkeypatch.delenv("FDTD2D_KERNEL", raising=False)
+    return request.param
+
+
+def test_plain_512_shot_checkpoints(gpu, kernel):
     """512^2 plain shot (linear slab plasma, point source, 4000 steps).
 
     Physical fields: error / peak norm over the run <= 1e-5 at every
@@ -57,8 +70,9 @@ def test_plain_512_shot_checkpoints(gpu):
         assert shot.check_finite()
 
 
-@pytest.mark.parametrize("nx,ny,P", [(203, 157, 7), (131, 96, 4), (64, 260, 12), (40, 40, 2)])
-def test_random_state_uniform(gpu, nx, ny, P):
+@pytest.mark.parametrize("nx,ny,P", [(203, 157, 7), (131, 96, 4), (64, 260, 12), (40, 40, 2),
+                                    (1100, 90, 9)])
+def test_random_state_uniform(gpu, kernel, nx, ny, P):
     """Random fields and psi on odd grids (nx not a multiple of 4, unit edges,
     tiny P), per-cell plasma, collisions; every code path of one step."""
     rng = np.random.default_rng(nx * 1000 + ny)
@@ -81,7 +95,7 @@ def test_random_state_uniform(gpu, nx, ny, P):
         compare_fields(shot, ref, FIELDS + PSI_FIELDS, tol=FIELD_TOL, ref32=ref32)
 
 
-def test_phased_array_traces_and_dft(gpu):
+def test_phased_array_traces_and_dft(gpu, kernel):
     """Multi-element steered array with co-located detectors on a tanh x GRF
     plasma: per-step traces and the FP64 running DFT."""
     n_elem = 8
