@@ -245,6 +245,7 @@ def run_ours(args, world, rank, local, dist) -> None:
     barrier(dist)
     shot.synchronize()
     launches0 = shot.launches()
+    kernel = shot.kernel_name()
     ms = shot.run_timed(W * S + 1, W * S + K * S)  # one event pair around the K blocks
     shot.synchronize()
     barrier(dist)
@@ -303,7 +304,7 @@ def run_ours(args, world, rank, local, dist) -> None:
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(args),
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic,
-                             "peak_source": peak_src, "kernel": "step_stream_kernel<0>",
+                             "peak_source": peak_src, "kernel": kernel,
                              "algorithmic_bytes_per_launch": BYTES_PER_CELL * cells},
                 "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk,
                 "finite": ok}

@@ -140,6 +140,7 @@ def _lib():
         "fdtd2d_destroy": (C.c_int, [vp]),
         "fdtd2d_device_bytes": (C.c_int64, [C.POINTER(Setup)]),
         "fdtd2d_launch_count": (C.c_int64, [vp]),
+        "fdtd2d_kernel_name": (C.c_char_p, [vp]),
         "fdtd2d_last_cuda_error": (C.c_int, [vp]),
         "fdtd2d_spec_defaults": (None, [C.POINTER(Spec)]),
         "fdtd2d_problem_from_spec": (C.c_int, [C.POINTER(Spec), C.POINTER(vp)]),
@@ -317,6 +318,10 @@ class Shot:
 
     def launches(self) -> int:
         return int(_lib().fdtd2d_launch_count(self._h))
+
+    def kernel_name(self) -> str:
+        """The step kernel this shot launches, with its launch shape."""
+        return _lib().fdtd2d_kernel_name(self._h).decode()
 
     def read_field(self, which) -> np.ndarray:
         w = FIELD_NAMES[which] if isinstance(which, str) else which

@@ -34,6 +34,8 @@ struct fdtd2d_ctx {
   int* d_flag = nullptr;
   int* d_err = nullptr;     // device error word (bounded waits)
   bool tma = false;         // shared-memory staged kernel (uniform medium)
+  int tma_shape = 0;        // its launch shape (index into the compiled shapes)
+  char kernel_name[48] = {0};
   // wave-front tracker and line probe
   int n_rc = 0, rc_j_cut = 0;
   float rc_level = 0;
@@ -295,10 +297,15 @@ int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
     const float* rows[kCpmlRows] = {s->be_x_1, s->ce_x_1, s->be_x_2, s->ce_x_2, s->bh_x_1, s->ch_x_1,
                                     s->bh_x_2, s->ch_x_2, s->be_y_1, s->ce_y_1, s->be_y_2, s->ce_y_2,
                                     s->bh_y_1, s->ch_y_1, s->bh_y_2, s->ch_y_2};
+    // b rows as given; c rows hold c/d (d = dx for the x strips, dy for the
+    // y strips), so the kernels multiply instead of dividing.
     for (int r = 0; r < kCpmlRows; ++r) {
       const bool hrow = (r % 8) >= 4;
       const int len = hrow ? P - 1 : P;
-      for (int k = 0; k < len; ++k) tab[(size_t)r * P + k] = rows[r][k];
+      const bool crow = (r % 2) == 1;
+      const double d = r < 8 ? (double)s->dx : (double)s->dy;
+      for (int k = 0; k < len; ++k)
+        tab[(size_t)r * P + k] = crow ? (float)((double)rows[r][k] / d) : rows[r][k];
     }
     std::vector<float> dex(pitch, 0.f), dhx(pitch, 0.f), dey(ny, 0.f), dhy(ny, 0.f);
     for (int i = 0; i < nx - 1; ++i) { dex[i] = s->den_ex[i]; dhx[i] = s->den_hx[i]; }
@@ -424,11 +431,20 @@ int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
   }
   std::vector<int4> units;
   if (c->tma) {
-    c->grid_warps = tma_resident_ctas(device);  // CTAs for this path
-    units = make_units(0, nx, ny, c->grid_warps, tma_band_cols());
+    // FDTD2D_TMA="W,ST" picks a compiled launch shape (W warps, ST stages).
+    if (const char* t = std::getenv("FDTD2D_TMA")) {
+      int w = 0, st = 0;
+      if (std::sscanf(t, "%d,%d", &w, &st) == 2 && tma_shape_find(w, st) >= 0) c->tma_shape = tma_shape_find(w, st);
+    }
+    c->grid_warps = tma_resident_ctas(c->tma_shape, P, device);  // CTAs for this path
+    units = make_units(0, nx, ny, c->grid_warps, tma_band_cols(c->tma_shape));
+    int w = 0, st = 0;
+    tma_shape_dims(c->tma_shape, &w, &st);
+    std::snprintf(c->kernel_name, sizeof c->kernel_name, "step_tma_kernel<%d,%d>", w, st);
   } else {
     c->grid_warps = resident_warps(c->medium, device);
     units = make_units(0, nx, ny, c->grid_warps);
+    std::snprintf(c->kernel_name, sizeof c->kernel_name, "step_stream_kernel<%d>", c->medium == FDTD2D_MEDIUM_UNIFORM ? 0 : 1);
   }
   c->n_units = (int)units.size();
   CK(dalloc(c, &c->d_units, units.size()));
@@ -447,7 +463,7 @@ int fdtd2d_run(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
   if (n_first != c->step + 1 || n_last < n_first - 1 || n_last > c->n_steps) return FDTD2D_ERR_RANGE;
   cudaSetDevice(c->device);
   for (int32_t n = n_first; n <= n_last; ++n) {
-    cudaError_t e = c->tma ? launch_step_tma(c->h, c->d_units, c->n_units, n, c->grid_warps, c->d_err, c->stream)
+    cudaError_t e = c->tma ? launch_step_tma(c->tma_shape, c->h, c->d_units, c->n_units, n, c->grid_warps, c->d_err, c->stream)
                            : launch_step(c->h, c->d_units, c->n_units, n, c->medium, c->grid_warps, c->stream);
     if (e != cudaSuccess) return fail_cuda(c, e);
     ++c->launches;
@@ -699,6 +715,11 @@ int fdtd2d_destroy(fdtd2d_ctx* c) {
 }
 
 int64_t fdtd2d_launch_count(const fdtd2d_ctx* c) { return c ? c->launches : -1; }
+
+const char* fdtd2d_kernel_name(const fdtd2d_ctx* c) {
+  if (!c) return "";
+  return c->kernel_name;
+}
 
 int fdtd2d_last_cuda_error(const fdtd2d_ctx* c) { return c ? c->last_cuda : -1; }
 

@@ -115,13 +115,16 @@ int resident_warps(int medium, int device);
 enum DeviceError : int { kErrNone = 0, kErrWaitTimeout = 1 };
 
 // Shared-memory staged step (step_tma.cu), uniform medium: one CTA per unit
-// of kBand columns.
-int tma_band_cols();
+// of a band of columns.  Compiled launch shapes (warps per CTA, ring stages)
+// are indexed 0..tma_shape_count()-1; shape 0 is the default.
+int tma_shape_count();
+int tma_shape_find(int warps, int stages);   // -1 if not compiled
+void tma_shape_dims(int shape, int* warps, int* stages);
+int tma_band_cols(int shape);
 int tma_max_pml();   // largest CPML depth the staged kernel takes
-size_t tma_smem_bytes();
-int tma_resident_ctas(int device);
-cudaError_t launch_step_tma(const DevShot& shot, const int4* units, int n_units, int n_global, int max_ctas,
-                            int* err, cudaStream_t stream);
+int tma_resident_ctas(int shape, int npml, int device);
+cudaError_t launch_step_tma(int shape, const DevShot& shot, const int4* units, int n_units, int n_global,
+                            int max_ctas, int* err, cudaStream_t stream);
 
 // Tabulate s_e(n) = scale*env[n]*cos(2*pi_c*(beta/2 t^2 + f0 t + phase_e)),
 // t = n*dt, for n = 0..n_steps, and the DFT twiddles, in FP64.

@@ -15,8 +15,13 @@ __device__ __forceinline__ float upd_h(float da, float h, float db, float ea, fl
 }
 
 // psi = b*psi + c*(a - b')/d                  FDTD_2D_Full/kernel.cu:226-227, 478-479
-__device__ __forceinline__ float upd_psi(float b, float psi, float c, float a, float a2, float d) {
-  return __fmaf_rn(b, psi, __fdiv_rn(__fmul_rn(c, __fsub_rn(a, a2)), d));
+// with cd = c/d folded on the host (the device CPML table holds c/d): an
+// IEEE divide per CPML cell takes its slow path whenever the numerator is
+// zero or subnormal (fields not yet arrived in the layer), which made the
+// CPML bands several times slower than the bulk.  Folding moves each psi by
+// at most a couple of FP32 ulps against the reference's c*(a-b')/d.
+__device__ __forceinline__ float upd_psi(float b, float psi, float cd, float a, float a2) {
+  return __fmaf_rn(b, psi, __fmul_rn(cd, __fsub_rn(a, a2)));
 }
 
 // Ez = CA*Ez + CB*(dHy*den_ex + dHx*den_ey - Jz)   FDTD_2D_Full/kernel.cu:444-446
@@ -144,7 +149,7 @@ __device__ float hy_cell(const DevShot& S, const MatH* mat_h, int par, int c, in
     const float* tb = S.cpml + (side ? kBhX2 : kBhX1) * P;
     const float* tc = S.cpml + (side ? kChX2 : kChX1) * P;
     const float psi = S.psi[par * S.psi_buf + S.o_hyx + ((int64_t)side * S.ny + j) * P + r];
-    const float pn = upd_psi(tb[r], psi, tc[r], ez_c1, ez_c, S.dx);
+    const float pn = upd_psi(tb[r], psi, tc[r], ez_c1, ez_c);
     h = __fmaf_rn(db, pn, h);
   }
   return h;
@@ -178,7 +183,7 @@ __device__ __forceinline__ void hx_row(const DevShot& S, const MediumRow<MEDIUM>
     for (int k = 0; k < 4; ++k) {
       pn[k] = psi[k];
       if (i + k <= nx - 2 && covered<MEDIUM>(S, kCovHxPml, (long long)r * (nx - 1) + i + k)) {
-        pn[k] = upd_psi(b, psi[k], c, ezj[k], ezj1[k], S.dy);
+        pn[k] = upd_psi(b, psi[k], c, ezj[k], ezj1[k]);
         out[k] = __fmaf_rn(m.dbx(k), pn[k], out[k]);
       }
     }

@@ -124,7 +124,7 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
           const float b = S.cpml[(side ? kBhX2 : kBhX1) * P + r];
           const float cc = S.cpml[(side ? kChX2 : kChX1) * P + r];
           const int64_t po = S.o_hyx + ((int64_t)side * ny + j) * P + r;
-          pn[k] = upd_psi(b, psr[po], cc, ezr[k], ezc[k], S.dx);
+          pn[k] = upd_psi(b, psr[po], cc, ezr[k], ezc[k]);
           hyn[k] = __fmaf_rn(m.dby(k), pn[k], hyn[k]);
           psw[po] = pn[k];
         }
@@ -170,7 +170,7 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
           const float b = S.cpml[(side ? kBeX2 : kBeX1) * P + r];
           const float cc = S.cpml[(side ? kCeX2 : kCeX1) * P + r];
           const int64_t po = S.o_ezx + ((int64_t)side * ny + j) * P + r;
-          const float pn = upd_psi(b, psr[po], cc, hyn[k], hyl4[k], S.dx);
+          const float pn = upd_psi(b, psr[po], cc, hyn[k], hyl4[k]);
           ezw4[k] = __fmaf_rn(m.cB(k), pn, ezw4[k]);
           psw[po] = pn;
         }
@@ -189,7 +189,7 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
         const int c = i + k;
         pn[k] = psi[k];
         if (c >= 1 && c <= nx - 2 && covered<MEDIUM>(S, kCovEzPmlJ, (long long)(r - 1) * (nx - 2) + (c - 1))) {
-          pn[k] = upd_psi(b, psi[k], cc, hxp[k], hxn[k], S.dy);
+          pn[k] = upd_psi(b, psi[k], cc, hxp[k], hxn[k]);
           ezw4[k] = __fmaf_rn(m.cB(k), pn[k], ezw4[k]);
         }
       }

@@ -1,15 +1,16 @@
 // Fused TMz step, shared-memory staged with bulk asynchronous copies (TMA).
 //
 // Same arithmetic and the same ping-pong buffers as step_stream_kernel, but
-// the rows reach the warps through shared memory: a CTA of kTmaWarps warps
-// owns a 512-column band of one shot and walks a range of rows; one thread
-// keeps a ring of kStages row stages filled with cp.async.bulk copies
-// (Ez(j+1), Hx(j), Hy(j), Jz(j), plasma drive (j), each the 520-float row
-// segment [c0-4, c0+516), halo included, in one copy), completion tracked by
-// an mbarrier per stage.  Bytes in flight per SM are then set by the ring
-// depth (3 stages x 10.4 KB per CTA, 4 CTAs per SM) instead of by registers
-// per warp, and the warp-edge neighbours (Ez(c0-1), Ez(c0+512), Hy(c0-1))
-// come from shared memory instead of dependent global loads.
+// the rows reach the warps through shared memory: a CTA of W warps owns a
+// band of 128*W columns of one shot and walks a range of rows; one thread
+// keeps a ring of ST row stages filled with cp.async.bulk copies (Ez(j+1),
+// Hx(j), Hy(j), Jz(j), plasma drive (j), each the row segment [c0-4,
+// c0+128W+4), halo included, in one copy; plus the CPML psi rows the band
+// reads in row j), completion tracked by an mbarrier per stage.  Bytes in
+// flight per SM are then set by the ring depth instead of by registers per
+// warp, and the warp-edge neighbours (Ez(i0-1), Ez(i0+128), Hy(i0-1)) come
+// from shared memory instead of dependent global loads.  The launch shape
+// (W, ST) is a template parameter; TmaShape lists the compiled ones.
 //
 // Every wait is bounded: after kSpinLimit failed polls the kernel records
 // kErrWaitTimeout in the shot's error word, waits (bounded) for the copies it
@@ -21,25 +22,31 @@ namespace fdtd2d {
 
 namespace {
 
-constexpr int kTmaWarps = 4;
-constexpr int kTmaThreads = kTmaWarps * 32;
-constexpr int kBand = kTmaWarps * kCols;       // 512 columns per CTA
-constexpr int kSeg = kBand + 8;                // staged floats per array row
-constexpr int kArrays = 5;                     // Ez(j+1), Hx, Hy, Jz, drive
-constexpr int kStages = 3;
-// A stage holds one row j of the band: the 5 field segments; the psi_Hxy and
-// psi_Ezy rows of the band (CPML y-strip rows only); and the row's x-strip
-// psi rows (psi_Hyx side 0/1, psi_Ezx side 0/1; bands touching a strip only),
-// each copied from its 16-byte-aligned start, kXSlot floats reserved.
-constexpr int kPsiOff = kArrays * kSeg;
-constexpr int kXOff = kPsiOff + 2 * kBand;
-constexpr int kXSlot = 128;
-constexpr int kStageFloats = kXOff + 4 * kXSlot;
-constexpr uint32_t kSegBytes = kSeg * 4;
-constexpr uint32_t kPsiBytes = kBand * 4;
-static_assert(kPsiOff % 4 == 0 && kXOff % 4 == 0 && kStageFloats % 4 == 0, "16-byte aligned stage slots");
 constexpr int kSpinLimit = 1 << 20;
+constexpr int kXSlot = 128;                    // floats reserved per staged x-strip row
 constexpr int kTmaMaxPml = kXSlot - 8;         // x-strip rows fit their stage slot
+
+// Launch shape: W warps (a band of 128*W columns) and an ST-stage ring.
+template <int W, int ST>
+struct Cfg {
+  static constexpr int kWarps = W;
+  static constexpr int kThreads = W * 32;
+  static constexpr int kStages = ST;
+  static constexpr int kBand = W * kCols;
+  static constexpr int kSeg = kBand + 8;       // staged floats per array row
+  // A stage holds one row j of the band: Ez(j+1), Hx, Hy, Jz, drive segments;
+  // the psi_Hxy and psi_Ezy rows of the band (CPML y-strip rows only); and the
+  // row's x-strip psi rows (psi_Hyx side 0/1, psi_Ezx side 0/1; bands touching
+  // a strip only), each copied from its 16-byte-aligned start.
+  static constexpr int kPsiOff = 5 * kSeg;
+  static constexpr int kXOff = kPsiOff + 2 * kBand;
+  static constexpr int kStageFloats = kXOff + 4 * kXSlot;
+  static constexpr uint32_t kSegBytes = kSeg * 4;
+  static constexpr uint32_t kPsiBytes = kBand * 4;
+  static constexpr size_t kSmem = (size_t)ST * kStageFloats * sizeof(float);
+  static constexpr int kMinBlocks = W <= 4 ? 4 : 2;   // caps registers at 128 per thread
+  static_assert(kPsiOff % 4 == 0 && kXOff % 4 == 0 && kStageFloats % 4 == 0, "16-byte aligned stage slots");
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -116,8 +123,9 @@ __device__ __forceinline__ int ezy_row(const DevShot& S, int j) {
 // x-strip sides a band reads: bit 0 = side 0 (columns < P), bit 1 = side 1
 // (columns >= nx - P), including the Hy halo column c0 - 1.  With P below
 // kTmaMaxPml only the first band reaches side 0.
+template <int BAND>
 __device__ __forceinline__ int band_x_sides(const DevShot& S, int c0) {
-  return (c0 == 0 ? 1 : 0) | (c0 + kBand - 1 >= S.nx - S.npml ? 2 : 0);
+  return (c0 == 0 ? 1 : 0) | (c0 + BAND - 1 >= S.nx - S.npml ? 2 : 0);
 }
 
 // Float offset, within S.psi, of x-strip row (side, j) of the array at `o`.
@@ -126,12 +134,13 @@ __device__ __forceinline__ int64_t xstrip_off(const DevShot& S, int par, int64_t
 }
 
 // Producer: copy row `j` of the unit (band starting at c0) into the next stage.
+template <class C>
 __device__ bool issue_row(Ring& R, const DevShot& S, int par, int c0, int j, bool has_kp, int xs) {
   const uint32_t g = R.issued++;
-  const int s = g % kStages;
-  if (g >= (uint32_t)kStages && !mbar_wait(&R.empty[s], ((g / kStages) - 1) & 1)) return false;
+  const int s = g % C::kStages;
+  if (g >= (uint32_t)C::kStages && !mbar_wait(&R.empty[s], ((g / C::kStages) - 1) & 1)) return false;
   const int64_t row = (int64_t)j * S.pitch + c0 - 4;
-  float* dst = R.stage + s * kStageFloats;
+  float* dst = R.stage + s * C::kStageFloats;
   const int rh = hxy_row(S, j), re = ezy_row(S, j);
   uint32_t xbytes[4] = {0, 0, 0, 0};
   int64_t xa[4] = {0, 0, 0, 0};
@@ -143,34 +152,37 @@ __device__ bool issue_row(Ring& R, const DevShot& S, int par, int c0, int j, boo
     xa[q] = off & ~(int64_t)3;
     xbytes[q] = (uint32_t)((((off + S.npml + 3) & ~(int64_t)3) - xa[q]) * 4);
   }
-  mbar_expect_tx(&R.full[s], kSegBytes * (has_kp ? 5 : 4) + (rh >= 0 ? kPsiBytes : 0) + (re >= 0 ? kPsiBytes : 0) +
+  mbar_expect_tx(&R.full[s], C::kSegBytes * (has_kp ? 5 : 4) + (rh >= 0 ? C::kPsiBytes : 0) + (re >= 0 ? C::kPsiBytes : 0) +
                                  xbytes[0] + xbytes[1] + xbytes[2] + xbytes[3]);
   const float* psr = S.psi + par * S.psi_buf;
-  if (rh >= 0) bulk_copy(dst + kPsiOff, psr + (int64_t)rh * S.pitch + c0, kPsiBytes, &R.full[s]);
-  if (re >= 0) bulk_copy(dst + kPsiOff + kBand, psr + S.o_ezy + (int64_t)re * S.pitch + c0, kPsiBytes, &R.full[s]);
+  if (rh >= 0) bulk_copy(dst + C::kPsiOff, psr + (int64_t)rh * S.pitch + c0, C::kPsiBytes, &R.full[s]);
+  if (re >= 0) bulk_copy(dst + C::kPsiOff + C::kBand, psr + S.o_ezy + (int64_t)re * S.pitch + c0, C::kPsiBytes, &R.full[s]);
 #pragma unroll
   for (int q = 0; q < 4; ++q)
-    if (xbytes[q]) bulk_copy(dst + kXOff + q * kXSlot, S.psi + xa[q], xbytes[q], &R.full[s]);
-  bulk_copy(dst + 0 * kSeg, field_ptr(S, kEz, par) + row + S.pitch, kSegBytes, &R.full[s]);
-  bulk_copy(dst + 1 * kSeg, field_ptr(S, kHx, par) + row, kSegBytes, &R.full[s]);
-  bulk_copy(dst + 2 * kSeg, field_ptr(S, kHy, par) + row, kSegBytes, &R.full[s]);
-  bulk_copy(dst + 3 * kSeg, field_ptr(S, kJz, par) + row, kSegBytes, &R.full[s]);
-  if (has_kp) bulk_copy(dst + 4 * kSeg, S.kp + row, kSegBytes, &R.full[s]);
+    if (xbytes[q]) bulk_copy(dst + C::kXOff + q * kXSlot, S.psi + xa[q], xbytes[q], &R.full[s]);
+  bulk_copy(dst + 0 * C::kSeg, field_ptr(S, kEz, par) + row + S.pitch, C::kSegBytes, &R.full[s]);
+  bulk_copy(dst + 1 * C::kSeg, field_ptr(S, kHx, par) + row, C::kSegBytes, &R.full[s]);
+  bulk_copy(dst + 2 * C::kSeg, field_ptr(S, kHy, par) + row, C::kSegBytes, &R.full[s]);
+  bulk_copy(dst + 3 * C::kSeg, field_ptr(S, kJz, par) + row, C::kSegBytes, &R.full[s]);
+  if (has_kp) bulk_copy(dst + 4 * C::kSeg, S.kp + row, C::kSegBytes, &R.full[s]);
   return true;
 }
 
 // After a timed-out wait: wait (bounded) for every copy still in flight.
+template <class C>
 __device__ void drain(Ring& R) {
-  for (uint32_t g = R.used; g < R.issued; ++g) mbar_wait(&R.full[g % kStages], (g / kStages) & 1);
+  for (uint32_t g = R.used; g < R.issued; ++g) mbar_wait(&R.full[g % C::kStages], (g / C::kStages) & 1);
 }
 
-__device__ void process_band(const DevShot& S, Ring& R, int c0, int j0, int j1, int n, int* err) {
+template <class C>
+__device__ void process_band(const DevShot& S, Ring& R, const float* __restrict__ cp, int c0, int j0, int j1, int n,
+                             int* err) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nx = S.nx, ny = S.ny, P = S.npml;
   const int64_t pitch = S.pitch;
   const int par = (n - 1) & 1;
   const bool has_kp = S.kp != nullptr;
-  const int xs = band_x_sides(S, c0);
+  const int xs = band_x_sides<C::kBand>(S, c0);
   const float* __restrict__ ezo = field_ptr(S, kEz, par);
   const float* __restrict__ hxo_p = field_ptr(S, kHx, par);
   float* __restrict__ ezw = field_ptr(S, kEz, par ^ 1);
@@ -185,13 +197,18 @@ __device__ void process_band(const DevShot& S, Ring& R, int c0, int j0, int j1, 
   const int ic = act ? i : 0;
   const int sl = 4 + warp * kCols + 4 * lane;  // lane's float4 in a staged segment
   const int rows = j1 - j0;
+  // The producer thread: lane 0 of a warp with no x-strip columns where the
+  // band has one (the first band's strip is in warp 0, the last band's in
+  // warp W-1), so the ring refill does not wait on the slower CPML lanes.
+  const int prod_warp = (c0 == 0 && C::kWarps > 1) ? C::kWarps - 1 : 0;
+  const bool producer = tid == prod_warp * 32;
 
   // Fill the ring.
-  if (tid == 0) {
-    for (int r = 0; r < rows && r < kStages; ++r)
-      if (!issue_row(R, S, par, c0, j0 + r, has_kp, xs)) {
+  if (producer) {
+    for (int r = 0; r < rows && r < C::kStages; ++r)
+      if (!issue_row<C>(R, S, par, c0, j0 + r, has_kp, xs)) {
         atomicExch(err, kErrWaitTimeout);
-        drain(R);
+        drain<C>(R);
         return;
       }
   }
@@ -232,32 +249,32 @@ __device__ void process_band(const DevShot& S, Ring& R, int c0, int j0, int j1, 
     const int p1_n = __ldg(S.row_start + jn + 1);
 
     const uint32_t g = R.used;
-    const int s = g % kStages;
-    if (!mbar_wait(&R.full[s], (g / kStages) & 1)) {
+    const int s = g % C::kStages;
+    if (!mbar_wait(&R.full[s], (g / C::kStages) & 1)) {
       atomicExch(err, kErrWaitTimeout);
-      if (tid == 0) drain(R);
+      if (producer) drain<C>(R);
       return;
     }
-    const float* st = R.stage + s * kStageFloats;
+    const float* st = R.stage + s * C::kStageFloats;
     float ezn[4], hxo[4], hyo[4], jzo[4];
-    lds4(ezn, st + 0 * kSeg + sl);
-    lds4(hxo, st + 1 * kSeg + sl);
-    lds4(hyo, st + 2 * kSeg + sl);
-    lds4(jzo, st + 3 * kSeg + sl);
+    lds4(ezn, st + 0 * C::kSeg + sl);
+    lds4(hxo, st + 1 * C::kSeg + sl);
+    lds4(hyo, st + 2 * C::kSeg + sl);
+    lds4(jzo, st + 3 * C::kSeg + sl);
     if (has_kp) {
-      lds4(m.kp, st + 4 * kSeg + sl);
+      lds4(m.kp, st + 4 * C::kSeg + sl);
     } else {
       zero4(m.kp);
     }
     // halo values of row j+1 for the next iteration, and Hy_old(i0-1, j)
-    const float ezl_next = st[0 * kSeg + 4 + warp * kCols - 1];
-    const float ezr_next = st[0 * kSeg + 4 + warp * kCols + kCols];
-    const float hyo_left = st[2 * kSeg + 4 + warp * kCols - 1];
+    const float ezl_next = st[0 * C::kSeg + 4 + warp * kCols - 1];
+    const float ezr_next = st[0 * C::kSeg + 4 + warp * kCols + kCols];
+    const float hyo_left = st[2 * C::kSeg + 4 + warp * kCols - 1];
     // staged x-strip rows (psi_Hyx, psi_Ezx; side 0, 1): value r at x..[r]
-    const float* xh0 = st + kXOff + 0 * kXSlot + (int)(xstrip_off(S, 0, S.o_hyx, 0, j) & 3);
-    const float* xh1 = st + kXOff + 1 * kXSlot + (int)(xstrip_off(S, 0, S.o_hyx, 1, j) & 3);
-    const float* xe0 = st + kXOff + 2 * kXSlot + (int)(xstrip_off(S, 0, S.o_ezx, 0, j) & 3);
-    const float* xe1 = st + kXOff + 3 * kXSlot + (int)(xstrip_off(S, 0, S.o_ezx, 1, j) & 3);
+    const float* xh0 = st + C::kXOff + 0 * kXSlot + (int)(xstrip_off(S, 0, S.o_hyx, 0, j) & 3);
+    const float* xh1 = st + C::kXOff + 1 * kXSlot + (int)(xstrip_off(S, 0, S.o_hyx, 1, j) & 3);
+    const float* xe0 = st + C::kXOff + 2 * kXSlot + (int)(xstrip_off(S, 0, S.o_ezx, 0, j) & 3);
+    const float* xe1 = st + C::kXOff + 3 * kXSlot + (int)(xstrip_off(S, 0, S.o_ezx, 1, j) & 3);
 
     // ---- H update: Hx bulk + y-strip CPML (psi from the stage)
     const int rh = hxy_row(S, j), re = ezy_row(S, j);
@@ -267,15 +284,15 @@ __device__ void process_band(const DevShot& S, Ring& R, int c0, int j0, int j1, 
       hxn[k] = (i + k <= nx - 2) ? upd_h(S.da, hxo[k], S.db, ezc[k], ezn[k], dhy) : hxo[k];
     if (rh >= 0) {
       const int side = rh >= P - 1, r = side ? rh - (P - 1) : rh;
-      const float b = S.cpml[(side ? kBhY2 : kBhY1) * P + r];
-      const float cc = S.cpml[(side ? kChY2 : kChY1) * P + r];
+      const float b = cp[(side ? kBhY2 : kBhY1) * P + r];
+      const float cc = cp[(side ? kChY2 : kChY1) * P + r];
       float psh[4], pn[4];
-      lds4(psh, st + kPsiOff + warp * kCols + 4 * lane);
+      lds4(psh, st + C::kPsiOff + warp * kCols + 4 * lane);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         pn[k] = psh[k];
         if (i + k <= nx - 2) {
-          pn[k] = upd_psi(b, psh[k], cc, ezc[k], ezn[k], S.dy);
+          pn[k] = upd_psi(b, psh[k], cc, ezc[k], ezn[k]);
           hxn[k] = __fmaf_rn(S.db, pn[k], hxn[k]);
         }
       }
@@ -296,9 +313,9 @@ __device__ void process_band(const DevShot& S, Ring& R, int c0, int j0, int j1, 
         if (c <= P - 2) { side = 0; r = c; }
         else if (c >= nx - P && c <= nx - 2) { side = 1; r = nx - 2 - c; }
         if (side >= 0) {
-          const float b = S.cpml[(side ? kBhX2 : kBhX1) * P + r];
-          const float cc = S.cpml[(side ? kChX2 : kChX1) * P + r];
-          const float pn = upd_psi(b, (side ? xh1 : xh0)[r], cc, ezr4[k], ezc[k], S.dx);
+          const float b = cp[(side ? kBhX2 : kBhX1) * P + r];
+          const float cc = cp[(side ? kChX2 : kChX1) * P + r];
+          const float pn = upd_psi(b, (side ? xh1 : xh0)[r], cc, ezr4[k], ezc[k]);
           hyn[k] = __fmaf_rn(m.dby(k), pn, hyn[k]);
           psw[S.o_hyx + ((int64_t)side * ny + j) * P + r] = pn;
         }
@@ -315,9 +332,9 @@ __device__ void process_band(const DevShot& S, Ring& R, int c0, int j0, int j1, 
         if (c <= P - 2) { side = 0; r = c; }
         else if (c >= nx - P && c <= nx - 2) { side = 1; r = nx - 2 - c; }
         if (side >= 0) {
-          const float b = S.cpml[(side ? kBhX2 : kBhX1) * P + r];
-          const float cc = S.cpml[(side ? kChX2 : kChX1) * P + r];
-          const float pn = upd_psi(b, (side ? xh1 : xh0)[r], cc, ezc[0], ezl, S.dx);
+          const float b = cp[(side ? kBhX2 : kBhX1) * P + r];
+          const float cc = cp[(side ? kChX2 : kChX1) * P + r];
+          const float pn = upd_psi(b, (side ? xh1 : xh0)[r], cc, ezc[0], ezl);
           h = __fmaf_rn(S.db, pn, h);
         }
         hyl = h;
@@ -345,9 +362,9 @@ __device__ void process_band(const DevShot& S, Ring& R, int c0, int j0, int j1, 
         if (c >= 1 && c <= P - 1) { side = 0; r = c; }
         else if (c >= nx - P && c <= nx - 2) { side = 1; r = nx - 1 - c; }
         if (side >= 0) {
-          const float b = S.cpml[(side ? kBeX2 : kBeX1) * P + r];
-          const float cc = S.cpml[(side ? kCeX2 : kCeX1) * P + r];
-          const float pn = upd_psi(b, (side ? xe1 : xe0)[r], cc, hyn[k], hyl4[k], S.dx);
+          const float b = cp[(side ? kBeX2 : kBeX1) * P + r];
+          const float cc = cp[(side ? kCeX2 : kCeX1) * P + r];
+          const float pn = upd_psi(b, (side ? xe1 : xe0)[r], cc, hyn[k], hyl4[k]);
           ezw4[k] = __fmaf_rn(S.cb, pn, ezw4[k]);
           psw[S.o_ezx + ((int64_t)side * ny + j) * P + r] = pn;
         }
@@ -355,15 +372,15 @@ __device__ void process_band(const DevShot& S, Ring& R, int c0, int j0, int j1, 
     }
     if (act && re >= 0) {
       const int side = re >= P, r = side ? re - P : re;
-      const float b = S.cpml[(side ? kBeY2 : kBeY1) * P + r];
-      const float cc = S.cpml[(side ? kCeY2 : kCeY1) * P + r];
+      const float b = cp[(side ? kBeY2 : kBeY1) * P + r];
+      const float cc = cp[(side ? kCeY2 : kCeY1) * P + r];
       float pse[4], pn[4];
-      lds4(pse, st + kPsiOff + kBand + warp * kCols + 4 * lane);
+      lds4(pse, st + C::kPsiOff + C::kBand + warp * kCols + 4 * lane);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         pn[k] = pse[k];
         if (i + k >= 1 && i + k <= nx - 2) {
-          pn[k] = upd_psi(b, pse[k], cc, hxp[k], hxn[k], S.dy);
+          pn[k] = upd_psi(b, pse[k], cc, hxp[k], hxn[k]);
           ezw4[k] = __fmaf_rn(S.cb, pn[k], ezw4[k]);
         }
       }
@@ -414,11 +431,11 @@ __device__ void process_band(const DevShot& S, Ring& R, int c0, int j0, int j1, 
       stcs4(jzw + o, jzw4);
     }
 
-    // Producer: refill this stage with row j + kStages.
-    if (tid == 0 && j + kStages < j1) {
-      if (!issue_row(R, S, par, c0, j + kStages, has_kp, xs)) {
+    // Producer: refill this stage with row j + C::kStages.
+    if (producer && j + C::kStages < j1) {
+      if (!issue_row<C>(R, S, par, c0, j + C::kStages, has_kp, xs)) {
         atomicExch(err, kErrWaitTimeout);
-        drain(R);
+        drain<C>(R);
         return;
       }
     }
@@ -439,15 +456,21 @@ __device__ void process_band(const DevShot& S, Ring& R, int c0, int j0, int j1, 
 // The shot descriptor is a __grid_constant__ parameter: its fields are read
 // through the constant cache, and the compiler need not reload them after the
 // kernel's global stores (a descriptor in global memory could alias them).
-__global__ void __launch_bounds__(kTmaThreads, 4)
+template <class C>
+__global__ void __launch_bounds__(C::kThreads, C::kMinBlocks)
 step_tma_kernel(const __grid_constant__ DevShot S, const int4* __restrict__ units, int n_units, int n_global,
                 int* err) {
   extern __shared__ __align__(128) float smem[];
-  __shared__ __align__(8) uint64_t full[kStages], empty[kStages];
+  __shared__ __align__(8) uint64_t full[C::kStages], empty[C::kStages];
+  // The CPML coefficient table (kCpmlRows x P floats) sits after the ring:
+  // its reads are per lane (x strips) or per row (y strips) on the critical
+  // path, so they come from shared memory instead of the L1/L2.
+  float* cp = smem + C::kStages * C::kStageFloats;
+  for (int t = threadIdx.x; t < kCpmlRows * S.npml; t += C::kThreads) cp[t] = S.cpml[t];
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
+    for (int s = 0; s < C::kStages; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], kTmaWarps);
+      mbar_init(&empty[s], C::kWarps);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -460,36 +483,69 @@ step_tma_kernel(const __grid_constant__ DevShot S, const int4* __restrict__ unit
   if (n < 1 || n > S.n_steps) return;
   for (int u = blockIdx.x; u < n_units; u += gridDim.x) {
     const int4 ud = __ldg(units + u);
-    process_band(S, R, ud.y, ud.z, ud.w, n, err);
+    process_band<C>(S, R, cp, ud.y, ud.z, ud.w, n, err);
     if (*(volatile int*)err) return;
   }
 }
 
+using KernelFn = void (*)(DevShot, const int4*, int, int, int*);
+
+struct ShapeEntry {
+  int warps, stages;
+  KernelFn fn;
+  size_t smem;
+};
+
+template <int W, int ST>
+constexpr ShapeEntry entry() {
+  return {W, ST, step_tma_kernel<Cfg<W, ST>>, Cfg<W, ST>::kSmem};
+}
+
+// Compiled launch shapes; the first is the default.
+const ShapeEntry kShapes[] = {entry<4, 3>(), entry<4, 2>(), entry<4, 4>(), entry<4, 6>(),
+                              entry<8, 2>(), entry<8, 3>(), entry<8, 4>(), entry<2, 4>(), entry<2, 6>()};
+constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
+
 }  // namespace
 
-int tma_band_cols() { return kBand; }
+int tma_shape_count() { return kNumShapes; }
+
+int tma_shape_find(int warps, int stages) {
+  for (int k = 0; k < kNumShapes; ++k)
+    if (kShapes[k].warps == warps && kShapes[k].stages == stages) return k;
+  return -1;
+}
+
+void tma_shape_dims(int shape, int* warps, int* stages) {
+  *warps = kShapes[shape].warps;
+  *stages = kShapes[shape].stages;
+}
+
+int tma_band_cols(int shape) { return kShapes[shape].warps * kCols; }
 
 int tma_max_pml() { return kTmaMaxPml; }
 
-size_t tma_smem_bytes() { return (size_t)kStages * kStageFloats * sizeof(float); }
+// Dynamic shared memory of one CTA: the ring, then the CPML table.
+static size_t smem_bytes(const ShapeEntry& e, int npml) {
+  return e.smem + (((size_t)kCpmlRows * npml * sizeof(float) + 15) & ~(size_t)15);
+}
 
-cudaError_t launch_step_tma(const DevShot& shot, const int4* units, int n_units, int n_global, int max_ctas,
-                            int* err, cudaStream_t stream) {
+cudaError_t launch_step_tma(int shape, const DevShot& shot, const int4* units, int n_units, int n_global,
+                            int max_ctas, int* err, cudaStream_t stream) {
+  const ShapeEntry& e = kShapes[shape];
   const int ctas = max_ctas < n_units ? max_ctas : n_units;
   if (ctas <= 0) return cudaSuccess;
-  step_tma_kernel<<<ctas, kTmaThreads, tma_smem_bytes(), stream>>>(shot, units, n_units, n_global, err);
+  e.fn<<<ctas, e.warps * 32, smem_bytes(e, shot.npml), stream>>>(shot, units, n_units, n_global, err);
   return cudaGetLastError();
 }
 
-int tma_resident_ctas(int device) {
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(step_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tma_smem_bytes());
-    configured = true;
-  }
+int tma_resident_ctas(int shape, int npml, int device) {
+  const ShapeEntry& e = kShapes[shape];
+  const size_t smem = smem_bytes(e, npml);
+  cudaFuncSetAttribute(e.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(e, kTmaMaxPml));
   int sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_tma_kernel, kTmaThreads, tma_smem_bytes());
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, e.fn, e.warps * 32, smem);
   if (per_sm < 1) per_sm = 1;
   return sms * per_sm;
 }

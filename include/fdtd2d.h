@@ -215,6 +215,10 @@ int64_t fdtd2d_device_bytes(const fdtd2d_setup *setup);
 /* Kernel launches issued by this context so far (for launch accounting). */
 int64_t fdtd2d_launch_count(const fdtd2d_ctx *ctx);
 
+/* Name of the step kernel this context launches, with its launch shape
+   (e.g. "step_tma_kernel<4,3>"; no counterpart in the reference). */
+const char *fdtd2d_kernel_name(const fdtd2d_ctx *ctx);
+
 /* Number of CUDA devices visible to this process (0 when none). */
 int fdtd2d_device_count(void);
 
