@@ -429,12 +429,67 @@ int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
     const char* k = std::getenv("FDTD2D_KERNEL");
     c->tma = (c->medium == FDTD2D_MEDIUM_UNIFORM) && P <= tma_max_pml() && !(k && std::strcmp(k, "stream") == 0);
   }
+  CK(dalloc(c, &c->d_err, 1));
   std::vector<int4> units;
   if (c->tma) {
-    // FDTD2D_TMA="W,ST" picks a compiled launch shape (W warps, ST stages).
+    // FDTD2D_TMA="W,ST" picks a compiled launch shape (W warps, ST stages);
+    // otherwise the shapes are timed on this shot and the fastest is kept,
+    // unless FDTD2D_TMA_AUTOTUNE=0 (then shape 0).
+    int forced = -1;
     if (const char* t = std::getenv("FDTD2D_TMA")) {
       int w = 0, st = 0;
-      if (std::sscanf(t, "%d,%d", &w, &st) == 2 && tma_shape_find(w, st) >= 0) c->tma_shape = tma_shape_find(w, st);
+      if (std::sscanf(t, "%d,%d", &w, &st) == 2) forced = tma_shape_find(w, st);
+    }
+    const char* at = std::getenv("FDTD2D_TMA_AUTOTUNE");
+    if (forced >= 0) {
+      c->tma_shape = forced;
+    } else if (!(at && std::strcmp(at, "0") == 0) && c->n_steps >= 1) {
+      // Each trial re-runs step 1 with traces and the DFT switched off: a
+      // step reads one buffer set and overwrites the other with values that
+      // depend on the first alone, so the trials leave nothing behind once
+      // step 1 runs for real.
+      DevShot t = h;
+      t.record = 0;
+      t.dft = nullptr;
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      CK(cudaEventCreate(&e0));
+      CK(cudaEventCreate(&e1));
+      float best = 0.f;
+      int best_k = 0;
+      for (int k = 0; k < tma_shape_count(); ++k) {
+        const int ctas = tma_resident_ctas(k, P, device);
+        const std::vector<int4> u = make_units(0, nx, ny, ctas, tma_band_cols(k));
+        int4* du = nullptr;
+        cudaError_t e = cudaMalloc(&du, u.size() * sizeof(int4));
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(du, u.data(), u.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
+        for (int r = 0; r < 4 && e == cudaSuccess; ++r) {
+          if (r == 1) e = cudaEventRecord(e0, c->stream);
+          if (e == cudaSuccess) e = launch_step_tma(k, t, du, (int)u.size(), t.base_n + 1, ctas, c->d_err, c->stream);
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (du) cudaFree(du);
+        if (e != cudaSuccess) {
+          cudaEventDestroy(e0);
+          cudaEventDestroy(e1);
+          rc = fail_cuda(c, e);
+          fdtd2d_destroy(c);
+          return rc;
+        }
+        if (k == 0 || ms < best) { best = ms; best_k = k; }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      int derr = 0;
+      CK(cudaMemcpy(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+      if (derr != kErrNone) {
+        fdtd2d_destroy(c);
+        return FDTD2D_ERR_TIMEOUT;
+      }
+      c->tma_shape = best_k;
     }
     c->grid_warps = tma_resident_ctas(c->tma_shape, P, device);  // CTAs for this path
     units = make_units(0, nx, ny, c->grid_warps, tma_band_cols(c->tma_shape));
@@ -451,7 +506,6 @@ int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
   CK(cudaMemcpyAsync(c->d_units, units.data(), units.size() * sizeof(int4), cudaMemcpyHostToDevice,
                      c->stream));
   CK(dalloc(c, &c->d_flag, 1));
-  CK(dalloc(c, &c->d_err, 1));
   CK(cudaStreamSynchronize(c->stream));
 #undef CK
   *out = c;

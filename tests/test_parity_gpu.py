@@ -95,6 +95,48 @@ def test_random_state_uniform(gpu, kernel, nx, ny, P):
         compare_fields(shot, ref, FIELDS + PSI_FIELDS, tol=FIELD_TOL, ref32=ref32)
 
 
+def _random_state_case(gpu, nx, ny, P, steps=60):
+    rng = np.random.default_rng(nx * 1000 + ny)
+    prob = F.Problem.from_spec(nx=nx, ny=ny, npml=P, n_steps=steps, profile=1, x_lo=nx // 3,
+                               x_hi=nx - 3, ne_peak=2e19, nu=3e9, src_i=P + 2, src_j=ny // 2,
+                               det_i=P + 4, det_j=ny // 2 + 1, n_det=1)
+    ref = O.Oracle(prob.setup_ptr)
+    ref32 = O.Oracle(prob.setup_ptr, fp32=True)
+    with F.Shot(prob, gpu) as shot:
+        name = shot.kernel_name()
+        st = random_state(shot, nx, ny, P, rng)
+        load_state([shot, ref, ref32], st)
+        shot.run(1, steps)
+        ref.run(1, steps)
+        ref32.run(1, steps)
+        compare_fields(shot, ref, FIELDS + PSI_FIELDS, tol=FIELD_TOL, ref32=ref32)
+    return name
+
+
+# Launch shapes (warps per CTA, ring stages) compiled into the staged kernel.
+TMA_SHAPES = [(4, 3), (4, 2), (4, 4), (4, 6), (8, 2), (8, 3), (8, 4), (2, 4), (2, 6)]
+
+
+@pytest.mark.parametrize("shape", TMA_SHAPES)
+def test_every_launch_shape(gpu, monkeypatch, shape):
+    """Each compiled launch shape of the staged kernel, forced through
+    FDTD2D_TMA, on grids whose width is not a multiple of any band and whose
+    CPML strips fall inside the first and last bands."""
+    monkeypatch.delenv("FDTD2D_KERNEL", raising=False)
+    monkeypatch.setenv("FDTD2D_TMA", f"{shape[0]},{shape[1]}")
+    for nx, ny, P in ((1100, 90, 9), (203, 157, 7)):
+        assert _random_state_case(gpu, nx, ny, P) == f"step_tma_kernel<{shape[0]},{shape[1]}>"
+
+
+def test_autotuned_shape_and_deep_cpml(gpu, monkeypatch):
+    """Without FDTD2D_TMA the create call times the shapes and keeps one; a
+    CPML deeper than the staged kernel's x-strip slots streams instead."""
+    monkeypatch.delenv("FDTD2D_KERNEL", raising=False)
+    monkeypatch.delenv("FDTD2D_TMA", raising=False)
+    assert _random_state_case(gpu, 700, 130, 16).startswith("step_tma_kernel<")
+    assert _random_state_case(gpu, 300, 260, 121, steps=20) == "step_stream_kernel<0>"
+
+
 def test_phased_array_traces_and_dft(gpu, kernel):
     """Multi-element steered array with co-located detectors on a tanh x GRF
     plasma: per-step traces and the FP64 running DFT."""
