@@ -156,7 +156,7 @@ def measured_peaks() -> dict:
 def profile_traffic() -> float | None:
     """DRAM bytes per launch of the step kernel on this workload, from the
     committed ncu summary (scaled to the full launch as stated there)."""
-    f = ROOT / "profiles" / "step_stream_8192_production.md"
+    f = ROOT / "profiles" / "step_tma_8192_production.md"
     if not f.exists():
         return None
     m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read_text())
