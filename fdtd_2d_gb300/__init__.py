@@ -145,6 +145,7 @@ def _lib():
         "fdtd2d_spec_defaults": (None, [C.POINTER(Spec)]),
         "fdtd2d_problem_from_spec": (C.c_int, [C.POINTER(Spec), C.POINTER(vp)]),
         "fdtd2d_problem_from_ini": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
+        "fdtd2d_problem_from_ini_vacuum": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
         "fdtd2d_problem_setup": (C.POINTER(Setup), [vp]),
         "fdtd2d_problem_free": (None, [vp]),
         "fdtd2d_run_settings": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int]),
@@ -228,9 +229,12 @@ class Problem:
         return cls(h.value)
 
     @classmethod
-    def from_ini(cls, path: str | os.PathLike) -> "Problem":
+    def from_ini(cls, path: str | os.PathLike, vacuum: bool = False) -> "Problem":
+        """Setup of a Settings.ini; vacuum=True gives its SourceToDetect vacuum
+        shot (no medium, fluctuation or wall)."""
         h = C.c_void_p()
-        _check(_lib().fdtd2d_problem_from_ini(str(path).encode(), C.byref(h)), "problem_from_ini")
+        fn = _lib().fdtd2d_problem_from_ini_vacuum if vacuum else _lib().fdtd2d_problem_from_ini
+        _check(fn(str(path).encode(), C.byref(h)), "problem_from_ini")
         return cls(h.value)
 
     def close(self) -> None:

@@ -17,10 +17,18 @@
 //   deb.txt           kernel.cu:2681-2751 (ID3 map dump)
 //   iniLOG.txt, log.txt
 //
+// SourceToDetect = 1 (initlimits, FDTD_cuda.cu:389-417) adds a first shot
+// without medium and wall (DevSourceToDetectInfluenceCalc, kernel.cu:1620-1926)
+// whose traces go to Detect_S2D.txt ("%lf\t%12lf\n ", time in us),
+// detAll_S2D.txt, detEz/Hx/Hy_S2D.txt, and DifDetEx.txt of the main shot holds
+// the component-trace differences (kernel.cu:2497-2538).  Here the vacuum shot
+// runs beside the main one on its own stream instead of before it.
+//
 // Sample rows follow the reference: row i of every trace file is the sample
 // taken at step i (row 0 is all zeros, the step-nMax sample is never printed).
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <ctime>
@@ -92,6 +100,98 @@ void write_ini_log(const std::string& dir, const IniParams& r) {
                r.p_load_weights);
 }
 
+// Traces of one shot in the reference's host layout: row i = step i, row 0
+// zeros, rows 0..nmax-1.
+struct Traces {
+  int nd = 0, nc = 0, nmax = 0;
+  std::vector<float> det, cez, chx, chy;
+  int read(fdtd2d_ctx* ctx, const fdtd2d_setup& s) {
+    nd = s.n_det; nc = s.n_comp; nmax = s.n_steps;
+    std::vector<float> d((size_t)nmax * nd), e((size_t)nmax * nc), x((size_t)nmax * nc), y((size_t)nmax * nc);
+    const int rc = fdtd2d_read_traces(ctx, 1, nmax, d.data(), e.data(), x.data(), y.data());
+    if (rc) return rc;
+    det.assign((size_t)nmax * nd, 0.f);
+    cez.assign((size_t)nmax * nc, 0.f);
+    chx.assign((size_t)nmax * nc, 0.f);
+    chy.assign((size_t)nmax * nc, 0.f);
+    // sample of step n (traces row n-1) goes to row n; step nmax is not kept
+    std::copy(d.begin(), d.end() - nd, det.begin() + nd);
+    std::copy(e.begin(), e.end() - nc, cez.begin() + nc);
+    std::copy(x.begin(), x.end() - nc, chx.begin() + nc);
+    std::copy(y.begin(), y.end() - nc, chy.begin() + nc);
+    return FDTD2D_OK;
+  }
+};
+
+// detEz/detHx/detHy rows (kernel.cu:2456-2493): per step, one line per element
+// and a blank line.
+void write_components(const Traces& t, FILE* ez, FILE* hx, FILE* hy, FILE* pp) {
+  for (int i = 0; i < t.nmax; ++i) {
+    for (int k = 0; k < t.nc; ++k) {
+      std::fprintf(ez, "%12lf\t", (double)t.cez[(size_t)i * t.nc + k] * 1000);
+      std::fprintf(hx, "%12lf\t", (double)t.chx[(size_t)i * t.nc + k] * 1000);
+      std::fprintf(hy, "%12lf\t", (double)t.chy[(size_t)i * t.nc + k] * 1000);
+      std::fputc('\n', ez);
+      std::fputc('\n', hx);
+      std::fputc('\n', hy);
+      if (pp) std::fputc('\n', pp);
+    }
+    std::fputc('\n', ez);
+    std::fputc('\n', hx);
+    std::fputc('\n', hy);
+    if (pp) std::fputc('\n', pp);
+  }
+}
+
+// The SourceToDetect vacuum shot's files (kernel.cu:1640-1652, 1818-1918).
+int write_s2d_files(const Traces& t, double dt, const std::string& dir) {
+  File pDet(join(dir, "Detect_S2D.txt"), "w"), pAll(join(dir, "detAll_S2D.txt"), "w");
+  File pEz(join(dir, "detEz_S2D.txt"), "w"), pHx(join(dir, "detHx_S2D.txt"), "w"),
+      pHy(join(dir, "detHy_S2D.txt"), "w");
+  File e1(join(dir, "CompDetect_S2D.txt"), "w"), e2(join(dir, "detEx_S2D.txt"), "w"),
+      e3(join(dir, "detEy_S2D.txt"), "w"), e4(join(dir, "detHz_S2D.txt"), "w"), e5(join(dir, "detP_S2D.txt"), "w");
+  if (!pDet || !pAll || !pEz || !pHx || !pHy) return FDTD2D_ERR_IO;
+  for (int i = 0; i < t.nmax; ++i) {
+    double sum = 0;
+    for (int k = 0; k < t.nd; ++k) sum += t.det[(size_t)i * t.nd + k];
+    std::fprintf(pDet.f, "%lf\t%12lf\n ", (dt * i) * 1000000, sum * 1000);
+  }
+  for (int i = 0; i < t.nmax; ++i) {
+    double s3 = 0, s4 = 0, s5 = 0;
+    for (int k = 0; k < t.nc; ++k) {
+      s3 += t.cez[(size_t)i * t.nc + k];
+      s4 += t.chx[(size_t)i * t.nc + k];
+      s5 += t.chy[(size_t)i * t.nc + k];
+    }
+    std::fprintf(pAll.f, "%lf\t%12lf\t%12lf\t%12lf\t%12lf\t%12lf\t%12lf\n", (dt * i) * 1000000, 0.0, 0.0,
+                 s3 * 1000, s4 * 1000, s5 * 1000, 0.0);
+  }
+  write_components(t, pEz.f, pHx.f, pHy.f, nullptr);
+  return FDTD2D_OK;
+}
+
+// DifDetEx.txt (kernel.cu:2497-2538): per step the sums over elements of the
+// component differences main - vacuum (each difference an FP32 subtraction,
+// summed in FP64), and |E x H| of the summed differences with Ex = Ey = Hz = 0.
+void write_difference(const Traces& m, const Traces& v, double dt, FILE* f) {
+  for (int i = 0; i < m.nmax; ++i) {
+    double s3 = 0, s4 = 0, s5 = 0;
+    for (int k = 0; k < m.nc; ++k) {
+      const size_t o = (size_t)i * m.nc + k;
+      s3 += (double)(float)(m.cez[o] - v.cez[o]);
+      s4 += (double)(float)(m.chx[o] - v.chx[o]);
+      s5 += (double)(float)(m.chy[o] - v.chy[o]);
+    }
+    const double s1 = 0, s2 = 0, s6 = 0;
+    const float eh_i = (float)(s2 * s6 - s3 * s5);
+    const float eh_j = (float)(-(s1 * s6 - s3 * s4));
+    const float eh_k = (float)(s1 * s5 - s2 * s4);
+    const double mag = std::sqrt((double)eh_i * eh_i + (double)eh_j * eh_j + (double)eh_k * eh_k);
+    std::fprintf(f, "%lf\t%12lf\t%12lf\t%12lf\t%12lf\t%12lf\t%12lf\t%12lf\n ", (dt * i) * 1000000, s1 * 1000,
+                 s2 * 1000, s3 * 1000, s4 * 1000, s5 * 1000, s6 * 1000, mag * 1000);
+  }
+}
+
 }  // namespace
 
 extern "C" int fdtd2d_run_settings(const char* ini_path, const char* out_dir, int device) {
@@ -111,12 +211,6 @@ extern "C" int fdtd2d_run_settings(const char* ini_path, const char* out_dir, in
   const IniParams& ip = p.ini;
   const fdtd2d_setup& s = p.s;
   const int nx = s.nx, ny = s.ny, nmax = s.n_steps;
-  if (ip.s2d == 1) {
-    // SourceToDetect runs the shot twice (vacuum, then with objects) and
-    // writes the differences; provided by the batched driver, not here.
-    fdtd2d_problem_free(handle);
-    return FDTD2D_ERR_CONFIG;
-  }
 
   // SourceP.txt, RcDet_data.txt (written during setup by the reference)
   {
@@ -137,11 +231,44 @@ extern "C" int fdtd2d_run_settings(const char* ini_path, const char* out_dir, in
     fdtd2d_problem_free(handle);
     return rc;
   }
+  // SourceToDetect: the vacuum shot, stepped alongside the main one.
+  fdtd2d_problem* vac_handle = nullptr;
+  fdtd2d_ctx* vac = nullptr;
+  if (ip.s2d == 1) {
+    rc = problem_from_ini_ex(ini_path, false, &vac_handle);
+    if (rc == FDTD2D_OK) rc = fdtd2d_create(fdtd2d_problem_setup(vac_handle), device, &vac);
+    if (rc) {
+      if (vac_handle) fdtd2d_problem_free(vac_handle);
+      fdtd2d_destroy(ctx);
+      fdtd2d_problem_free(handle);
+      return rc;
+    }
+  }
+  int32_t vac_done = 0;
+  // Step both shots to n in chunks, so the vacuum shot's launches stay queued
+  // beside the main shot's on their own stream.
+  auto advance = [&](int32_t from, int32_t to) -> int {
+    for (int32_t a = from; a <= to; a += 256) {
+      const int32_t b = std::min(to, a + 255);
+      if (vac) {
+        const int r = fdtd2d_run(vac, vac_done + 1, b);
+        if (r) return r;
+        vac_done = b;
+      }
+      const int r = fdtd2d_run(ctx, a, b);
+      if (r) return r;
+    }
+    return FDTD2D_OK;
+  };
 
   File pEz(join(dir, "Ez.txt"), "w");
   File pEx(join(dir, "Ex.txt"), "wb"), pEy(join(dir, "Ey.txt"), "wb");
   File pHx(join(dir, "Hx.txt"), "w"), pHy(join(dir, "Hy.txt"), "w"), pHz(join(dir, "Hz.txt"), "w");
   if (!pEz) {
+    if (vac) {
+      fdtd2d_destroy(vac);
+      fdtd2d_problem_free(vac_handle);
+    }
     fdtd2d_destroy(ctx);
     fdtd2d_problem_free(handle);
     return FDTD2D_ERR_IO;
@@ -164,7 +291,7 @@ extern "C" int fdtd2d_run_settings(const char* ini_path, const char* out_dir, in
       }
     }
     if (!save && n < nmax) continue;
-    rc = fdtd2d_run(ctx, done + 1, n);
+    rc = advance(done + 1, n);
     done = n;
     if (rc || !save) continue;
     rc = fdtd2d_read_field(ctx, FDTD2D_FIELD_EZ, ez.data());
@@ -189,53 +316,44 @@ extern "C" int fdtd2d_run_settings(const char* ini_path, const char* out_dir, in
     if (f) std::fprintf(f.f, "%d %d", count_m, save_counter);
   }
 
-  // Detector files.  traces are [step-1][element]; output row i = step i.
-  const int nd = s.n_det, nc = s.n_comp;
-  std::vector<float> det((size_t)nmax * nd), cez((size_t)nmax * nc), chx((size_t)nmax * nc),
-      chy((size_t)nmax * nc);
-  if (rc == FDTD2D_OK)
-    rc = fdtd2d_read_traces(ctx, 1, nmax, det.data(), cez.data(), chx.data(), chy.data());
+  // Detector files (rows: step i).
+  Traces tr, vtr;
+  if (rc == FDTD2D_OK) rc = tr.read(ctx, s);
+  if (rc == FDTD2D_OK && vac) {
+    rc = vtr.read(vac, *fdtd2d_problem_setup(vac_handle));
+    if (rc == FDTD2D_OK) rc = write_s2d_files(vtr, s.dt, dir);
+  }
   if (rc == FDTD2D_OK) {
+    const int nd = tr.nd, nc = tr.nc;
     File pDet(join(dir, "Detect.txt"), "w");
     File pAll(join(dir, "detAll.txt"), "w");
     File pdEz(join(dir, "detEz.txt"), "w"), pdHx(join(dir, "detHx.txt"), "w"),
         pdHy(join(dir, "detHy.txt"), "w"), pdP(join(dir, "detP.txt"), "w");
     File e1(join(dir, "detEx.txt"), "w"), e2(join(dir, "detEy.txt"), "w"), e3(join(dir, "detHz.txt"), "w");
-    File e4(join(dir, "DifDetEx.txt"), "w"), e5(join(dir, "CompDetect.txt"), "w");
+    File pDif(join(dir, "DifDetEx.txt"), "w"), e5(join(dir, "CompDetect.txt"), "w");
     File e6(join(dir, "LineDetect.txt"), "w"), e7(join(dir, "LineDetect2.txt"), "w");
     File e8(join(dir, "test.txt"), "w"), e9(join(dir, "SDetect.txt"), "w");
-    if (!pDet || !pAll || !pdEz || !pdHx || !pdHy) rc = FDTD2D_ERR_IO;
+    if (!pDet || !pAll || !pdEz || !pdHx || !pdHy || !pDif) rc = FDTD2D_ERR_IO;
     for (int i = 0; i < nmax && rc == FDTD2D_OK; ++i) {
       double sum = 0;
-      if (i > 0)
-        for (int k = 0; k < nd; ++k) sum += det[(size_t)(i - 1) * nd + k];
+      for (int k = 0; k < nd; ++k) sum += tr.det[(size_t)i * nd + k];
       std::fprintf(pDet.f, "%lf\t%12lf\t%12lf\n ", (s.dt * i) * 1e12, sum * 1000, 0.0);
       double s3 = 0, s4 = 0, s5 = 0;
-      if (i > 0)
-        for (int k = 0; k < nc; ++k) {
-          s3 += cez[(size_t)(i - 1) * nc + k];
-          s4 += chx[(size_t)(i - 1) * nc + k];
-          s5 += chy[(size_t)(i - 1) * nc + k];
-        }
+      for (int k = 0; k < nc; ++k) {
+        s3 += tr.cez[(size_t)i * nc + k];
+        s4 += tr.chx[(size_t)i * nc + k];
+        s5 += tr.chy[(size_t)i * nc + k];
+      }
       std::fprintf(pAll.f, "%lf\t%12lf\t%12lf\t%12lf\t%12lf\t%12lf\t%12lf\n ", (s.dt * i) * 1000000,
                    0.0, 0.0, s3 * 1000, s4 * 1000, s5 * 1000, 0.0);
-      for (int k = 0; k < nc; ++k) {
-        const float vez = i > 0 ? cez[(size_t)(i - 1) * nc + k] : 0.f;
-        const float vhx = i > 0 ? chx[(size_t)(i - 1) * nc + k] : 0.f;
-        const float vhy = i > 0 ? chy[(size_t)(i - 1) * nc + k] : 0.f;
-        std::fprintf(pdEz.f, "%12lf\t", (double)vez * 1000);
-        std::fprintf(pdHx.f, "%12lf\t", (double)vhx * 1000);
-        std::fprintf(pdHy.f, "%12lf\t", (double)vhy * 1000);
-        std::fputc('\n', pdEz.f);
-        std::fputc('\n', pdHx.f);
-        std::fputc('\n', pdHy.f);
-        if (pdP) std::fputc('\n', pdP.f);
-      }
-      std::fputc('\n', pdEz.f);
-      std::fputc('\n', pdHx.f);
-      std::fputc('\n', pdHy.f);
-      if (pdP) std::fputc('\n', pdP.f);
     }
+    if (rc == FDTD2D_OK) write_components(tr, pdEz.f, pdHx.f, pdHy.f, pdP ? pdP.f : nullptr);
+    if (rc == FDTD2D_OK && vac) write_difference(tr, vtr, s.dt, pDif.f);
+  }
+  if (vac) {
+    fdtd2d_destroy(vac);
+    fdtd2d_problem_free(vac_handle);
+    vac = nullptr;
   }
 
   // Wave-front tracker outputs (RC_Line.txt, TAU_Line.txt).

@@ -473,7 +473,7 @@ std::vector<int> array_positions(int cen, int size, int d, int* count) {
 
 }  // namespace
 
-int build_from_ini(const IniParams& ip, Problem& p) {
+int build_from_ini(const IniParams& ip, Problem& p, bool objects) {
   p.from_ini = true;
   const int nx = ip.imax, ny = ip.jmax, P = kPmlSize;
   if (nx < 2 * P + 2 || ny < 2 * P + 2 || ip.n_max < 1) return FDTD2D_ERR_CONFIG;
@@ -515,10 +515,15 @@ int build_from_ini(const IniParams& ip, Problem& p) {
   p.id2.assign((size_t)nx * ny, 0);
   p.id3.assign((size_t)nx * ny, 0);
   Maps M{nx, ny, p.id1, p.id2, p.id3};
-  if (ip.build_medium == 1) sphere_medium(ip, M);
-  if (ip.build_medium == 2) torus_medium(ip, M);
-  if (ip.fluc_build != 0) fluc_medium(ip, p.mat_ne, M);
-  if (ip.draw_wall == 1) plate_medium(ip, M);
+  if (objects) {
+    if (ip.build_medium == 1) sphere_medium(ip, M);
+    if (ip.build_medium == 2) torus_medium(ip, M);
+    if (ip.fluc_build != 0) fluc_medium(ip, p.mat_ne, M);
+  }
+  // The steel wall: Build_Stell_wall takes DrawWall only outside the
+  // SourceToDetect mode (initlimits, FDTD_2D_Full/FDTD_cuda.cu:384-437), so
+  // neither run of that mode has it.
+  if (ip.draw_wall == 1 && ip.s2d != 1) plate_medium(ip, M);
   for (size_t t = 0; t < p.id1.size(); ++t) {
     if (p.id1[t] >= kNumMaterials || p.id2[t] >= kNumMaterials || p.id3[t] >= kNumMaterials ||
         p.id1[t] < 0 || p.id2[t] < 0 || p.id3[t] < 0) {
@@ -605,10 +610,13 @@ int build_from_ini(const IniParams& ip, Problem& p) {
   // the bulk grid has floor(floor(Imax*Jmax/1024)/2) x 3 blocks, the I-strip
   // grid floor(PML_SIZE*Jmax/1024) blocks, the J-strip grid
   // floor(Imax*PML_SIZE/1024) blocks.
+  // The SourceToDetect vacuum shot launches with 1024 x 1 blocks and one
+  // block more than the floor (kernel.cu:1671-1675), which covers every cell.
   {
-    const int64_t bulk = (int64_t)(((int64_t)nx * ny / 1024) / 2) * 3 * 1024;
-    const int64_t pml_i = (int64_t)((int64_t)P * ny / 1024) * 1024;
-    const int64_t pml_j = (int64_t)((int64_t)nx * P / 1024) * 1024;
+    const int64_t bulk = objects ? (int64_t)(((int64_t)nx * ny / 1024) / 2) * 3 * 1024
+                                 : ((int64_t)nx * ny / 1024 + 1) * 1024;
+    const int64_t pml_i = ((int64_t)P * ny / 1024 + (objects ? 0 : 1)) * 1024;
+    const int64_t pml_j = ((int64_t)nx * P / 1024 + (objects ? 0 : 1)) * 1024;
     const int64_t cov[8] = {bulk, pml_j, bulk, pml_i, bulk, bulk, pml_i, pml_j};
     for (int k = 0; k < 8; ++k) p.s.cover[k] = cov[k] > 0 ? cov[k] : -1;  // -1: no thread at all
   }

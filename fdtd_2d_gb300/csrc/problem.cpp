@@ -320,6 +320,22 @@ int fdtd2d_problem_from_spec(const fdtd2d_spec* sp, fdtd2d_problem** out) {
 }
 
 int fdtd2d_problem_from_ini(const char* path, fdtd2d_problem** out) {
+  return fdtd2d::problem_from_ini_ex(path, true, out);
+}
+
+int fdtd2d_problem_from_ini_vacuum(const char* path, fdtd2d_problem** out) {
+  return fdtd2d::problem_from_ini_ex(path, false, out);
+}
+
+const fdtd2d_setup* fdtd2d_problem_setup(const fdtd2d_problem* p) { return p ? &p->p.s : nullptr; }
+
+void fdtd2d_problem_free(fdtd2d_problem* p) { delete p; }
+
+}  // extern "C"
+
+namespace fdtd2d {
+
+int problem_from_ini_ex(const char* path, bool objects, fdtd2d_problem** out) {
   if (!path || !out) return FDTD2D_ERR_INVALID;
   *out = nullptr;
   fdtd2d_problem* pr = new (std::nothrow) fdtd2d_problem();
@@ -331,7 +347,7 @@ int fdtd2d_problem_from_ini(const char* path, fdtd2d_problem** out) {
     return rc;
   }
   ini_to_metric(pr->p.ini);
-  rc = build_from_ini(pr->p.ini, pr->p);
+  rc = build_from_ini(pr->p.ini, pr->p, objects);
   if (rc) {
     delete pr;
     return rc;
@@ -341,12 +357,5 @@ int fdtd2d_problem_from_ini(const char* path, fdtd2d_problem** out) {
   return FDTD2D_OK;
 }
 
-const fdtd2d_setup* fdtd2d_problem_setup(const fdtd2d_problem* p) { return p ? &p->p.s : nullptr; }
-
-void fdtd2d_problem_free(fdtd2d_problem* p) { delete p; }
-
-}  // extern "C"
-
-namespace fdtd2d {
 Problem* problem_internal(fdtd2d_problem* p) { return p ? &p->p : nullptr; }
 }  // namespace fdtd2d

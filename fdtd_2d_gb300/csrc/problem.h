@@ -102,6 +102,11 @@ void build_cpml(Problem& p, int nx, int ny, int npml, double dx, double dy, doub
 
 int parse_ini(const char* path, IniParams& ip, std::string& log);
 void ini_to_metric(IniParams& ip);
-int build_from_ini(const IniParams& ip, Problem& p);
+// objects = false is the SourceToDetect vacuum run: no medium, no fluctuation
+// (buildObject with ObjectsEnable == false, FDTD_2D_Full/FDTD_cuda.cu:2602-2625).
+int build_from_ini(const IniParams& ip, Problem& p, bool objects = true);
+
+// fdtd2d_problem_from_ini with the objects switch of build_from_ini.
+int problem_from_ini_ex(const char* path, bool objects, fdtd2d_problem** out);
 
 }  // namespace fdtd2d

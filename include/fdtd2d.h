@@ -282,6 +282,12 @@ int fdtd2d_problem_from_spec(const fdtd2d_spec *spec, fdtd2d_problem **out);
    reference builds (FDTD_2D_Full/FDTD_cuda.cu:305-382, 1122-1579, 2602-3655). */
 int fdtd2d_problem_from_ini(const char *ini_path, fdtd2d_problem **out);
 
+/* The SourceToDetect vacuum shot of a Settings.ini: the same setup with no
+   medium, fluctuation or wall (ObjectsEnable = false).  Replaces the first pass
+   of initlimits in that mode (FDTD_2D_Full/FDTD_cuda.cu:389-406) feeding
+   DevSourceToDetectInfluenceCalc (FDTD_2D_Full/kernel.cu:1620-1926). */
+int fdtd2d_problem_from_ini_vacuum(const char *ini_path, fdtd2d_problem **out);
+
 const fdtd2d_setup *fdtd2d_problem_setup(const fdtd2d_problem *p);
 void fdtd2d_problem_free(fdtd2d_problem *p);
 

@@ -35,13 +35,15 @@ REF_BIN = ROOT / "oracle" / "_ref" / "ref_fdtd2d"
 
 KEEP_TEXT = ["Detect.txt", "detAll.txt", "detEz.txt", "detHx.txt", "detHy.txt", "RC_Line.txt",
              "TAU_Line.txt", "SourceP.txt", "FieldSaveDat.txt", "Ez.txt", "RcDet_data.txt",
-             "SD.txt", "CF.txt", "ARC.txt", "det_SD.txt", "det_CF.txt", "det_ARC.txt"]
+             "SD.txt", "CF.txt", "ARC.txt", "det_SD.txt", "det_CF.txt", "det_ARC.txt",
+             "Detect_S2D.txt", "detAll_S2D.txt", "detEz_S2D.txt", "detHx_S2D.txt", "detHy_S2D.txt",
+             "DifDetEx.txt"]
 
 BASE = """;golden case {name}
 [hardware]
 GPU_device=0
 [regimes]
-SourceToDetect = 0
+SourceToDetect = {s2d}
 [grid]
 Use_Exp_time = 1
 Imax = {imax}
@@ -160,13 +162,19 @@ CASES = {
     "tof_line": dict(ds=1.0, imax=80, jmax=120, exp=0.6, isrc=40, angle=0, chirp=0, save_to=-1,
                      sieve=100, build=1, jcen=100, fluc=0, fluci=0, flucj=0, wall=0, wallpos=950,
                      extra=PROCESSING),
+    # SourceToDetect: a vacuum run (no medium, no wall) then the run with the
+    # medium; the wall is asked for but the reference never builds it in this
+    # mode; difference traces in DifDetEx.txt
+    "s2d_sphere": dict(s2d=1, imax=60, jmax=110, exp=0.3, isrc=30, angle=5, chirp=0, save_to=-1,
+                       sieve=100, build=1, jcen=70, fluc=2, fluci=25, flucj=60, wall=1,
+                       wallpos=180, extra=""),
 }
 
 
 def make_case(name: str, params: dict) -> None:
     out = HERE / name
     out.mkdir(exist_ok=True)
-    ini = BASE.format(name=name, **{"ds": 0.5, **params})
+    ini = BASE.format(name=name, **{"ds": 0.5, "s2d": 0, **params})
     with tempfile.TemporaryDirectory() as td:
         run = Path(td)
         (run / "Settings.ini").write_text(ini)
@@ -192,7 +200,7 @@ def make_case(name: str, params: dict) -> None:
         np.savez_compressed(out / "state.npz", **state)
         (out / "Settings.ini").write_text(ini)
         for f in KEEP_TEXT:
-            if name == "long_rc" and f in ("detEz.txt", "detHx.txt", "detHy.txt"):
+            if name in ("long_rc", "s2d_sphere") and f in ("detEz.txt", "detHx.txt", "detHy.txt"):
                 continue  # the same samples are in state.npz; keeps the fixture small
             src = run / f
             if src.exists() and src.stat().st_size > 0:

@@ -105,3 +105,36 @@ def test_tof_files(run):
         m, r = np.loadtxt(out / f), np.loadtxt(ref_f)
         assert m.shape == r.shape and np.array_equal(m[:, 0], r[:, 0]), f
         assert np.mean(np.abs(m[:, 1] - r[:, 1]) <= 1) >= 0.95, f
+
+
+def test_source_to_detect_files(run):
+    """SourceToDetect cases: the vacuum shot's *_S2D.txt files and the
+    main - vacuum DifDetEx.txt against the reference's (per-element samples
+    relative L2 <= 1e-5; sum columns within 1e-5 of the summed element
+    magnitudes)."""
+    case, out = run
+    g = GOLDEN / case
+    if not (g / "Detect_S2D.txt").exists():
+        pytest.skip("not a SourceToDetect case")
+    per = {}
+    for f in ("detEz_S2D.txt", "detHx_S2D.txt", "detHy_S2D.txt"):
+        m, r = numbers(out / f), numbers(g / f)
+        assert m.shape == r.shape, f
+        assert np.linalg.norm(m - r) <= 1e-5 * np.linalg.norm(r), f
+        per[f[3:5]] = r.reshape(len(table(g / "Detect_S2D.txt")), -1)
+    m, r = np.array(table(out / "Detect_S2D.txt")), np.array(table(g / "Detect_S2D.txt"))
+    assert m.shape == r.shape
+    assert np.abs(m[:, 0] - r[:, 0]).max() <= 1.5e-6 * max(1.0, np.abs(r[:, 0]).max())
+    assert np.linalg.norm(m[:, 1] - r[:, 1]) <= 1e-5 * np.linalg.norm(np.abs(per["Ez"]).sum(1))
+    m, r = np.array(table(out / "detAll_S2D.txt")), np.array(table(g / "detAll_S2D.txt"))
+    assert m.shape == r.shape
+    for c, k in ((3, "Ez"), (4, "Hx"), (5, "Hy")):
+        assert np.linalg.norm(m[:, c] - r[:, c]) <= 1e-5 * np.linalg.norm(np.abs(per[k]).sum(1)), c
+    st = np.load(g / "state.npz")
+    main = {"Ez": st["det_Ez"] * 1000, "Hx": st["det_Hx"] * 1000, "Hy": st["det_Hy"] * 1000}
+    m, r = np.array(table(out / "DifDetEx.txt")), np.array(table(g / "DifDetEx.txt"))
+    assert m.shape == r.shape and not m[:, [1, 2, 6]].any()
+    for c, k in ((3, "Ez"), (4, "Hx"), (5, "Hy")):
+        mag = (np.abs(main[k]) + np.abs(per[k])).sum(1)
+        assert np.linalg.norm(m[:, c] - r[:, c]) <= 1e-5 * np.linalg.norm(mag), c
+    assert np.linalg.norm(m[:, 7] - r[:, 7]) <= 1e-5 * np.linalg.norm(r[:, 7])

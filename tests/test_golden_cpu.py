@@ -10,6 +10,7 @@ tests/golden/make_golden.py from the reference's own sources built for the CPU).
   TAU_Line.txt, TOF files) reproduces the reference's files from the
   reference's own inputs.
 """
+import re
 from pathlib import Path
 
 import numpy as np
@@ -180,3 +181,61 @@ def test_tof_files_match_reference(case, tmp_path):
         # may move by a step when the fields differ in the last bits)
         assert np.mean(np.abs(mine[:, 1] - ref[:, 1]) <= 1) >= 0.95, f
         assert np.array_equal(mine[:, 0], ref[:, 0]), f
+
+
+NUM = re.compile(r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[eE][-+]?\d+)?")
+
+
+def _table(path: Path) -> np.ndarray:
+    return np.array([[float(x) for x in NUM.findall(ln)] for ln in path.read_text().splitlines() if ln.strip()])
+
+
+def _rows(a: np.ndarray) -> np.ndarray:
+    """Oracle trace rows (row r = step r+1) in the reference's file rows
+    (row i = step i, row 0 zeros, the last step not printed)."""
+    out = np.zeros_like(a)
+    out[1:] = a[:-1]
+    return out
+
+
+def test_source_to_detect_files_match_reference():
+    """SourceToDetect mode: the vacuum shot (no medium, no wall, full launch
+    coverage: that pass launches one block more than the floor) against the
+    reference's *_S2D.txt files, and main - vacuum against DifDetEx.txt.  Sum
+    columns are held to 1e-5 of the summed element magnitudes (the Hy sum
+    nearly cancels about the array centre)."""
+    g = GOLDEN / "s2d_sphere"
+    p = F.Problem.from_ini(g / "Settings.ini")
+    v = F.Problem.from_ini(g / "Settings.ini", vacuum=True)
+    n = p.n_steps
+    sv = v.setup
+    assert not np.ctypeslib.as_array(sv.id3, shape=(sv.nx * sv.ny,)).any()
+    need = [sv.nx * sv.ny, sv.nx * sv.npml, sv.nx * sv.ny, sv.npml * sv.ny, sv.nx * sv.ny, sv.nx * sv.ny,
+            sv.npml * sv.ny, sv.nx * sv.npml]   # cells per reference launch (kernel order of cover[])
+    assert all(sv.cover[k] >= need[k] for k in range(8))
+    om, ov = O.Oracle(p.setup_ptr), O.Oracle(v.setup_ptr)
+    om.run(1, n)
+    ov.run(1, n)
+    tm, tv = om.traces(1, n), ov.traces(1, n)
+    vez, vhx, vhy = (_rows(tv[k]) for k in ("comp_ez", "comp_hx", "comp_hy"))
+    mez, mhx, mhy = (_rows(tm[k]) for k in ("comp_ez", "comp_hx", "comp_hy"))
+    for f, a in (("detEz_S2D.txt", vez), ("detHx_S2D.txt", vhx), ("detHy_S2D.txt", vhy)):
+        ref = np.array([float(x) for x in NUM.findall((g / f).read_text())]).reshape(n, -1) / 1000
+        assert O.rel_l2(a, ref) <= 1e-5, f
+    det = _table(g / "Detect_S2D.txt")
+    vd = _rows(tv["det_ez"])
+    assert np.abs(det[:, 0] - np.arange(n) * p.setup.dt * 1e6).max() <= 1e-6
+    assert np.linalg.norm(det[:, 1] / 1000 - vd.sum(1)) <= 1e-5 * np.linalg.norm(np.abs(vd).sum(1))
+    alls = _table(g / "detAll_S2D.txt")
+    for c, a in ((3, vez), (4, vhx), (5, vhy)):
+        assert np.linalg.norm(alls[:, c] / 1000 - a.sum(1)) <= 1e-5 * np.linalg.norm(np.abs(a).sum(1)), c
+    dif = _table(g / "DifDetEx.txt")
+    assert dif.shape == (n, 8) and not dif[:, [1, 2, 6]].any()
+    sums = []
+    for c, (m, w) in ((3, (mez, vez)), (4, (mhx, vhx)), (5, (mhy, vhy))):
+        d = (m - w).sum(1)
+        sums.append(d)
+        assert np.linalg.norm(dif[:, c] / 1000 - d) <= 1e-5 * np.linalg.norm((np.abs(m) + np.abs(w)).sum(1)), c
+    s3, s4, s5 = sums
+    eh = np.hypot(s3 * s5, s3 * s4)
+    assert O.rel_l2(dif[:, 7] / 1000, eh) <= 1e-5
