@@ -141,6 +141,17 @@ def _lib():
         "fdtd2d_device_bytes": (C.c_int64, [C.POINTER(Setup)]),
         "fdtd2d_launch_count": (C.c_int64, [vp]),
         "fdtd2d_kernel_name": (C.c_char_p, [vp]),
+        "fdtd2d_batch_create": (C.c_int, [C.c_int, C.c_int64, C.POINTER(vp)]),
+        "fdtd2d_batch_add": (C.c_int, [vp, C.POINTER(Setup), C.POINTER(C.c_int32)]),
+        "fdtd2d_batch_run": (C.c_int, [vp, C.c_int32]),
+        "fdtd2d_batch_synchronize": (C.c_int, [vp]),
+        "fdtd2d_batch_shot_step": (C.c_int32, [vp, C.c_int32]),
+        "fdtd2d_batch_shot": (vp, [vp, C.c_int32]),
+        "fdtd2d_batch_remove": (C.c_int, [vp, C.c_int32]),
+        "fdtd2d_batch_free_bytes": (C.c_int64, [vp]),
+        "fdtd2d_batch_launch_count": (C.c_int64, [vp]),
+        "fdtd2d_batch_kernel_name": (C.c_char_p, [vp]),
+        "fdtd2d_batch_destroy": (C.c_int, [vp]),
         "fdtd2d_last_cuda_error": (C.c_int, [vp]),
         "fdtd2d_spec_defaults": (None, [C.POINTER(Spec)]),
         "fdtd2d_problem_from_spec": (C.c_int, [C.POINTER(Spec), C.POINTER(vp)]),
@@ -289,11 +300,15 @@ class Problem:
 class Shot:
     """One shot's device state on one GPU (one CUDA stream)."""
 
-    def __init__(self, problem: Problem, device: int = 0):
+    def __init__(self, problem: Problem, device: int = 0, _handle=None):
         self.problem = problem
         s = problem.setup
         self.nx, self.ny, self.npml, self.n_steps = s.nx, s.ny, s.npml, s.n_steps
         self.n_det, self.n_comp = s.n_det, s.n_comp
+        self._owned = _handle is None
+        if _handle is not None:   # a batch member's context (owned by the batch)
+            self._h = C.c_void_p(_handle)
+            return
         h = C.c_void_p()
         _check(_lib().fdtd2d_create(problem.setup_ptr, device, C.byref(h)), "fdtd2d_create")
         self._h = h
@@ -377,8 +392,79 @@ class Shot:
         return True
 
     def close(self) -> None:
-        if getattr(self, "_h", None) and self._h.value:
+        if getattr(self, "_h", None) and self._h.value and getattr(self, "_owned", True):
             _lib().fdtd2d_destroy(self._h)
+        self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many uniform-medium shots advanced together on one GPU (fdtd2d_batch_*):
+    one persistent launch per time step in CUDA-graph blocks, each shot at its
+    own step, admission by a device-memory budget."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0):
+        h = C.c_void_p()
+        _check(_lib().fdtd2d_batch_create(device, budget_bytes, C.byref(h)), "fdtd2d_batch_create")
+        self._h = h
+        self._problems: dict[int, Problem] = {}
+
+    def add(self, problem: Problem) -> int | None:
+        """Admit a shot; None when it does not fit the remaining budget."""
+        sid = C.c_int32()
+        rc = _lib().fdtd2d_batch_add(self._h, problem.setup_ptr, C.byref(sid))
+        if rc == ERR_BUDGET:
+            return None
+        _check(rc, "fdtd2d_batch_add")
+        self._problems[sid.value] = problem
+        return sid.value
+
+    def run(self, n_steps: int) -> None:
+        _check(_lib().fdtd2d_batch_run(self._h, n_steps), "fdtd2d_batch_run")
+
+    def synchronize(self) -> None:
+        _check(_lib().fdtd2d_batch_synchronize(self._h), "fdtd2d_batch_synchronize")
+
+    def step(self, shot: int) -> int:
+        return int(_lib().fdtd2d_batch_shot_step(self._h, shot))
+
+    def finished(self, shot: int) -> bool:
+        return self.step(shot) >= self._problems[shot].n_steps
+
+    def shot(self, shot: int) -> Shot:
+        """The member as a Shot (traces, dft, read_field); owned by the batch."""
+        h = _lib().fdtd2d_batch_shot(self._h, shot)
+        if not h:
+            raise FdtdError(ERR_INVALID, "fdtd2d_batch_shot")
+        return Shot(self._problems[shot], _handle=h)
+
+    def remove(self, shot: int) -> None:
+        _check(_lib().fdtd2d_batch_remove(self._h, shot), "fdtd2d_batch_remove")
+        self._problems.pop(shot, None)
+
+    def free_bytes(self) -> int:
+        return int(_lib().fdtd2d_batch_free_bytes(self._h))
+
+    def launches(self) -> int:
+        return int(_lib().fdtd2d_batch_launch_count(self._h))
+
+    def kernel_name(self) -> str:
+        return _lib().fdtd2d_batch_kernel_name(self._h).decode()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            _lib().fdtd2d_batch_destroy(self._h)
             self._h = C.c_void_p()
 
     def __enter__(self):

@@ -17,34 +17,7 @@
 
 using namespace fdtd2d;
 
-struct fdtd2d_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  int nx = 0, ny = 0, pitch = 0, npml = 0, n_steps = 0;
-  int n_det = 0, n_comp = 0, record = 0, medium = 0;
-  bool dft = false;
-  int32_t step = 0;
-  int last_cuda = 0;
-  int64_t launches = 0;
-  DevShot h{};              // host copy of the device descriptor
-  DevShot* d_shot = nullptr;
-  int4* d_units = nullptr;
-  int n_units = 0;
-  int grid_warps = 0;
-  int* d_flag = nullptr;
-  int* d_err = nullptr;     // device error word (bounded waits)
-  bool tma = false;         // shared-memory staged kernel (uniform medium)
-  int tma_shape = 0;        // its launch shape (index into the compiled shapes)
-  char kernel_name[48] = {0};
-  // wave-front tracker and line probe
-  int n_rc = 0, rc_j_cut = 0;
-  float rc_level = 0;
-  int *d_rc_scan = nullptr, *d_rc_max = nullptr, *d_spd = nullptr;
-  float* d_edge = nullptr;
-  int line_n = 0, line_i0 = 0, line_j = 0, line_first = 0, line_last = -1;
-  float* d_line = nullptr;
-  std::vector<void*> allocs;
-};
+#include "ctx.h"
 
 namespace {
 
@@ -180,6 +153,22 @@ int64_t fdtd2d_device_bytes(const fdtd2d_setup* s) {
 }
 
 int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
+  return fdtd2d::create_ctx(s, device, false, out);
+}
+
+}  // extern "C"
+
+void fdtd2d::adopt_ctx(fdtd2d_ctx* c, cudaStream_t batch_stream) {
+  cudaSetDevice(c->device);
+  if (c->stream && !c->batch) {
+    cudaStreamSynchronize(c->stream);
+    cudaStreamDestroy(c->stream);
+  }
+  c->stream = batch_stream;
+  c->batch = true;
+}
+
+int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out) {
   if (!out) return FDTD2D_ERR_INVALID;
   *out = nullptr;
   int rc = validate(s);
@@ -441,7 +430,9 @@ int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
       if (std::sscanf(t, "%d,%d", &w, &st) == 2) forced = tma_shape_find(w, st);
     }
     const char* at = std::getenv("FDTD2D_TMA_AUTOTUNE");
-    if (forced >= 0) {
+    if (member) {
+      // batch members are stepped by the batch's kernel
+    } else if (forced >= 0) {
       c->tma_shape = forced;
     } else if (!(at && std::strcmp(at, "0") == 0) && c->n_steps >= 1) {
       // Each trial re-runs step 1 with traces and the DFT switched off: a
@@ -512,8 +503,11 @@ int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
   return FDTD2D_OK;
 }
 
+extern "C" {
+
 int fdtd2d_run(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
   if (!c) return FDTD2D_ERR_INVALID;
+  if (c->batch) return FDTD2D_ERR_STATE;   // stepped by its batch
   if (n_first != c->step + 1 || n_last < n_first - 1 || n_last > c->n_steps) return FDTD2D_ERR_RANGE;
   cudaSetDevice(c->device);
   for (int32_t n = n_first; n <= n_last; ++n) {
@@ -763,7 +757,7 @@ int fdtd2d_destroy(fdtd2d_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (void* p : c->allocs) cudaFree(p);
-  if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->stream && !c->batch) cudaStreamDestroy(c->stream);
   delete c;
   return FDTD2D_OK;
 }

@@ -1,0 +1,52 @@
+// One shot's device state and launch configuration (the opaque fdtd2d_ctx of
+// the C ABI), shared by the single-shot entry points (api.cu) and the batch
+// (batch.cu), which owns shots created on its stream and steps them with its
+// own kernel.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/fdtd2d.h"
+#include "internal.h"
+
+struct fdtd2d_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool batch = false;       // member of a batch: stream borrowed, stepped by the batch
+  int nx = 0, ny = 0, pitch = 0, npml = 0, n_steps = 0;
+  int n_det = 0, n_comp = 0, record = 0, medium = 0;
+  bool dft = false;
+  int32_t step = 0;
+  int last_cuda = 0;
+  int64_t launches = 0;
+  fdtd2d::DevShot h{};      // host copy of the device descriptor
+  fdtd2d::DevShot* d_shot = nullptr;
+  int4* d_units = nullptr;
+  int n_units = 0;
+  int grid_warps = 0;
+  int* d_flag = nullptr;
+  int* d_err = nullptr;     // device error word (bounded waits)
+  bool tma = false;         // shared-memory staged kernel (uniform medium)
+  int tma_shape = 0;        // its launch shape (index into the compiled shapes)
+  char kernel_name[48] = {0};
+  // wave-front tracker and line probe
+  int n_rc = 0, rc_j_cut = 0;
+  float rc_level = 0;
+  int *d_rc_scan = nullptr, *d_rc_max = nullptr, *d_spd = nullptr;
+  float* d_edge = nullptr;
+  int line_n = 0, line_i0 = 0, line_j = 0, line_first = 0, line_last = -1;
+  float* d_line = nullptr;
+  std::vector<void*> allocs;
+};
+
+namespace fdtd2d {
+// fdtd2d_create; member = true makes a shot for a batch: no launch-shape
+// timing, and the batch adopts it (adopt_ctx) once its uploads are done.
+int create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out);
+// Hand a member shot to the batch's stream: its own stream is released and
+// fdtd2d_run is refused from then on (the batch steps it).
+void adopt_ctx(fdtd2d_ctx* c, cudaStream_t batch_stream);
+}  // namespace fdtd2d

@@ -125,6 +125,13 @@ int tma_max_pml();   // largest CPML depth the staged kernel takes
 int tma_resident_ctas(int shape, int npml, int device);
 cudaError_t launch_step_tma(int shape, const DevShot& shot, const int4* units, int n_units, int n_global,
                             int max_ctas, int* err, cudaStream_t stream);
+// Batched form: one launch advances every shot in `shots` by one step, units
+// (shot, c0, j0, j1) handed out dynamically; n_global = *gstep + k + 1.
+// counters: 2 ints, zero before the first launch.
+cudaError_t launch_step_tma_batch(int shape, const DevShot* shots, const int4* units, const int* n_units,
+                                  const int* gstep, int k, int* counters, int max_pml, int ctas, int* err,
+                                  cudaStream_t stream);
+int tma_batch_resident_ctas(int shape, int max_pml, int device);
 
 // Tabulate s_e(n) = scale*env[n]*cos(2*pi_c*(beta/2 t^2 + f0 t + phase_e)),
 // t = n*dt, for n = 0..n_steps, and the DFT twiddles, in FP64.

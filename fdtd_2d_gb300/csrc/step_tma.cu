@@ -12,7 +12,7 @@
 // from shared memory instead of dependent global loads.  The launch shape
 // (W, ST) is a template parameter; TmaShape lists the compiled ones.
 //
-// Every wait is bounded: after kSpinLimit failed polls the kernel records
+// Every wait is bounded: after kWaitNs (1 s) without progress the kernel records
 // kErrWaitTimeout in the shot's error word, waits (bounded) for the copies it
 // issued, and returns; the host reports FDTD2D_ERR_TIMEOUT.
 #include "internal.h"
@@ -22,7 +22,7 @@ namespace fdtd2d {
 
 namespace {
 
-constexpr int kSpinLimit = 1 << 20;
+constexpr uint64_t kWaitNs = 1000000000ull;   // 1 s bound on any barrier wait
 constexpr int kXSlot = 128;                    // floats reserved per staged x-strip row
 constexpr int kTmaMaxPml = kXSlot - 8;         // x-strip rows fit their stage slot
 
@@ -65,10 +65,19 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// Poll the barrier's phase `parity` at most kSpinLimit times.
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait for the barrier's phase `parity` to complete, for at most kWaitNs of
+// wall time (a try_wait may itself suspend for a while, so the bound is on
+// time, not on the number of polls).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   const uint32_t a = smem_u32(bar);
-  for (int it = 0; it < kSpinLimit; ++it) {
+  uint64_t t0 = 0;
+  for (int it = 0;; ++it) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -76,8 +85,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
         : "r"(a), "r"(parity)
         : "memory");
     if (done) return true;
+    if (it == 0) {
+      t0 = global_ns();
+    } else if ((it & 15) == 0 && global_ns() - t0 > kWaitNs) {
+      return false;
+    }
   }
-  return false;
 }
 
 __device__ __forceinline__ void bulk_copy(float* dst, const float* src, uint32_t bytes, uint64_t* bar) {
@@ -202,6 +215,10 @@ __device__ void process_band(const DevShot& S, Ring& R, const float* __restrict_
   // warp W-1), so the ring refill does not wait on the slower CPML lanes.
   const int prod_warp = (c0 == 0 && C::kWarps > 1) ? C::kWarps - 1 : 0;
   const bool producer = tid == prod_warp * 32;
+  // The ring is drained between units (every issued row was consumed), and
+  // every thread counts the consumed rows, so the ring position carries over
+  // to whichever thread produces for this unit.
+  R.issued = R.used;
 
   // Fill the ring.
   if (producer) {
@@ -488,17 +505,77 @@ step_tma_kernel(const __grid_constant__ DevShot S, const int4* __restrict__ unit
   }
 }
 
+// Batched form: one launch advances every shot of a batch by one step.  The
+// shots' descriptors sit in a device array; units (shot, c0, j0, j1) are
+// handed out dynamically (one atomic counter per step parity, so CTAs that
+// drew short or fast units take more); each shot runs its own step
+// n = n_global - base_n, and units of shots outside [1, n_steps] are skipped,
+// so shots admitted at different times advance together.  n_global is read
+// from device memory (the step-block base, advanced by the graph's last node)
+// plus the launch's offset k within the block, so one captured graph of K
+// launches serves every block.
+template <class C>
+__global__ void __launch_bounds__(C::kThreads, C::kMinBlocks)
+step_tma_batch_kernel(const DevShot* __restrict__ shots, const int4* __restrict__ units,
+                      const int* __restrict__ n_units_p, const int* __restrict__ gstep_p, int k, int* counters,
+                      int* err) {
+  extern __shared__ __align__(128) float smem[];
+  __shared__ __align__(8) uint64_t full[C::kStages], empty[C::kStages];
+  __shared__ __align__(16) DevShot sS;
+  __shared__ int s_unit;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    for (int s = 0; s < C::kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], C::kWarps);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  const int n_global = *gstep_p + k + 1;
+  const int n_units = *n_units_p;
+  int* ctr = counters + (n_global & 1);
+  if (blockIdx.x == 0 && tid == 0) counters[(n_global + 1) & 1] = 0;   // the next step's counter
+  __syncthreads();
+  Ring R;
+  R.stage = smem;
+  R.full = full;
+  R.empty = empty;
+  float* cp = smem + C::kStages * C::kStageFloats;   // CPML table of the current shot
+  int cur = -1;
+  for (;;) {
+    if (tid == 0) s_unit = *(volatile int*)err ? n_units : atomicAdd(ctr, 1);
+    __syncthreads();
+    const int u = s_unit;
+    if (u >= n_units) break;
+    const int4 ud = __ldg(units + u);
+    if (ud.x != cur) {
+      const int* src = reinterpret_cast<const int*>(shots + ud.x);
+      int* dst = reinterpret_cast<int*>(&sS);
+      for (int t = tid; t < (int)(sizeof(DevShot) / 4); t += C::kThreads) dst[t] = __ldg(src + t);
+      __syncthreads();
+      for (int t = tid; t < kCpmlRows * sS.npml; t += C::kThreads) cp[t] = sS.cpml[t];
+      cur = ud.x;
+      __syncthreads();
+    }
+    const int n = n_global - sS.base_n;
+    if (n >= 1 && n <= sS.n_steps) process_band<C>(sS, R, cp, ud.y, ud.z, ud.w, n, err);
+    __syncthreads();   // every thread has read s_unit (and sS) before the next unit overwrites them
+  }
+}
+
 using KernelFn = void (*)(DevShot, const int4*, int, int, int*);
+using BatchFn = void (*)(const DevShot*, const int4*, const int*, const int*, int, int*, int*);
 
 struct ShapeEntry {
   int warps, stages;
   KernelFn fn;
+  BatchFn bfn;
   size_t smem;
 };
 
 template <int W, int ST>
 constexpr ShapeEntry entry() {
-  return {W, ST, step_tma_kernel<Cfg<W, ST>>, Cfg<W, ST>::kSmem};
+  return {W, ST, step_tma_kernel<Cfg<W, ST>>, step_tma_batch_kernel<Cfg<W, ST>>, Cfg<W, ST>::kSmem};
 }
 
 // Compiled launch shapes; the first is the default.
@@ -537,6 +614,25 @@ cudaError_t launch_step_tma(int shape, const DevShot& shot, const int4* units, i
   if (ctas <= 0) return cudaSuccess;
   e.fn<<<ctas, e.warps * 32, smem_bytes(e, shot.npml), stream>>>(shot, units, n_units, n_global, err);
   return cudaGetLastError();
+}
+
+cudaError_t launch_step_tma_batch(int shape, const DevShot* shots, const int4* units, const int* n_units,
+                                  const int* gstep, int k, int* counters, int max_pml, int ctas, int* err,
+                                  cudaStream_t stream) {
+  const ShapeEntry& e = kShapes[shape];
+  e.bfn<<<ctas, e.warps * 32, smem_bytes(e, max_pml), stream>>>(shots, units, n_units, gstep, k, counters, err);
+  return cudaGetLastError();
+}
+
+int tma_batch_resident_ctas(int shape, int max_pml, int device) {
+  const ShapeEntry& e = kShapes[shape];
+  const size_t smem = smem_bytes(e, max_pml);
+  cudaFuncSetAttribute(e.bfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(e, kTmaMaxPml));
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, e.bfn, e.warps * 32, smem);
+  if (per_sm < 1) per_sm = 1;
+  return sms * per_sm;
 }
 
 int tma_resident_ctas(int shape, int npml, int device) {

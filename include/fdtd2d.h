@@ -219,6 +219,36 @@ int64_t fdtd2d_launch_count(const fdtd2d_ctx *ctx);
    (e.g. "step_tma_kernel<4,3>"; no counterpart in the reference). */
 const char *fdtd2d_kernel_name(const fdtd2d_ctx *ctx);
 
+/* ---- Batched and continuous stepping (no counterpart in the reference, which
+   runs one shot per process with global state, FDTD_2D_Full/kernel.cu:1928-2818).
+   A batch advances many uniform-medium shots (CPML <= 120 cells, no wave-front
+   tracker or line probe) together: one persistent launch per time step, issued
+   in blocks captured as CUDA graphs, each shot at its own step.  Shots can be
+   admitted between fdtd2d_batch_run calls while others are in flight. ---- */
+typedef struct fdtd2d_batch fdtd2d_batch;
+
+/* hbm_budget_bytes <= 0: 90 % of the device memory free now. */
+int fdtd2d_batch_create(int device, int64_t hbm_budget_bytes, fdtd2d_batch **out);
+/* Admit a shot (its device state is allocated and uploaded now; its step 1
+   runs in the next step the batch issues).  FDTD2D_ERR_BUDGET when its
+   fdtd2d_device_bytes would exceed the remaining budget. */
+int fdtd2d_batch_add(fdtd2d_batch *b, const fdtd2d_setup *setup, int32_t *shot);
+/* Issue n_steps more steps of every admitted, unfinished shot (asynchronous). */
+int fdtd2d_batch_run(fdtd2d_batch *b, int32_t n_steps);
+/* Wait for the issued steps; FDTD2D_ERR_TIMEOUT if a kernel wait ran out. */
+int fdtd2d_batch_synchronize(fdtd2d_batch *b);
+/* Steps issued for a shot (it is finished when this equals its n_steps). */
+int32_t fdtd2d_batch_shot_step(const fdtd2d_batch *b, int32_t shot);
+/* The shot's context, for fdtd2d_read_* (which wait for the batch's stream);
+   fdtd2d_run on it returns FDTD2D_ERR_STATE. */
+fdtd2d_ctx *fdtd2d_batch_shot(fdtd2d_batch *b, int32_t shot);
+/* Free a shot's device memory and its slot. */
+int fdtd2d_batch_remove(fdtd2d_batch *b, int32_t shot);
+int64_t fdtd2d_batch_free_bytes(const fdtd2d_batch *b);
+int64_t fdtd2d_batch_launch_count(const fdtd2d_batch *b);
+const char *fdtd2d_batch_kernel_name(const fdtd2d_batch *b);
+int fdtd2d_batch_destroy(fdtd2d_batch *b);
+
 /* Number of CUDA devices visible to this process (0 when none). */
 int fdtd2d_device_count(void);
 

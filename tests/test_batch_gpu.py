@@ -1,0 +1,142 @@
+"""Batched / continuous stepping (fdtd2d_batch_*) on the GPU.
+
+A shot stepped in a batch goes through the same update code as a shot
+stepped alone (one launch per step, every unit's halo recomputed bit-exactly
+from the previous step's buffers), so its fields, traces and DFT must be
+bitwise identical to the same shot run alone, whatever else is in the batch
+and whenever it was admitted.  One member is also checked against the FP64
+oracle.
+"""
+import numpy as np
+import pytest
+
+import fdtd_2d_gb300 as F
+import oracle as O
+from helpers import FIELD_TOL, FIELDS, PSI_FIELDS, compare_fields, dft_phase_error, rel
+
+pytestmark = pytest.mark.gpu
+
+
+def shot_spec(k: int) -> dict:
+    """Uneven shots: sizes, CPML depths, frequencies, plasma and arrays differ."""
+    rng = np.random.default_rng(100 + k)
+    nx = int(rng.integers(150, 700))
+    ny = int(rng.integers(120, 500))
+    P = int(rng.integers(6, 24))
+    n_elem = int(rng.integers(2, 6))
+    return dict(nx=nx, ny=ny, npml=P, n_steps=int(rng.integers(150, 400)), dx=0.5e-3, dy=0.5e-3,
+                courant=0.9, profile=3, ne_peak=float(rng.uniform(5e18, 3e19)), x_center=nx * 0.6,
+                width=nx * 0.1, grf_rms=0.05, grf_corr=8, seed=k + 1, nu=2e9, n_elem=n_elem,
+                src_i=P + 6, src_j=ny // 2 - 2 * n_elem, src_di=0, src_dj=4,
+                freq=float(rng.uniform(20e9, 60e9)), steer_deg=10, pulse=1, pulse_width=0.1e-9,
+                n_det=n_elem, det_i=P + 6, det_j=ny // 2 - 2 * n_elem, det_di=0, det_dj=4,
+                dft_freq=0.0)
+
+
+def problems(n: int):
+    out = []
+    for k in range(n):
+        sp = shot_spec(k)
+        sp["dft_freq"] = sp["freq"]
+        out.append(F.Problem.from_spec(**sp))
+    return out
+
+
+def alone(prob, gpu):
+    with F.Shot(prob, gpu) as s:
+        s.run(1, prob.n_steps)
+        return snapshot(s)
+
+
+def snapshot(shot):
+    d = {w: shot.read_field(w) for w in FIELDS + PSI_FIELDS}
+    d["traces"] = shot.traces()
+    d["dft"] = shot.dft()
+    return d
+
+
+def assert_same(a, b, what):
+    for k in a:
+        if k == "traces":
+            for t in a[k]:
+                assert np.array_equal(a[k][t], b[k][t]), (what, k, t)
+        else:
+            assert np.array_equal(a[k], b[k]), (what, k)
+
+
+def test_batch_members_equal_alone(gpu):
+    """Five uneven shots admitted together, stepped to completion in blocks
+    that do not divide their lengths: each equals its solo run bitwise."""
+    probs = problems(5)
+    ref = [alone(p, gpu) for p in probs]
+    with F.Batch(gpu) as b:
+        ids = [b.add(p) for p in probs]
+        assert all(i is not None for i in ids)
+        assert b.kernel_name().startswith("step_tma_batch_kernel<")
+        while not all(b.finished(i) for i in ids):
+            b.run(37)
+        b.synchronize()
+        for i, r, p in zip(ids, ref, probs):
+            assert b.step(i) == p.n_steps
+            assert_same(snapshot(b.shot(i)), r, f"shot {i}")
+
+
+def test_continuous_admission_equal_alone(gpu):
+    """Shots admitted while others are part-way through (continuous batching),
+    and a finished shot removed to make room: results are unchanged."""
+    probs = problems(4)
+    ref = [alone(p, gpu) for p in probs]
+    with F.Batch(gpu) as b:
+        a = b.add(probs[0])
+        b.run(60)
+        c = b.add(probs[1])
+        b.run(45)
+        d = b.add(probs[2])
+        while not b.finished(a):
+            b.run(16)
+        b.synchronize()
+        assert_same(snapshot(b.shot(a)), ref[0], "first")
+        b.remove(a)
+        e = b.add(probs[3])
+        while not all(b.finished(i) for i in (c, d, e)):
+            b.run(50)
+        b.synchronize()
+        for i, r in ((c, ref[1]), (d, ref[2]), (e, ref[3])):
+            assert_same(snapshot(b.shot(i)), r, f"shot {i}")
+
+
+def test_member_against_oracle(gpu):
+    """A batch member against the FP64 oracle: fields (1e-5 of the peak norm),
+    traces and DFT phase, with another shot in the batch."""
+    p0, p1 = problems(2)
+    ref = O.Oracle(p0.setup_ptr)
+    ref32 = O.Oracle(p0.setup_ptr, fp32=True)
+    ref.run(1, p0.n_steps)
+    ref32.run(1, p0.n_steps)
+    with F.Batch(gpu) as b:
+        i = b.add(p0)
+        b.add(p1)
+        b.run(max(p0.n_steps, p1.n_steps))
+        b.synchronize()
+        s = b.shot(i)
+        compare_fields(s, ref, FIELDS + PSI_FIELDS, tol=FIELD_TOL, ref32=ref32)
+        assert rel(s.traces()["det_ez"], ref.traces()["det_ez"]) <= FIELD_TOL
+        assert dft_phase_error(s, ref) <= 1e-4
+
+
+def test_budget_admission_and_state(gpu):
+    """Admission by device-memory budget; a member cannot be run on its own."""
+    p0, p1 = problems(2)
+    budget = p0.device_bytes() + p1.device_bytes() // 2
+    with F.Batch(gpu, budget_bytes=budget) as b:
+        i = b.add(p0)
+        assert i is not None
+        assert b.add(p1) is None                    # does not fit yet
+        assert b.free_bytes() == budget - p0.device_bytes()
+        with pytest.raises(F.FdtdError) as ei:
+            b.shot(i).run(1, 1)
+        assert ei.value.status == F.ERR_STATE
+        b.run(p0.n_steps)
+        b.synchronize()
+        b.remove(i)
+        assert b.add(p1) is not None                # room after the removal
