@@ -39,6 +39,8 @@ import tempfile
 import time
 from pathlib import Path
 
+import numpy as np
+
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
@@ -182,6 +184,168 @@ def make_problem(n_steps: int, size: int):
     return F.Problem.from_spec(F.production_spec(n_steps=n_steps, **kw))
 
 
+C0 = 299792458.0
+
+
+def mixed_shot_spec(rng, side_lo: float, side_hi: float, f_lo: float, f_hi: float, step_scale: float,
+                    seed: int, aspect: bool = True, freq: float | None = None) -> dict:
+    """One uneven reflectometry shot: side log-uniform in [side_lo, side_hi]
+    (aspect 1:1..1:3 on a random axis), CPML 16..32, dx = lambda/20 at the
+    probe frequency, 4..16 elements (pitch 5) with co-located detectors and an
+    FP64 DFT at the probe frequency, tanh plasma with peak in [5e18, 5e19] and
+    centre in [0.4, 0.8] nx, width 600 * (0.25 mm / dx) cells, 5 % GRF,
+    nu = 2e9, 8000..16000 steps times step_scale.  The Courant number is the
+    largest <= 0.99 that keeps the Drude leapfrog stable at the peak density."""
+    L = float(np.exp(rng.uniform(np.log(side_lo), np.log(side_hi))))
+    a = float(rng.uniform(1, 3)) if aspect else 1.0
+    S = max(384.0, L / a)
+    nx, ny = (int(L), int(S)) if rng.uniform() < 0.5 else (int(S), int(L))
+    P = int(rng.integers(16, 33))
+    f = float(rng.uniform(f_lo, f_hi)) if freq is None else freq
+    dx = C0 / f / 20
+    peak = float(rng.uniform(5e18, 5e19))
+    xc = float(rng.uniform(0.4, 0.8)) * nx
+    wp = 56.4 * np.sqrt(peak * 1.25)            # GRF headroom on the peak
+    g = wp * dx / (2 * C0 * np.sqrt(2))         # (omega_p dt / 2) per unit Courant number
+    cour = float(min(0.99, 0.985 / np.sqrt(1 + g * g)))
+    n_elem = int(rng.integers(4, 17))
+    steps = max(16, int(int(rng.integers(8000, 16001)) * step_scale))
+    j0 = ny // 2 - 5 * n_elem // 2
+    return dict(nx=nx, ny=ny, npml=P, n_steps=steps, dx=dx, dy=dx, courant=cour, profile=3, ne_peak=peak,
+                x_center=xc, width=600 * (0.25e-3 / dx), grf_rms=0.05, grf_corr=40, seed=seed, nu=2e9,
+                n_elem=n_elem, src_i=P + 32, src_j=j0, src_di=0, src_dj=5, freq=f, steer_deg=15, pulse=1,
+                pulse_width=2e-9, n_det=n_elem, det_i=P + 32, det_j=j0, det_di=0, det_dj=5, dft_freq=f)
+
+
+def run_batched(args, local: int) -> tuple[dict, float]:
+    """64 uneven shots (seed 1002) end to end: one at a time through the
+    single-shot ABI vs all admitted to one batch.  Returns the JSON object and
+    the batch's throughput in cell updates per second."""
+    import fdtd_2d_gb300 as F
+
+    rng = np.random.default_rng(1002)
+    specs = [mixed_shot_spec(rng, 1024, 6144, 20e9, 75e9, args.batch_step_scale, 1002 + k)
+             for k in range(args.batch_shots)]
+    probs = [F.Problem.from_spec(**sp) for sp in specs]
+    cells = sum(p.nx * p.ny * p.n_steps for p in probs)
+    t = time.perf_counter()
+    plain_dft = []
+    for p in probs:
+        with F.Shot(p, local) as s:
+            s.run(1, p.n_steps)
+            s.traces()
+            plain_dft.append(s.dft())
+    tp = time.perf_counter() - t
+    t = time.perf_counter()
+    with F.Batch(local) as b:
+        ids = [b.add(p) for p in probs]
+        if any(i is None for i in ids):
+            raise RuntimeError("batch budget too small for the mixed-shot sample")
+        while not all(b.finished(i) for i in ids):
+            b.run(256)
+        b.synchronize()
+        batch_dft = []
+        for i in ids:
+            sh = b.shot(i)
+            sh.traces()
+            batch_dft.append(sh.dft())
+        name = b.kernel_name()
+        launches = b.launches()
+    tb = time.perf_counter() - t
+    same = all(np.array_equal(x, y) for x, y in zip(plain_dft, batch_dft))
+    n = len(probs)
+    out = {"shots": n, "sample": f"{n} shots, seed 1002, sides log-uniform 1024..6144 (aspect 1..3), CPML 16..32, "
+                                 f"20..75 GHz at dx = lambda/20, 4..16 elements, 8000..16000 steps x "
+                                 f"{args.batch_step_scale} ({sum(p.n_steps for p in probs)} steps in all)",
+           "cell_updates": cells, "plain_shots_per_s": n / tp, "batched_shots_per_s": n / tb,
+           "speedup": tp / tb, "plain_gcells": cells / tp / 1e9, "batched_gcells": cells / tb / 1e9,
+           "kernel": name, "gpu_launches": int(launches),
+           "dft_equal_to_plain": bool(same),
+           "note": "end to end from host setups: create/upload, all steps, traces + DFT read back; the batch "
+                   "is one persistent launch per step in CUDA-graph blocks of 16"}
+    return out, cells / tb
+
+
+def run_serving(args, local: int, capacity: float) -> dict:
+    """Poisson request stream (seed 1004) at 0.8 x the measured batched
+    capacity: each request a 4..12-shot frequency sweep over 10..75 GHz on one
+    grid size; served by the continuous-batching loop vs one request at a
+    time through the single-shot ABI."""
+    import fdtd_2d_gb300 as F
+
+    rng = np.random.default_rng(1004)
+    reqs = []
+    for r in range(args.serve_requests):
+        n_shots = int(rng.integers(4, 13))
+        freqs = np.sort(rng.uniform(10e9, 75e9, n_shots))
+        side = float(np.exp(rng.uniform(np.log(512), np.log(args.serve_max_side))))
+        shots = []
+        for k, f in enumerate(freqs):
+            sub = np.random.default_rng([1004, r, k])
+            sp = mixed_shot_spec(sub, side, side, f, f, args.batch_step_scale, 5000 + 100 * r + k, aspect=False,
+                                 freq=float(f))
+            shots.append(F.Problem.from_spec(**sp))
+        reqs.append(shots)
+    work = [sum(p.nx * p.ny * p.n_steps for p in q) for q in reqs]
+    rate = 0.8 * capacity / (sum(work) / len(work))      # requests per second
+    gaps = rng.exponential(1.0 / rate, len(reqs))
+    arrive = np.cumsum(gaps) - gaps[0]
+
+    def pct(lat):
+        return {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
+                "p99": float(np.percentile(lat, 99))}
+
+    # continuous batching
+    t0 = time.perf_counter()
+    done_at = {}
+    left = {r: len(q) for r, q in enumerate(reqs)}
+    nxt = 0
+    with F.Server(local, block_steps=64) as srv:
+        while len(done_at) < len(reqs):
+            now = time.perf_counter() - t0
+            while nxt < len(reqs) and arrive[nxt] <= now:
+                for k, p in enumerate(reqs[nxt]):
+                    srv.submit(p, nxt * 1000 + k)
+                nxt += 1
+            q, running, fin = srv.counts()
+            if q == 0 and running == 0 and fin == 0 and nxt < len(reqs):
+                time.sleep(max(0.0, arrive[nxt] - (time.perf_counter() - t0)))
+                continue
+            srv.step()
+            while (res := srv.pop()) is not None:
+                r = res["tag"] // 1000
+                left[r] -= 1
+                if left[r] == 0:
+                    done_at[r] = time.perf_counter() - t0
+        kernel = srv.batch_kernel_name()
+    t_batch = max(done_at.values())
+    lat_b = [done_at[r] - arrive[r] for r in range(len(reqs))]
+
+    # one request at a time, in arrival order
+    t0 = time.perf_counter()
+    lat_p = []
+    for r, q in enumerate(reqs):
+        now = time.perf_counter() - t0
+        if now < arrive[r]:
+            time.sleep(arrive[r] - now)
+        for p in q:
+            with F.Shot(p, local) as s:
+                s.run(1, p.n_steps)
+                s.traces()
+                s.dft()
+        lat_p.append(time.perf_counter() - t0 - arrive[r])
+    t_plain = time.perf_counter() - t0
+    n_shots = sum(len(q) for q in reqs)
+    return {"requests": len(reqs), "shots": n_shots,
+            "sample": f"{len(reqs)} Poisson requests (seed 1004) of 4..12-shot sweeps over 10..75 GHz, square "
+                      f"grids log-uniform 512..{args.serve_max_side}, profiles as the mixed-shot sample, "
+                      f"steps x {args.batch_step_scale}; offered load 0.8 x the batched capacity",
+           "rate_req_per_s": rate, "shots_per_s": n_shots / t_batch, "latency_s": pct(lat_b),
+           "plain_shots_per_s": n_shots / t_plain, "plain_latency_s": pct(lat_p), "kernel": kernel,
+           "note": "latency = completion of a request's last shot - its arrival; plain = requests one at a "
+                   "time through the single-shot ABI"}
+
+
 def cpu_baseline(prob, seconds: float, threads: int | None = None) -> dict:
     """FP32 oracle restatement on the host cores, bounded to ~`seconds`."""
     import oracle as O
@@ -297,6 +461,13 @@ def run_ours(args, world, rank, local, dist) -> None:
     cpu = None
     if rank == 0 and world == 1 and args.cpu_seconds > 0:
         cpu = cpu_baseline(prob, args.cpu_seconds)
+    del shot
+    batched = serving = None
+    if args.batch_shots > 0:
+        barrier(dist)
+        batched, capacity = run_batched(args, local)
+        if args.serve_requests > 0:
+            serving = run_serving(args, local, capacity)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -307,7 +478,7 @@ def run_ours(args, world, rank, local, dist) -> None:
                              "peak_source": peak_src, "kernel": kernel,
                              "algorithmic_bytes_per_launch": BYTES_PER_CELL * cells},
                 "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk,
-                "finite": ok}
+                "finite": ok, "batched": batched, "serving": serving}
         print(json.dumps(line), flush=True)
 
 
@@ -322,6 +493,11 @@ def main() -> None:
     ap.add_argument("--e2e-runs", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--size", type=int, default=8192, help="grid side (8192 = the production shot)")
+    ap.add_argument("--batch-shots", type=int, default=64, help="mixed-shot sample size (0: skip batched/serving)")
+    ap.add_argument("--batch-step-scale", type=float, default=0.05,
+                    help="fraction of the 8000..16000 steps each mixed shot runs")
+    ap.add_argument("--serve-requests", type=int, default=6, help="requests in the serving sample (0: skip)")
+    ap.add_argument("--serve-max-side", type=int, default=4096)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -152,6 +152,14 @@ def _lib():
         "fdtd2d_batch_launch_count": (C.c_int64, [vp]),
         "fdtd2d_batch_kernel_name": (C.c_char_p, [vp]),
         "fdtd2d_batch_destroy": (C.c_int, [vp]),
+        "fdtd2d_server_create": (C.c_int, [C.c_int, C.c_int64, C.c_int32, C.POINTER(vp)]),
+        "fdtd2d_server_submit": (C.c_int, [vp, C.POINTER(Setup), C.c_int64]),
+        "fdtd2d_server_step": (C.c_int, [vp]),
+        "fdtd2d_server_pop": (C.c_int, [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                        C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_float), C.c_int64]),
+        "fdtd2d_server_counts": (C.c_int, [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+        "fdtd2d_server_batch": (vp, [vp]),
+        "fdtd2d_server_destroy": (C.c_int, [vp]),
         "fdtd2d_last_cuda_error": (C.c_int, [vp]),
         "fdtd2d_spec_defaults": (None, [C.POINTER(Spec)]),
         "fdtd2d_problem_from_spec": (C.c_int, [C.POINTER(Spec), C.POINTER(vp)]),
@@ -465,6 +473,77 @@ class Batch:
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value:
             _lib().fdtd2d_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Serving loop (fdtd2d_server_*): shots queued as they arrive, admitted in
+    arrival order by device-memory budget, stepped together in blocks of
+    `block_steps`, retired as soon as the GPU has finished them."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0, block_steps: int = 64):
+        h = C.c_void_p()
+        _check(_lib().fdtd2d_server_create(device, budget_bytes, block_steps, C.byref(h)), "fdtd2d_server_create")
+        self._h = h
+        self._held: dict[int, Problem] = {}   # setups must outlive admission
+
+    def submit(self, problem: Problem, tag: int) -> None:
+        _check(_lib().fdtd2d_server_submit(self._h, problem.setup_ptr, tag), "fdtd2d_server_submit")
+        self._held[tag] = problem
+
+    def step(self) -> int:
+        rc = _lib().fdtd2d_server_step(self._h)
+        if rc < 0:
+            raise FdtdError(rc, "fdtd2d_server_step")
+        return rc
+
+    def counts(self) -> tuple[int, int, int]:
+        q, r, f = C.c_int32(), C.c_int32(), C.c_int32()
+        _check(_lib().fdtd2d_server_counts(self._h, C.byref(q), C.byref(r), C.byref(f)), "fdtd2d_server_counts")
+        return q.value, r.value, f.value
+
+    def pop(self) -> dict | None:
+        """Oldest finished shot: {"tag", "dft" (complex per detector), "det_ez"
+        ([n_steps][n_det])}, or None."""
+        tag, nd, ns = C.c_int64(), C.c_int32(), C.c_int32()
+        if not self.counts()[2]:
+            return None
+        # sizes first: peek via the held problem of the oldest finished shot is
+        # not possible, so allocate for the largest held setup
+        md = max((p.setup.n_det for p in self._held.values()), default=0)
+        mt = max((p.setup.n_det * p.setup.n_steps for p in self._held.values()), default=0)
+        dft = np.zeros(2 * max(md, 1), np.float64)
+        tr = np.zeros(max(mt, 1), np.float32)
+        rc = _lib().fdtd2d_server_pop(self._h, C.byref(tag), C.byref(nd), C.byref(ns),
+                                      dft.ctypes.data_as(C.POINTER(C.c_double)), md,
+                                      tr.ctypes.data_as(C.POINTER(C.c_float)), mt)
+        if rc < 0:
+            raise FdtdError(rc, "fdtd2d_server_pop")
+        if rc == 0:
+            return None
+        self._held.pop(tag.value, None)
+        n_det, n_steps = nd.value, ns.value
+        return {"tag": tag.value, "dft": dft[: 2 * n_det:2] + 1j * dft[1: 2 * n_det:2],
+                "det_ez": tr[: n_steps * n_det].reshape(n_steps, n_det).copy()}
+
+    def batch_kernel_name(self) -> str:
+        return _lib().fdtd2d_batch_kernel_name(_lib().fdtd2d_server_batch(self._h)).decode()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            _lib().fdtd2d_server_destroy(self._h)
             self._h = C.c_void_p()
 
     def __enter__(self):

@@ -33,7 +33,10 @@ cudaError_t dalloc(fdtd2d_ctx* c, T** p, size_t count) {
   *p = nullptr;
   if (count == 0) return cudaSuccess;
   void* q = nullptr;
-  cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+  // Stream-ordered allocation from the device's pool: a shot's memory is
+  // released with cudaFreeAsync behind its last kernel, so retiring a batch
+  // member never waits for the device.
+  cudaError_t e = cudaMallocAsync(&q, count * sizeof(T), c->stream);
   if (e != cudaSuccess) return e;
   c->allocs.push_back(q);
   *p = static_cast<T*>(q);
@@ -41,6 +44,20 @@ cudaError_t dalloc(fdtd2d_ctx* c, T** p, size_t count) {
 }
 
 int pitch_for(int nx) { return row_pitch(nx); }
+
+// Keep freed shot memory in this process's pool of the device (default
+// release threshold 0 hands it back at every synchronisation, and the next
+// shot pays to map it again).  A property of this process's pool only.
+void keep_pool_memory(int device) {
+  static bool done[64] = {false};
+  if (device < 0 || device >= 64 || done[device]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  done[device] = true;
+}
 
 __global__ void drive_from_density(float* kp, int64_t pitch, int nx, int ny, float beta) {
   // kp = beta * ne in place over the nx x ny cells; no plasma (ne <= 0) -> 0.
@@ -182,6 +199,7 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
   c->device = device;
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) keep_pool_memory(device);
   if (e != cudaSuccess) {
     rc = fail_cuda(c, e);
     fdtd2d_destroy(c);
@@ -755,9 +773,15 @@ int fdtd2d_check_finite(fdtd2d_ctx* c) {
 int fdtd2d_destroy(fdtd2d_ctx* c) {
   if (!c) return FDTD2D_ERR_INVALID;
   cudaSetDevice(c->device);
-  if (c->stream) cudaStreamSynchronize(c->stream);
-  for (void* p : c->allocs) cudaFree(p);
-  if (c->stream && !c->batch) cudaStreamDestroy(c->stream);
+  // A batch member's memory is freed behind the batch's queued kernels (no
+  // wait); a single shot waits for its stream and releases it.
+  if (c->stream) {
+    for (void* p : c->allocs) cudaFreeAsync(p, c->stream);
+  }
+  if (c->stream && !c->batch) {
+    cudaStreamSynchronize(c->stream);
+    cudaStreamDestroy(c->stream);
+  }
   delete c;
   return FDTD2D_OK;
 }

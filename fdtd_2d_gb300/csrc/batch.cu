@@ -369,9 +369,8 @@ int32_t fdtd2d_batch_shot_step(const fdtd2d_batch* b, int32_t shot) {
 int fdtd2d_batch_remove(fdtd2d_batch* b, int32_t shot) {
   if (!b || shot < 0 || shot >= (int)b->m.size() || !b->m[shot].live) return FDTD2D_ERR_INVALID;
   cudaSetDevice(b->device);
-  cudaStreamSynchronize(b->stream);
   Member& x = b->m[shot];
-  fdtd2d_destroy(x.ctx);
+  fdtd2d_destroy(x.ctx);   // memory released behind the queued kernels
   b->used -= x.bytes;
   x = Member();
   b->dirty = true;
@@ -403,6 +402,215 @@ int fdtd2d_batch_destroy(fdtd2d_batch* b) {
   if (b->d_misc) cudaFree(b->d_misc);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
+  return FDTD2D_OK;
+}
+
+}  // extern "C"
+
+// ---- Serving loop -----------------------------------------------------------
+//
+// A request loop on top of a batch: shots are queued as they arrive, admitted
+// in arrival order while they fit the device-memory budget, stepped together
+// in blocks, and retired as soon as the block that issued their last step has
+// completed on the GPU (a CUDA event per block; no device-wide wait): their
+// DFT accumulators and Ez traces are copied out and their memory is released
+// behind the queued kernels.  The caller drives it with fdtd2d_server_step and
+// collects results with fdtd2d_server_pop.
+
+namespace {
+
+struct Queued {
+  const fdtd2d_setup* s;
+  int64_t tag;
+};
+struct Running {
+  int32_t slot;
+  int64_t tag;
+  int32_t last_g;   // global step that completes the shot
+};
+struct Finished {
+  int64_t tag;
+  int32_t n_det, n_steps;
+  std::vector<double> dft;    // re, im per detector
+  std::vector<float> trace;   // [n_steps][n_det] Ez samples
+};
+
+}  // namespace
+
+struct fdtd2d_server {
+  fdtd2d_batch* b = nullptr;
+  int32_t block = 64;
+  std::vector<Queued> queue;            // FIFO (front = index 0)
+  std::vector<Running> running;
+  std::vector<Finished> finished;       // FIFO
+  std::vector<std::pair<int32_t, cudaEvent_t>> blocks;   // (global step after the block, event)
+  std::vector<cudaEvent_t> spare;
+  int32_t g_complete = 0;               // global steps known complete on the GPU
+};
+
+namespace {
+
+cudaEvent_t take_event(fdtd2d_server* s) {
+  if (!s->spare.empty()) {
+    cudaEvent_t e = s->spare.back();
+    s->spare.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  return e;
+}
+
+// Retire every running shot whose last step has completed.
+int retire(fdtd2d_server* s, int* n_done) {
+  fdtd2d_batch* b = s->b;
+  size_t k = 0;
+  for (; k < s->blocks.size(); ++k) {
+    if (cudaEventQuery(s->blocks[k].second) != cudaSuccess) break;
+    s->g_complete = std::max(s->g_complete, s->blocks[k].first);
+    s->spare.push_back(s->blocks[k].second);
+  }
+  s->blocks.erase(s->blocks.begin(), s->blocks.begin() + k);
+  for (size_t r = 0; r < s->running.size();) {
+    const Running x = s->running[r];
+    if (x.last_g > s->g_complete) {
+      ++r;
+      continue;
+    }
+    fdtd2d_ctx* c = b->m[x.slot].ctx;
+    Finished f;
+    f.tag = x.tag;
+    f.n_det = c->n_det;
+    f.n_steps = c->n_steps;
+    cudaError_t e = cudaSuccess;
+    if (c->dft && c->n_det > 0) {
+      f.dft.resize((size_t)2 * c->n_det);
+      e = cudaMemcpy(f.dft.data(), c->h.dft, f.dft.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    }
+    if (e == cudaSuccess && c->record && c->n_det > 0) {
+      f.trace.resize((size_t)c->n_steps * c->n_det);
+      e = cudaMemcpy(f.trace.data(), c->h.trace, f.trace.size() * sizeof(float), cudaMemcpyDeviceToHost);
+    }
+    if (e != cudaSuccess) return fail(b, e);
+    fdtd2d_batch_remove(b, x.slot);
+    s->finished.push_back(std::move(f));
+    s->running.erase(s->running.begin() + r);
+    ++*n_done;
+  }
+  return FDTD2D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdtd2d_server_create(int device, int64_t hbm_budget_bytes, int32_t block_steps, fdtd2d_server** out) {
+  if (!out || block_steps < 1) return FDTD2D_ERR_INVALID;
+  *out = nullptr;
+  fdtd2d_server* s = new (std::nothrow) fdtd2d_server();
+  if (!s) return FDTD2D_ERR_NOMEM;
+  const int rc = fdtd2d_batch_create(device, hbm_budget_bytes, &s->b);
+  if (rc) {
+    delete s;
+    return rc;
+  }
+  s->block = block_steps;
+  *out = s;
+  return FDTD2D_OK;
+}
+
+int fdtd2d_server_submit(fdtd2d_server* s, const fdtd2d_setup* setup, int64_t tag) {
+  if (!s || !setup) return FDTD2D_ERR_INVALID;
+  if (setup->medium != FDTD2D_MEDIUM_UNIFORM || setup->npml > tma_max_pml() || setup->n_rc > 0 ||
+      setup->line_n > 0)
+    return FDTD2D_ERR_INVALID;
+  const int64_t bytes = fdtd2d_device_bytes(setup);
+  if (bytes < 0) return FDTD2D_ERR_INVALID;
+  if (bytes > s->b->budget) return FDTD2D_ERR_BUDGET;   // could never be admitted
+  s->queue.push_back({setup, tag});
+  return FDTD2D_OK;
+}
+
+int fdtd2d_server_step(fdtd2d_server* s) {
+  if (!s) return FDTD2D_ERR_INVALID;
+  fdtd2d_batch* b = s->b;
+  cudaSetDevice(b->device);
+  int n_done = 0;
+  // 1. admit in arrival order while the head fits (uploads overlap the queued steps)
+  size_t q = 0;
+  for (; q < s->queue.size(); ++q) {
+    int32_t slot = -1;
+    const int rc = fdtd2d_batch_add(b, s->queue[q].s, &slot);
+    if (rc == FDTD2D_ERR_BUDGET) break;
+    if (rc) return rc;
+    const fdtd2d_ctx* c = b->m[slot].ctx;
+    s->running.push_back({slot, s->queue[q].tag, b->m[slot].base + c->n_steps});
+  }
+  s->queue.erase(s->queue.begin(), s->queue.begin() + q);
+  // 2. retire what the GPU has finished
+  int rc = retire(s, &n_done);
+  if (rc) return rc;
+  // 3. issue one block while any shot has steps left
+  bool steps_left = false;
+  for (const Running& x : s->running) steps_left = steps_left || x.last_g > b->g;
+  if (steps_left) {
+    rc = fdtd2d_batch_run(b, s->block);
+    if (rc) return rc;
+    cudaEvent_t e = take_event(s);
+    const cudaError_t ce = cudaEventRecord(e, b->stream);
+    if (ce != cudaSuccess) return fail(b, ce);
+    s->blocks.push_back({b->g, e});
+    // keep at most two blocks ahead of the GPU
+    while (s->blocks.size() > 2) {
+      const cudaError_t we = cudaEventSynchronize(s->blocks.front().second);
+      if (we != cudaSuccess) return fail(b, we);
+      rc = retire(s, &n_done);
+      if (rc) return rc;
+    }
+  } else if (!s->blocks.empty()) {
+    // nothing more to issue: wait for the oldest block instead of spinning
+    const cudaError_t we = cudaEventSynchronize(s->blocks.front().second);
+    if (we != cudaSuccess) return fail(b, we);
+    rc = retire(s, &n_done);
+    if (rc) return rc;
+  }
+  int err = 0;
+  if (cudaMemcpy(&err, b->d_misc + kErr, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && err)
+    return FDTD2D_ERR_TIMEOUT;
+  return n_done;
+}
+
+int fdtd2d_server_pop(fdtd2d_server* s, int64_t* tag, int32_t* n_det, int32_t* n_steps, double* dft,
+                      int32_t max_det, float* trace, int64_t max_trace) {
+  if (!s) return FDTD2D_ERR_INVALID;
+  if (s->finished.empty()) return 0;
+  Finished& f = s->finished.front();
+  if (tag) *tag = f.tag;
+  if (n_det) *n_det = f.n_det;
+  if (n_steps) *n_steps = f.n_steps;
+  if (dft && !f.dft.empty()) std::memcpy(dft, f.dft.data(), std::min<size_t>(f.dft.size(), 2 * (size_t)max_det) * 8);
+  if (trace && !f.trace.empty())
+    std::memcpy(trace, f.trace.data(), std::min<size_t>(f.trace.size(), (size_t)std::max<int64_t>(0, max_trace)) * 4);
+  s->finished.erase(s->finished.begin());
+  return 1;
+}
+
+int fdtd2d_server_counts(const fdtd2d_server* s, int32_t* queued, int32_t* running, int32_t* finished) {
+  if (!s) return FDTD2D_ERR_INVALID;
+  if (queued) *queued = (int32_t)s->queue.size();
+  if (running) *running = (int32_t)s->running.size();
+  if (finished) *finished = (int32_t)s->finished.size();
+  return FDTD2D_OK;
+}
+
+fdtd2d_batch* fdtd2d_server_batch(fdtd2d_server* s) { return s ? s->b : nullptr; }
+
+int fdtd2d_server_destroy(fdtd2d_server* s) {
+  if (!s) return FDTD2D_ERR_INVALID;
+  if (s->b) fdtd2d_batch_destroy(s->b);
+  for (auto& x : s->blocks) cudaEventDestroy(x.second);
+  for (cudaEvent_t e : s->spare) cudaEventDestroy(e);
+  delete s;
   return FDTD2D_OK;
 }
 

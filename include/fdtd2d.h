@@ -249,6 +249,31 @@ int64_t fdtd2d_batch_launch_count(const fdtd2d_batch *b);
 const char *fdtd2d_batch_kernel_name(const fdtd2d_batch *b);
 int fdtd2d_batch_destroy(fdtd2d_batch *b);
 
+/* ---- Serving loop (no counterpart in the reference): shots are queued as they
+   arrive, admitted in arrival order while they fit the budget, stepped together
+   in blocks of block_steps launches, and retired as soon as the GPU has
+   finished them (their DFT and Ez traces copied out, their memory released
+   behind the queued kernels). ---- */
+typedef struct fdtd2d_server fdtd2d_server;
+
+int fdtd2d_server_create(int device, int64_t hbm_budget_bytes, int32_t block_steps, fdtd2d_server **out);
+/* Queue a shot under the caller's tag.  The setup and the arrays it points to
+   must stay valid until the shot is admitted (a later fdtd2d_server_step).
+   FDTD2D_ERR_BUDGET if it could never fit the budget. */
+int fdtd2d_server_submit(fdtd2d_server *s, const fdtd2d_setup *setup, int64_t tag);
+/* One scheduling round: admit, retire finished shots, issue one block (at most
+   two blocks run ahead of the GPU).  Returns the number of shots finished in
+   this round (>= 0) or a negative status. */
+int fdtd2d_server_step(fdtd2d_server *s);
+/* Pop the oldest finished shot: returns 1 (0 if none); its tag, detector count,
+   step count, DFT (re, im per detector, up to max_det) and Ez traces
+   ([n_steps][n_det], up to max_trace floats) into caller buffers (may be null). */
+int fdtd2d_server_pop(fdtd2d_server *s, int64_t *tag, int32_t *n_det, int32_t *n_steps, double *dft,
+                      int32_t max_det, float *trace, int64_t max_trace);
+int fdtd2d_server_counts(const fdtd2d_server *s, int32_t *queued, int32_t *running, int32_t *finished);
+fdtd2d_batch *fdtd2d_server_batch(fdtd2d_server *s);
+int fdtd2d_server_destroy(fdtd2d_server *s);
+
 /* Number of CUDA devices visible to this process (0 when none). */
 int fdtd2d_device_count(void);
 

@@ -140,3 +140,31 @@ def test_budget_admission_and_state(gpu):
         b.synchronize()
         b.remove(i)
         assert b.add(p1) is not None                # room after the removal
+
+
+def test_serving_results_equal_alone(gpu):
+    """Serving loop: requests arrive while others are on the GPU (submitted
+    between scheduling rounds), a budget that holds only part of them forces
+    queueing; every shot's DFT and Ez traces equal its solo run bitwise."""
+    probs = problems(6)
+    solo = []
+    for p in probs:
+        with F.Shot(p, gpu) as s:
+            s.run(1, p.n_steps)
+            solo.append((s.dft(), s.traces()["det_ez"]))
+    budget = sum(sorted(p.device_bytes() for p in probs)[-3:])   # about three at a time
+    got = {}
+    with F.Server(gpu, budget_bytes=budget, block_steps=24) as srv:
+        arrivals = {0: [0, 1], 2: [2], 5: [3, 4], 9: [5]}   # round -> shots arriving
+        rnd = 0
+        while len(got) < len(probs):
+            for k in arrivals.get(rnd, []):
+                srv.submit(probs[k], k)
+            srv.step()
+            while (r := srv.pop()) is not None:
+                got[r["tag"]] = r
+            rnd += 1
+            assert rnd < 10000
+    for k, (dft, tr) in enumerate(solo):
+        assert np.array_equal(got[k]["dft"], dft), k
+        assert np.array_equal(got[k]["det_ez"], tr), k
