@@ -175,13 +175,13 @@ def workload_config(args) -> dict:
             "parallelism": f"replicas x{args.gpus}"}
 
 
-def make_problem(n_steps: int, size: int):
+def make_problem(n_steps: int, size: int, storage: int = 0):
     import fdtd_2d_gb300 as F
 
     kw = {}
     if size != 8192:
         kw = dict(nx=size, ny=size, x_center=size * 5000 / 8192, src_j=size // 2 - 37, det_j=size // 2 - 37)
-    return F.Problem.from_spec(F.production_spec(n_steps=n_steps, **kw))
+    return F.Problem.from_spec(F.production_spec(n_steps=n_steps, storage=storage, **kw))
 
 
 C0 = 299792458.0
@@ -346,6 +346,70 @@ def run_serving(args, local: int, capacity: float) -> dict:
                    "time through the single-shot ABI"}
 
 
+def run_precision(args, local: int) -> dict:
+    """Reduced field storage on the production shot: F16 (per-array 2^k
+    scales) and BF16 storage, FP32 arithmetic, FP64 DFT.  Throughput is
+    device-timed like `value`; errors are against the FP32 GPU run of the same
+    shot after --prec-steps steps, and against the FP64 oracle on a small
+    shot of the same physics (384 x 320, 8 elements, 1500 steps)."""
+    import fdtd_2d_gb300 as F
+    import oracle as O
+
+    def phase_err(a, b):
+        return float(np.max(np.abs(np.angle(a * np.conj(b)))))
+
+    def rel(a, b):
+        return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-300))
+
+    out = {}
+    S, K, W = args.block, max(3, args.steps // 3), args.warmup
+    n_err = args.prec_steps
+    ref32 = None
+    for name, store in (("f32", F.STORE_F32), ("f16", F.STORE_F16), ("bf16", F.STORE_BF16)):
+        prob = make_problem(max(20000, (W + K) * S, n_err), args.size, storage=store)
+        cells = prob.nx * prob.ny
+        with F.Shot(prob, local) as shot:
+            shot.run(1, n_err)
+            ez = shot.read_field("ez").astype(np.float64)
+            tr = shot.traces(1, n_err)["det_ez"].astype(np.float64)
+            dft = shot.dft()
+            entry = {"kernel": shot.kernel_name()}
+            if store != F.STORE_F32:
+                ms = shot.run_timed(n_err + 1, n_err + K * S)
+                bpc = 18
+                val = cells * K * S / (ms / 1e3) / 1e9
+                entry.update({"value": val, "unit": UNIT, "bytes_per_cell_update": bpc,
+                              "achieved_gbs": bpc * val, "ok_finite": shot.check_finite()})
+        if store == F.STORE_F32:
+            ref32 = (ez, tr, dft)
+            continue
+        entry.update({"ez_rel_l2_vs_f32": rel(ez, ref32[0]), "trace_rel_l2_vs_f32": rel(tr, ref32[1]),
+                      "dft_phase_err_vs_f32_rad": phase_err(dft, ref32[2]), "steps_compared": n_err})
+        out[name] = entry
+    # against the FP64 oracle on a small shot of the same physics
+    small = dict(nx=384, ny=320, npml=16, n_steps=1500, dx=0.25e-3, dy=0.25e-3, courant=0.99, profile=3,
+                 ne_peak=3e19, x_center=250, width=40, grf_rms=0.05, grf_corr=10, seed=7, nu=2e9, n_elem=8,
+                 src_i=40, src_j=140, src_dj=5, src_di=0, freq=50e9, steer_deg=15, pulse=1, pulse_width=0.2e-9,
+                 n_det=8, det_i=40, det_j=140, det_dj=5, det_di=0, dft_freq=50e9)
+    p64 = F.Problem.from_spec(**small)
+    o = O.Oracle(p64.setup_ptr)
+    o.run(1, small["n_steps"])
+    o_f = {w: o.read_field(F.FIELD_NAMES[w]) for w in ("ez", "hx", "hy", "jz")}
+    o_tr = o.traces(1, small["n_steps"])["det_ez"]
+    o_dft = o.dft()
+    for name, store in (("f32", F.STORE_F32), ("f16", F.STORE_F16), ("bf16", F.STORE_BF16)):
+        p = F.Problem.from_spec(**small, storage=store)
+        with F.Shot(p, local) as shot:
+            shot.run(1, small["n_steps"])
+            e = {w: rel(shot.read_field(w), o_f[w]) for w in o_f}
+            res = {"field_rel_l2": e, "trace_rel_l2": rel(shot.traces()["det_ez"], o_tr),
+                   "dft_phase_err_rad": phase_err(shot.dft(), o_dft)}
+        out.setdefault(name, {})["vs_fp64_oracle_384x320_1500_steps"] = res
+    out["note"] = ("F16: Ez, Hx, Hy, Jz and the drive map stored as FP16 with a power-of-two scale per array; "
+                   "BF16 the same without scales; 18 B per cell-update (FP32: 36); arithmetic FP32, DFT FP64")
+    return out
+
+
 def cpu_baseline(prob, seconds: float, threads: int | None = None) -> dict:
     """FP32 oracle restatement on the host cores, bounded to ~`seconds`."""
     import oracle as O
@@ -462,7 +526,9 @@ def run_ours(args, world, rank, local, dist) -> None:
     if rank == 0 and world == 1 and args.cpu_seconds > 0:
         cpu = cpu_baseline(prob, args.cpu_seconds)
     del shot
-    batched = serving = None
+    batched = serving = precision = None
+    if args.prec_steps > 0 and world == 1:
+        precision = run_precision(args, local)
     if args.batch_shots > 0:
         barrier(dist)
         batched, capacity = run_batched(args, local)
@@ -478,7 +544,7 @@ def run_ours(args, world, rank, local, dist) -> None:
                              "peak_source": peak_src, "kernel": kernel,
                              "algorithmic_bytes_per_launch": BYTES_PER_CELL * cells},
                 "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk,
-                "finite": ok, "batched": batched, "serving": serving}
+                "finite": ok, "precision": precision, "batched": batched, "serving": serving}
         print(json.dumps(line), flush=True)
 
 
@@ -498,6 +564,8 @@ def main() -> None:
                     help="fraction of the 8000..16000 steps each mixed shot runs")
     ap.add_argument("--serve-requests", type=int, default=6, help="requests in the serving sample (0: skip)")
     ap.add_argument("--serve-max-side", type=int, default=4096)
+    ap.add_argument("--prec-steps", type=int, default=2000,
+                    help="steps of the F16/BF16 vs FP32 comparison on the production shot (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

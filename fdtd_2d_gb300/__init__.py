@@ -85,7 +85,7 @@ class Setup(C.Structure):
         ("rc_level", C.c_float), ("rc_edge0", C.c_float),
         ("line_n", C.c_int32), ("line_i0", C.c_int32), ("line_j", C.c_int32),
         ("line_first", C.c_int32), ("line_last", C.c_int32),
-        ("cover", C.c_int64 * 8),
+        ("cover", C.c_int64 * 8), ("field_max", C.c_double),
     ]
 
 
@@ -106,6 +106,7 @@ class Spec(C.Structure):
         ("n_det", C.c_int32), ("det_i", C.c_int32), ("det_j", C.c_int32),
         ("det_di", C.c_int32), ("det_dj", C.c_int32),
         ("record_traces", C.c_int32), ("dft_freq", C.c_double), ("storage", C.c_int32),
+        ("field_max", C.c_double),
     ]
 
 

@@ -6,6 +6,9 @@
 #include "../../include/fdtd2d.h"
 #include "internal.h"
 
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -44,6 +47,41 @@ cudaError_t dalloc(fdtd2d_ctx* c, T** p, size_t count) {
 }
 
 int pitch_for(int nx) { return row_pitch(nx); }
+
+// Power-of-two scale for an array whose values reach about `m`: stored
+// values then reach about 2^14, with 4x headroom below the FP16 maximum.
+void pow2_scale(double m, float* sc, float* isc) {
+  int k = 0;
+  if (m > 0 && std::isfinite(m)) k = std::max(-100, std::min(100, (int)std::ceil(std::log2(m)) - 14));
+  *sc = std::ldexp(1.f, k);
+  *isc = std::ldexp(1.f, -k);
+}
+
+// Per-array scales for F16 storage (BF16 keeps FP32's exponent range: 1).
+// Peaks: |Ez| from field_max, or 16 x (array elements) x (source amplitude)
+// / max(2 pi f0 dt, 1e-3) (a soft source adds its sample every step, about
+// 1/(2 pi f dt) steps per radian); |H| ~ |Ez|/eta0 x 4; |Jz| from the Drude
+// update's steady response kp |Ez| / |1 - ja e^{-i w dt}| x 2; the drive map
+// from its exact maximum.
+void set_storage_scales(const fdtd2d_setup* s, double beta, DevShot* h) {
+  if (h->store != FDTD2D_STORE_F16) return;
+  double env = 0;
+  for (int n = 0; n <= s->n_steps; ++n) env = std::max(env, (double)std::fabs(s->envelope[n]));
+  const double wdt = 2 * kPi * std::max(s->f0, s->f1) * s->dt;
+  double em = s->field_max;
+  if (em <= 0) em = 16.0 * std::max(1, s->n_src) * std::fabs(s->src_scale) * env / std::max(wdt, 1e-3);
+  double kmax = 0;
+  if (s->ne)
+    for (int64_t t = 0; t < (int64_t)s->nx * s->ny; ++t) kmax = std::max(kmax, beta * (double)s->ne[t]);
+  const double ja = h->ja;
+  const double jm = em * kmax / std::max(std::sqrt((1 - ja) * (1 - ja) + wdt * wdt), 1e-3) * 2;
+  const double eta0 = 376.730313668;
+  pow2_scale(em, &h->sc[0], &h->isc[0]);
+  pow2_scale(em / eta0 * 4, &h->sc[1], &h->isc[1]);
+  pow2_scale(em / eta0 * 4, &h->sc[2], &h->isc[2]);
+  pow2_scale(jm, &h->sc[3], &h->isc[3]);
+  pow2_scale(kmax, &h->sc[4], &h->isc[4]);
+}
 
 // Keep freed shot memory in this process's pool of the device (default
 // release threshold 0 hands it back at every synchronisation, and the next
@@ -88,7 +126,10 @@ int validate(const fdtd2d_setup* s) {
   } else if (s->medium != FDTD2D_MEDIUM_UNIFORM) {
     return FDTD2D_ERR_INVALID;
   }
-  if (s->storage != FDTD2D_STORE_F32) return FDTD2D_ERR_INVALID;  // reduced storage: batch API
+  if (s->storage < FDTD2D_STORE_F32 || s->storage > FDTD2D_STORE_BF16) return FDTD2D_ERR_INVALID;
+  // reduced storage runs on the shared-memory staged kernel only
+  if (s->storage != FDTD2D_STORE_F32 && (s->medium != FDTD2D_MEDIUM_UNIFORM || s->npml > tma_max_pml()))
+    return FDTD2D_ERR_INVALID;
   auto interior = [&](const fdtd2d_point& p) {
     return p.i >= 1 && p.i <= s->nx - 2 && p.j >= 1 && p.j <= s->ny - 2;
   };
@@ -161,8 +202,9 @@ int64_t fdtd2d_device_bytes(const fdtd2d_setup* s) {
   const int64_t pitch = pitch_for(s->nx);
   const int64_t cells = buffer_floats(s->nx, s->ny);
   const int64_t P = s->npml;
-  int64_t b = cells * 4 * 8;                                       // 4 fields x 2
-  b += (s->medium == FDTD2D_MEDIUM_UNIFORM) ? (s->ne ? cells * 4 : 0) : cells * 3;
+  const int64_t es = (s->storage == FDTD2D_STORE_F16 || s->storage == FDTD2D_STORE_BF16) ? 2 : 4;
+  int64_t b = cells * es * 8;                                      // 4 fields x 2
+  b += (s->medium == FDTD2D_MEDIUM_UNIFORM) ? (s->ne ? cells * es : 0) : cells * 3;
   b += 2 * 4 * (2 * (P - 1) * pitch + 2 * P * pitch + 2 * s->ny * P * 2);
   b += 4 * (int64_t)s->n_steps * (s->record_traces ? (s->n_det + 3 * s->n_comp) : 0);
   b += 4 * (int64_t)(s->n_steps + 1) + 16 * (int64_t)s->n_det + (1 << 20);
@@ -231,7 +273,10 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
   } while (0)
 
   h.cells = cells;
-  CK(dalloc(c, &h.fld, (size_t)cells * 8));
+  h.store = s->storage;
+  for (int a = 0; a < 5; ++a) h.sc[a] = h.isc[a] = 1.f;
+  const int es = store_bytes(h.store);
+  CK(dalloc(c, &h.fld, (size_t)cells * 8 * es / 4));
   h.o_ezy = (int64_t)2 * (P - 1) * pitch;
   h.o_hyx = h.o_ezy + (int64_t)2 * P * pitch;
   h.o_ezx = h.o_hyx + (int64_t)2 * ny * P;
@@ -243,16 +288,31 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
   // medium
   if (s->medium == FDTD2D_MEDIUM_UNIFORM) {
     h.ca = s->ca; h.cb = s->cb; h.da = s->da; h.db = s->db;
+    if (h.store != FDTD2D_STORE_F32) set_storage_scales(s, beta, &h);
     if (s->ne) {
       float* kp_buf = nullptr;
-      CK(dalloc(c, &kp_buf, cells));
+      if (h.store == FDTD2D_STORE_F32) {
+        CK(dalloc(c, &kp_buf, cells));
+      } else {
+        CK(cudaMallocAsync(&kp_buf, (size_t)cells * sizeof(float), c->stream));   // FP32 staging
+        CK(cudaMemsetAsync(kp_buf, 0, (size_t)cells * sizeof(float), c->stream));
+      }
       float* kp = kp_buf + kMargin;
       CK(cudaMemcpy2DAsync(kp, pitch * sizeof(float), s->ne, nx * sizeof(float), nx * sizeof(float),
                            ny, cudaMemcpyHostToDevice, c->stream));
       drive_from_density<<<1024, 256, 0, c->stream>>>(kp, pitch, nx, ny, (float)beta);
       ++c->launches;
       CK(cudaGetLastError());
-      h.kp = kp;
+      if (h.store == FDTD2D_STORE_F32) {
+        h.kp = kp;
+      } else {
+        uint16_t* kp16 = nullptr;
+        CK(dalloc(c, &kp16, (size_t)cells));
+        CK(launch_to_storage(kp_buf, kp16, cells, h.store, h.isc[4], c->stream));
+        ++c->launches;
+        CK(cudaFreeAsync(kp_buf, c->stream));
+        h.kp = reinterpret_cast<const float*>(kp16 + kMargin);   // elements of the storage type
+      }
     }
   } else {
     std::vector<uint8_t> ids((size_t)cells * 3, 0);
@@ -434,7 +494,8 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
   // deeper CPMLs always stream.
   {
     const char* k = std::getenv("FDTD2D_KERNEL");
-    c->tma = (c->medium == FDTD2D_MEDIUM_UNIFORM) && P <= tma_max_pml() && !(k && std::strcmp(k, "stream") == 0);
+    c->tma = (c->medium == FDTD2D_MEDIUM_UNIFORM) && P <= tma_max_pml() &&
+             (h.store != FDTD2D_STORE_F32 || !(k && std::strcmp(k, "stream") == 0));
   }
   CK(dalloc(c, &c->d_err, 1));
   std::vector<int4> units;
@@ -442,11 +503,7 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
     // FDTD2D_TMA="W,ST" picks a compiled launch shape (W warps, ST stages);
     // otherwise the shapes are timed on this shot and the fastest is kept,
     // unless FDTD2D_TMA_AUTOTUNE=0 (then shape 0).
-    int forced = -1;
-    if (const char* t = std::getenv("FDTD2D_TMA")) {
-      int w = 0, st = 0;
-      if (std::sscanf(t, "%d,%d", &w, &st) == 2) forced = tma_shape_find(w, st);
-    }
+    const int forced = tma_shape_parse(std::getenv("FDTD2D_TMA"));
     const char* at = std::getenv("FDTD2D_TMA_AUTOTUNE");
     if (member) {
       // batch members are stepped by the batch's kernel
@@ -466,7 +523,7 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
       float best = 0.f;
       int best_k = 0;
       for (int k = 0; k < tma_shape_count(); ++k) {
-        const int ctas = tma_resident_ctas(k, P, device);
+        const int ctas = tma_resident_ctas(k, P, h.store, device);
         const std::vector<int4> u = make_units(0, nx, ny, ctas, tma_band_cols(k));
         int4* du = nullptr;
         cudaError_t e = cudaMalloc(&du, u.size() * sizeof(int4));
@@ -500,11 +557,9 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
       }
       c->tma_shape = best_k;
     }
-    c->grid_warps = tma_resident_ctas(c->tma_shape, P, device);  // CTAs for this path
+    c->grid_warps = tma_resident_ctas(c->tma_shape, P, h.store, device);  // CTAs for this path
     units = make_units(0, nx, ny, c->grid_warps, tma_band_cols(c->tma_shape));
-    int w = 0, st = 0;
-    tma_shape_dims(c->tma_shape, &w, &st);
-    std::snprintf(c->kernel_name, sizeof c->kernel_name, "step_tma_kernel<%d,%d>", w, st);
+    tma_shape_name(c->tma_shape, "step_tma_kernel", c->kernel_name, sizeof c->kernel_name);
   } else {
     c->grid_warps = resident_warps(c->medium, device);
     units = make_units(0, nx, ny, c->grid_warps);
@@ -722,10 +777,86 @@ bool field_view(fdtd2d_ctx* c, int which, int buf, FieldView* v) {
   }
 }
 
+// The four physical fields in 16-bit storage: rows of the reference layout,
+// converted with the array's scale on the host.
+struct View16 {
+  const uint16_t* base;  // device, column 0 of row 0 of buffer b
+  int rows, cols;
+  float sc, isc;
+};
+
+bool view16(fdtd2d_ctx* c, int which, int b, View16* v) {
+  const DevShot& h = c->h;
+  const int nx = c->nx, ny = c->ny;
+  int f = -1, rows = ny, cols = nx;
+  switch (which) {
+    case FDTD2D_FIELD_EZ: f = kEz; break;
+    case FDTD2D_FIELD_JZ: f = kJz; break;
+    case FDTD2D_FIELD_HX: f = kHx; rows = ny - 1; break;
+    case FDTD2D_FIELD_HY: f = kHy; cols = nx - 1; break;
+    default: return false;
+  }
+  *v = {field_ptr_t<uint16_t>(h, f, b), rows, cols, h.sc[f], h.isc[f]};
+  return true;
+}
+
+float from16(uint16_t u, int store) {
+  if (store == FDTD2D_STORE_F16) {
+    __half x;
+    std::memcpy(&x, &u, 2);
+    return __half2float(x);
+  }
+  __nv_bfloat16 x;
+  std::memcpy(&x, &u, 2);
+  return __bfloat162float(x);
+}
+
+uint16_t to16(float f, int store) {
+  uint16_t u;
+  if (store == FDTD2D_STORE_F16) {
+    const __half x = __float2half_rn(f);
+    std::memcpy(&u, &x, 2);
+  } else {
+    const __nv_bfloat16 x = __float2bfloat16_rn(f);
+    std::memcpy(&u, &x, 2);
+  }
+  return u;
+}
+
+int read_field16(fdtd2d_ctx* c, int which, float* host) {
+  View16 v;
+  if (!view16(c, which, c->step & 1, &v)) return FDTD2D_ERR_INVALID;
+  cudaSetDevice(c->device);
+  std::vector<uint16_t> buf((size_t)v.rows * v.cols);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2D(buf.data(), (size_t)v.cols * 2, v.base, (size_t)c->pitch * 2, (size_t)v.cols * 2, v.rows,
+                     cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  for (size_t t = 0; t < buf.size(); ++t) host[t] = from16(buf[t], c->h.store) * v.sc;
+  return FDTD2D_OK;
+}
+
+int write_field16(fdtd2d_ctx* c, int which, const float* host) {
+  cudaSetDevice(c->device);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+    View16 v;
+    if (!view16(c, which, b, &v)) return FDTD2D_ERR_INVALID;
+    std::vector<uint16_t> buf((size_t)v.rows * v.cols);
+    for (size_t t = 0; t < buf.size(); ++t) buf[t] = to16(host[t] * v.isc, c->h.store);
+    e = cudaMemcpy2D(const_cast<uint16_t*>(v.base), (size_t)c->pitch * 2, buf.data(), (size_t)v.cols * 2,
+                     (size_t)v.cols * 2, v.rows, cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  return FDTD2D_OK;
+}
+
 }  // namespace
 
 int fdtd2d_read_field(fdtd2d_ctx* c, int which, float* host) {
   if (!c || !host) return FDTD2D_ERR_INVALID;
+  if (c->h.store != FDTD2D_STORE_F32 && which <= FDTD2D_FIELD_JZ) return read_field16(c, which, host);
   FieldView v;
   if (!field_view(c, which, c->step & 1, &v)) return FDTD2D_ERR_INVALID;
   cudaSetDevice(c->device);
@@ -739,6 +870,7 @@ int fdtd2d_read_field(fdtd2d_ctx* c, int which, float* host) {
 
 int fdtd2d_write_field(fdtd2d_ctx* c, int which, const float* host) {
   if (!c || !host) return FDTD2D_ERR_INVALID;
+  if (c->h.store != FDTD2D_STORE_F32 && which <= FDTD2D_FIELD_JZ) return write_field16(c, which, host);
   cudaSetDevice(c->device);
   cudaError_t e = cudaStreamSynchronize(c->stream);
   for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
@@ -757,10 +889,12 @@ int fdtd2d_check_finite(fdtd2d_ctx* c) {
   const int b = c->step & 1;
   const int64_t cells = c->h.cells;  // whole buffers, margins included (they stay 0)
   cudaError_t e = cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream);
-  const float* arrs[4] = {field_ptr(c->h, kEz, b) - kMargin, field_ptr(c->h, kHx, b) - kMargin,
-                          field_ptr(c->h, kHy, b) - kMargin, field_ptr(c->h, kJz, b) - kMargin};
   for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
-    e = launch_nonfinite(arrs[k], cells, c->d_flag, c->stream);
+    if (c->h.store == FDTD2D_STORE_F32)
+      e = launch_nonfinite(field_ptr(c->h, k, b) - kMargin, cells, c->d_flag, c->stream);
+    else
+      e = launch_nonfinite16(field_ptr_t<uint16_t>(c->h, k, b) - kMargin, cells,
+                             c->h.store == FDTD2D_STORE_BF16, c->d_flag, c->stream);
     ++c->launches;
   }
   int flag = 0;

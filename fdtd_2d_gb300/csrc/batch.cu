@@ -246,7 +246,8 @@ int fdtd2d_batch_create(int device, int64_t hbm_budget_bytes, fdtd2d_batch** out
 int fdtd2d_batch_add(fdtd2d_batch* b, const fdtd2d_setup* s, int32_t* shot) {
   if (!b || !s || !shot) return FDTD2D_ERR_INVALID;
   *shot = -1;
-  if (s->medium != FDTD2D_MEDIUM_UNIFORM || s->npml > tma_max_pml() || s->n_rc > 0 || s->line_n > 0)
+  if (s->medium != FDTD2D_MEDIUM_UNIFORM || s->npml > tma_max_pml() || s->n_rc > 0 || s->line_n > 0 ||
+      s->storage != FDTD2D_STORE_F32)
     return FDTD2D_ERR_INVALID;
   const int64_t bytes = fdtd2d_device_bytes(s);
   if (bytes < 0) return FDTD2D_ERR_INVALID;
@@ -293,10 +294,9 @@ int fdtd2d_batch_run(fdtd2d_batch* b, int32_t n_steps) {
     for (const Member& x : b->m) any = any || (x.live && !x.done);
     if (!any) return FDTD2D_OK;
     if (!b->tuned) {
-      const char* t = std::getenv("FDTD2D_TMA");
-      int w = 0, st = 0;
-      if (t && std::sscanf(t, "%d,%d", &w, &st) == 2 && tma_shape_find(w, st) >= 0) {
-        b->shape = tma_shape_find(w, st);
+      const int forced = tma_shape_parse(std::getenv("FDTD2D_TMA"));
+      if (forced >= 0) {
+        b->shape = forced;
         b->tuned = true;
       } else {
         const int rc = autotune(b);
@@ -522,7 +522,7 @@ int fdtd2d_server_create(int device, int64_t hbm_budget_bytes, int32_t block_ste
 int fdtd2d_server_submit(fdtd2d_server* s, const fdtd2d_setup* setup, int64_t tag) {
   if (!s || !setup) return FDTD2D_ERR_INVALID;
   if (setup->medium != FDTD2D_MEDIUM_UNIFORM || setup->npml > tma_max_pml() || setup->n_rc > 0 ||
-      setup->line_n > 0)
+      setup->line_n > 0 || setup->storage != FDTD2D_STORE_F32)
     return FDTD2D_ERR_INVALID;
   const int64_t bytes = fdtd2d_device_bytes(setup);
   if (bytes < 0) return FDTD2D_ERR_INVALID;

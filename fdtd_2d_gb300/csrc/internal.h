@@ -79,6 +79,12 @@ struct DevShot {
   // Reference launch coverage per update kernel (material medium only):
   // a cell update with reference thread index l >= cov[k] is skipped.
   long long cov[8];
+  // Field storage (FDTD2D_STORE_*): Ez, Hx, Hy, Jz and the drive map hold
+  // F32, F16 or BF16 elements (fld and kp point at elements of that type);
+  // stored = value * isc[a], value = stored * sc[a], sc a power of two per
+  // array a in (Ez, Hx, Hy, Jz, drive).  Arithmetic is FP32 throughout.
+  int store;
+  float sc[5], isc[5];
 };
 
 enum FieldId : int { kEz = 0, kHx = 1, kHy = 2, kJz = 3 };
@@ -89,6 +95,15 @@ constexpr int kMargin = 32;
 __host__ __device__ inline float* field_ptr(const DevShot& S, int f, int b) {
   return S.fld + (int64_t)(2 * f + b) * S.cells + kMargin;
 }
+
+// The same for storage element type T (F32 storage: T = float).
+template <class T>
+__host__ __device__ inline T* field_ptr_t(const DevShot& S, int f, int b) {
+  return reinterpret_cast<T*>(S.fld) + (int64_t)(2 * f + b) * S.cells + kMargin;
+}
+
+// Bytes per stored field element.
+inline int store_bytes(int store) { return store == 0 ? 4 : 2; }
 
 // Row pitch (floats) for nx columns: 128-byte rows with kMargin on each side.
 inline int row_pitch(int nx) { return (nx + 31) / 32 * 32 + 2 * kMargin; }
@@ -120,9 +135,14 @@ enum DeviceError : int { kErrNone = 0, kErrWaitTimeout = 1 };
 int tma_shape_count();
 int tma_shape_find(int warps, int stages);   // -1 if not compiled
 void tma_shape_dims(int shape, int* warps, int* stages);
+// "W,ST" -> shape index, -1 if not compiled
+int tma_shape_parse(const char* text);
+// "<kernel><W,ST>"
+void tma_shape_name(int shape, const char* kernel, char* out, size_t n);
 int tma_band_cols(int shape);
 int tma_max_pml();   // largest CPML depth the staged kernel takes
-int tma_resident_ctas(int shape, int npml, int device);
+int tma_resident_ctas(int shape, int npml, int store, int device);
+// Launches the instantiation for shot.store.
 cudaError_t launch_step_tma(int shape, const DevShot& shot, const int4* units, int n_units, int n_global,
                             int max_ctas, int* err, cudaStream_t stream);
 // Batched form: one launch advances every shot in `shots` by one step, units
@@ -151,5 +171,8 @@ cudaError_t launch_line(const float* ez, int64_t pitch, int j, int i0, int n, fl
 
 // Count non-finite values in n floats (atomic count into *flag).
 cudaError_t launch_nonfinite(const float* a, int64_t n, int* flag, cudaStream_t stream);
+cudaError_t launch_nonfinite16(const uint16_t* a, int64_t n, bool bf16, int* flag, cudaStream_t stream);
+// n FP32 values to F16 (store 1) or BF16 (store 2) elements, times isc.
+cudaError_t launch_to_storage(const float* src, void* dst, int64_t n, int store, float isc, cudaStream_t stream);
 
 }  // namespace fdtd2d

@@ -314,6 +314,7 @@ int fdtd2d_problem_from_spec(const fdtd2d_spec* sp, fdtd2d_problem** out) {
   p.s.record_traces = sp->record_traces;
   p.s.dft_freq = sp->dft_freq > 0 ? sp->dft_freq : sp->freq;
   p.s.storage = sp->storage;
+  p.s.field_max = sp->field_max;
   p.bind();
   *out = pr;
   return FDTD2D_OK;

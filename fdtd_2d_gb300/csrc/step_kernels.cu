@@ -20,6 +20,9 @@
 // (__fmaf_rn, __fmul_rn, ...), so the owner's value and a recomputed copy are
 // bit-identical whatever the surrounding code, and results do not depend on
 // how the grid is cut into units.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include "internal.h"
 #include "step_common.cuh"
 
@@ -412,6 +415,42 @@ __global__ void nonfinite_kernel(const float* __restrict__ a, int64_t n, int* fl
 
 cudaError_t launch_nonfinite(const float* a, int64_t n, int* flag, cudaStream_t stream) {
   nonfinite_kernel<<<1024, 256, 0, stream>>>(a, n, flag);
+  return cudaGetLastError();
+}
+
+// 16-bit storage: an element is Inf/NaN when its exponent bits are all ones
+// (FP16: 0x7C00, BF16: 0x7F80).
+__global__ void nonfinite16_kernel(const uint16_t* __restrict__ a, int64_t n, uint16_t mask, int* flag) {
+  int bad = 0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    bad |= (a[t] & mask) == mask;
+  }
+  bad = __syncthreads_or(bad);
+  if (bad && threadIdx.x == 0) atomicAdd(flag, 1);
+}
+
+cudaError_t launch_nonfinite16(const uint16_t* a, int64_t n, bool bf16, int* flag, cudaStream_t stream) {
+  nonfinite16_kernel<<<1024, 256, 0, stream>>>(a, n, bf16 ? 0x7F80 : 0x7C00, flag);
+  return cudaGetLastError();
+}
+
+// FP32 values to the storage type: dst[t] = src[t] * isc, rounded to nearest.
+__global__ void to_half_kernel(const float* __restrict__ src, __half* __restrict__ dst, int64_t n, float isc) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    dst[t] = __float2half_rn(src[t] * isc);
+}
+__global__ void to_bf16_kernel(const float* __restrict__ src, __nv_bfloat16* __restrict__ dst, int64_t n,
+                               float isc) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    dst[t] = __float2bfloat16_rn(src[t] * isc);
+}
+
+cudaError_t launch_to_storage(const float* src, void* dst, int64_t n, int store, float isc, cudaStream_t stream) {
+  if (store == 1)
+    to_half_kernel<<<1024, 256, 0, stream>>>(src, static_cast<__half*>(dst), n, isc);
+  else
+    to_bf16_kernel<<<1024, 256, 0, stream>>>(src, static_cast<__nv_bfloat16*>(dst), n, isc);
   return cudaGetLastError();
 }
 

@@ -15,6 +15,11 @@
 // Every wait is bounded: after kWaitNs (1 s) without progress the kernel records
 // kErrWaitTimeout in the shot's error word, waits (bounded) for the copies it
 // issued, and returns; the host reports FDTD2D_ERR_TIMEOUT.
+#include <cstdio>
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include "internal.h"
 #include "step_common.cuh"
 
@@ -26,27 +31,122 @@ constexpr uint64_t kWaitNs = 1000000000ull;   // 1 s bound on any barrier wait
 constexpr int kXSlot = 128;                    // floats reserved per staged x-strip row
 constexpr int kTmaMaxPml = kXSlot - 8;         // x-strip rows fit their stage slot
 
-// Launch shape: W warps (a band of 128*W columns) and an ST-stage ring.
-template <int W, int ST>
+// Launch shape: W warps (a band of 128*W columns) and an ST-stage ring, for
+// field storage element type T.
+template <int W, int ST, class T>
 struct Cfg {
+  using Elem = T;
   static constexpr int kWarps = W;
   static constexpr int kThreads = W * 32;
   static constexpr int kStages = ST;
   static constexpr int kBand = W * kCols;
-  static constexpr int kSeg = kBand + 8;       // staged floats per array row
-  // A stage holds one row j of the band: Ez(j+1), Hx, Hy, Jz, drive segments;
-  // the psi_Hxy and psi_Ezy rows of the band (CPML y-strip rows only); and the
-  // row's x-strip psi rows (psi_Hyx side 0/1, psi_Ezx side 0/1; bands touching
-  // a strip only), each copied from its 16-byte-aligned start.
-  static constexpr int kPsiOff = 5 * kSeg;
-  static constexpr int kXOff = kPsiOff + 2 * kBand;
-  static constexpr int kStageFloats = kXOff + 4 * kXSlot;
-  static constexpr uint32_t kSegBytes = kSeg * 4;
+  static constexpr int kHalo = 16 / (int)sizeof(T);        // halo elements each side: 16 bytes
+  static constexpr int kSeg = kBand + 2 * kHalo;           // staged elements per array row
+  // A stage holds one row j of the band (byte offsets): Ez(j+1), Hx, Hy, Jz,
+  // drive segments (T); the psi_Hxy and psi_Ezy rows of the band (float; CPML
+  // y-strip rows only); and the row's x-strip psi rows (float; psi_Hyx side
+  // 0/1, psi_Ezx side 0/1; bands touching a strip only), each copied from its
+  // 16-byte-aligned start.
+  static constexpr uint32_t kSegBytes = kSeg * sizeof(T);
+  static constexpr uint32_t kPsiOffB = 5 * kSegBytes;
   static constexpr uint32_t kPsiBytes = kBand * 4;
-  static constexpr size_t kSmem = (size_t)ST * kStageFloats * sizeof(float);
+  static constexpr uint32_t kXOffB = kPsiOffB + 2 * kPsiBytes;
+  static constexpr uint32_t kStageBytes = kXOffB + 4 * kXSlot * 4;
+  static constexpr size_t kSmem = (size_t)ST * kStageBytes;
   static constexpr int kMinBlocks = W <= 4 ? 4 : 2;   // caps registers at 128 per thread
-  static_assert(kPsiOff % 4 == 0 && kXOff % 4 == 0 && kStageFloats % 4 == 0, "16-byte aligned stage slots");
+  static_assert(kSegBytes % 16 == 0 && kPsiOffB % 16 == 0 && kXOffB % 16 == 0 && kStageBytes % 16 == 0,
+                "16-byte aligned stage slots");
 };
+
+// Loads and stores of 4 consecutive stored elements (and of one), converted
+// to / from FP32 with the array's power-of-two scale.
+template <class T>
+struct Sto;
+
+template <>
+struct Sto<float> {
+  __device__ static __forceinline__ void lds4(float (&d)[4], const float* p, float) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+  }
+  __device__ static __forceinline__ void ldg4(float (&d)[4], const float* p, float) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+    d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+  }
+  __device__ static __forceinline__ float ld1(const float* p, float) { return *p; }
+  __device__ static __forceinline__ float ldg1(const float* p, float) { return __ldg(p); }
+  __device__ static __forceinline__ void stcs4(float* p, const float (&d)[4], float) {
+    __stcs(reinterpret_cast<float4*>(p), make_float4(d[0], d[1], d[2], d[3]));
+  }
+};
+
+template <class T, class T2>
+struct Sto16 {
+  __device__ static __forceinline__ float2 to_f2(uint32_t w);
+  __device__ static __forceinline__ uint32_t from_f2(float a, float b);
+};
+
+template <>
+__device__ __forceinline__ float2 Sto16<__half, __half2>::to_f2(uint32_t w) {
+  __half2 h;
+  memcpy(&h, &w, 4);
+  return __half22float2(h);
+}
+template <>
+__device__ __forceinline__ uint32_t Sto16<__half, __half2>::from_f2(float a, float b) {
+  const __half2 h = __floats2half2_rn(a, b);
+  uint32_t w;
+  memcpy(&w, &h, 4);
+  return w;
+}
+template <>
+__device__ __forceinline__ float2 Sto16<__nv_bfloat16, __nv_bfloat162>::to_f2(uint32_t w) {
+  __nv_bfloat162 h;
+  memcpy(&h, &w, 4);
+  return __bfloat1622float2(h);
+}
+template <>
+__device__ __forceinline__ uint32_t Sto16<__nv_bfloat16, __nv_bfloat162>::from_f2(float a, float b) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  uint32_t w;
+  memcpy(&w, &h, 4);
+  return w;
+}
+
+template <class T, class T2>
+struct Sto16Ops {
+  using B = Sto16<T, T2>;
+  __device__ static __forceinline__ void cvt(float (&d)[4], uint2 v, float sc) {
+    const float2 a = B::to_f2(v.x), b = B::to_f2(v.y);
+    d[0] = a.x * sc; d[1] = a.y * sc; d[2] = b.x * sc; d[3] = b.y * sc;
+  }
+  __device__ static __forceinline__ void lds4(float (&d)[4], const T* p, float sc) {
+    cvt(d, *reinterpret_cast<const uint2*>(p), sc);
+  }
+  __device__ static __forceinline__ void ldg4(float (&d)[4], const T* p, float sc) {
+    cvt(d, __ldg(reinterpret_cast<const uint2*>(p)), sc);
+  }
+  __device__ static __forceinline__ float ld1(const T* p, float sc) {
+    uint16_t u;
+    memcpy(&u, p, 2);
+    return B::to_f2((uint32_t)u).x * sc;
+  }
+  __device__ static __forceinline__ float ldg1(const T* p, float sc) {
+    const uint16_t u = __ldg(reinterpret_cast<const unsigned short*>(p));
+    return B::to_f2((uint32_t)u).x * sc;
+  }
+  __device__ static __forceinline__ void stcs4(T* p, const float (&d)[4], float isc) {
+    uint2 v;
+    v.x = B::from_f2(d[0] * isc, d[1] * isc);
+    v.y = B::from_f2(d[2] * isc, d[3] * isc);
+    __stcs(reinterpret_cast<uint2*>(p), v);
+  }
+};
+
+template <>
+struct Sto<__half> : Sto16Ops<__half, __half2> {};
+template <>
+struct Sto<__nv_bfloat16> : Sto16Ops<__nv_bfloat16, __nv_bfloat162> {};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -93,7 +193,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   }
 }
 
-__device__ __forceinline__ void bulk_copy(float* dst, const float* src, uint32_t bytes, uint64_t* bar) {
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
   asm volatile(
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
           smem_u32(dst)),
@@ -101,17 +201,13 @@ __device__ __forceinline__ void bulk_copy(float* dst, const float* src, uint32_t
       : "memory");
 }
 
-__device__ __forceinline__ void lds4(float (&d)[4], const float* p) {
+__device__ __forceinline__ void lds4f(float (&d)[4], const float* p) {
   const float4 v = *reinterpret_cast<const float4*>(p);
   d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
 }
 
-__device__ __forceinline__ void stcs4(float* p, const float (&d)[4]) {
-  __stcs(reinterpret_cast<float4*>(p), make_float4(d[0], d[1], d[2], d[3]));
-}
-
 struct Ring {
-  float* stage;          // kStages * kStageFloats
+  unsigned char* stage;  // kStages * kStageBytes
   uint64_t* full;        // completion of a stage's copies
   uint64_t* empty;       // all warps done reading a stage
   uint32_t issued = 0;   // rows issued into the ring (producer thread only)
@@ -152,8 +248,9 @@ __device__ bool issue_row(Ring& R, const DevShot& S, int par, int c0, int j, boo
   const uint32_t g = R.issued++;
   const int s = g % C::kStages;
   if (g >= (uint32_t)C::kStages && !mbar_wait(&R.empty[s], ((g / C::kStages) - 1) & 1)) return false;
-  const int64_t row = (int64_t)j * S.pitch + c0 - 4;
-  float* dst = R.stage + s * C::kStageFloats;
+  using T = typename C::Elem;
+  const int64_t row = (int64_t)j * S.pitch + c0 - C::kHalo;
+  unsigned char* dst = R.stage + s * C::kStageBytes;
   const int rh = hxy_row(S, j), re = ezy_row(S, j);
   uint32_t xbytes[4] = {0, 0, 0, 0};
   int64_t xa[4] = {0, 0, 0, 0};
@@ -168,16 +265,17 @@ __device__ bool issue_row(Ring& R, const DevShot& S, int par, int c0, int j, boo
   mbar_expect_tx(&R.full[s], C::kSegBytes * (has_kp ? 5 : 4) + (rh >= 0 ? C::kPsiBytes : 0) + (re >= 0 ? C::kPsiBytes : 0) +
                                  xbytes[0] + xbytes[1] + xbytes[2] + xbytes[3]);
   const float* psr = S.psi + par * S.psi_buf;
-  if (rh >= 0) bulk_copy(dst + C::kPsiOff, psr + (int64_t)rh * S.pitch + c0, C::kPsiBytes, &R.full[s]);
-  if (re >= 0) bulk_copy(dst + C::kPsiOff + C::kBand, psr + S.o_ezy + (int64_t)re * S.pitch + c0, C::kPsiBytes, &R.full[s]);
+  if (rh >= 0) bulk_copy(dst + C::kPsiOffB, psr + (int64_t)rh * S.pitch + c0, C::kPsiBytes, &R.full[s]);
+  if (re >= 0)
+    bulk_copy(dst + C::kPsiOffB + C::kPsiBytes, psr + S.o_ezy + (int64_t)re * S.pitch + c0, C::kPsiBytes, &R.full[s]);
 #pragma unroll
   for (int q = 0; q < 4; ++q)
-    if (xbytes[q]) bulk_copy(dst + C::kXOff + q * kXSlot, S.psi + xa[q], xbytes[q], &R.full[s]);
-  bulk_copy(dst + 0 * C::kSeg, field_ptr(S, kEz, par) + row + S.pitch, C::kSegBytes, &R.full[s]);
-  bulk_copy(dst + 1 * C::kSeg, field_ptr(S, kHx, par) + row, C::kSegBytes, &R.full[s]);
-  bulk_copy(dst + 2 * C::kSeg, field_ptr(S, kHy, par) + row, C::kSegBytes, &R.full[s]);
-  bulk_copy(dst + 3 * C::kSeg, field_ptr(S, kJz, par) + row, C::kSegBytes, &R.full[s]);
-  if (has_kp) bulk_copy(dst + 4 * C::kSeg, S.kp + row, C::kSegBytes, &R.full[s]);
+    if (xbytes[q]) bulk_copy(dst + C::kXOffB + q * kXSlot * 4, S.psi + xa[q], xbytes[q], &R.full[s]);
+  bulk_copy(dst + 0 * C::kSegBytes, field_ptr_t<T>(S, kEz, par) + row + S.pitch, C::kSegBytes, &R.full[s]);
+  bulk_copy(dst + 1 * C::kSegBytes, field_ptr_t<T>(S, kHx, par) + row, C::kSegBytes, &R.full[s]);
+  bulk_copy(dst + 2 * C::kSegBytes, field_ptr_t<T>(S, kHy, par) + row, C::kSegBytes, &R.full[s]);
+  bulk_copy(dst + 3 * C::kSegBytes, field_ptr_t<T>(S, kJz, par) + row, C::kSegBytes, &R.full[s]);
+  if (has_kp) bulk_copy(dst + 4 * C::kSegBytes, reinterpret_cast<const T*>(S.kp) + row, C::kSegBytes, &R.full[s]);
   return true;
 }
 
@@ -196,19 +294,23 @@ __device__ void process_band(const DevShot& S, Ring& R, const float* __restrict_
   const int par = (n - 1) & 1;
   const bool has_kp = S.kp != nullptr;
   const int xs = band_x_sides<C::kBand>(S, c0);
-  const float* __restrict__ ezo = field_ptr(S, kEz, par);
-  const float* __restrict__ hxo_p = field_ptr(S, kHx, par);
-  float* __restrict__ ezw = field_ptr(S, kEz, par ^ 1);
-  float* __restrict__ hxw = field_ptr(S, kHx, par ^ 1);
-  float* __restrict__ hyw = field_ptr(S, kHy, par ^ 1);
-  float* __restrict__ jzw = field_ptr(S, kJz, par ^ 1);
+  using T = typename C::Elem;
+  using St = Sto<T>;
+  const T* __restrict__ ezo = field_ptr_t<T>(S, kEz, par);
+  const T* __restrict__ hxo_p = field_ptr_t<T>(S, kHx, par);
+  T* __restrict__ ezw = field_ptr_t<T>(S, kEz, par ^ 1);
+  T* __restrict__ hxw = field_ptr_t<T>(S, kHx, par ^ 1);
+  T* __restrict__ hyw = field_ptr_t<T>(S, kHy, par ^ 1);
+  T* __restrict__ jzw = field_ptr_t<T>(S, kJz, par ^ 1);
   float* __restrict__ psw = S.psi + (par ^ 1) * S.psi_buf;
+  // per-array scales (Ez, Hx, Hy, Jz, drive); 1 for F32 storage
+  const float sE = S.sc[0], sHx = S.sc[1], sHy = S.sc[2], sJ = S.sc[3], sK = S.sc[4];
 
   const int i0 = c0 + warp * kCols;            // this warp's first column
   const int i = i0 + 4 * lane;
   const bool act = i < nx;
   const int ic = act ? i : 0;
-  const int sl = 4 + warp * kCols + 4 * lane;  // lane's float4 in a staged segment
+  const int sl = C::kHalo + warp * kCols + 4 * lane;  // lane's 4 elements in a staged segment
   const int rows = j1 - j0;
   // The producer thread: lane 0 of a warp with no x-strip columns where the
   // band has one (the first band's strip is in warp 0, the last band's in
@@ -242,16 +344,16 @@ __device__ void process_band(const DevShot& S, Ring& R, const float* __restrict_
   float ezc[4], hxp[4];
   zero4(ezc);
   zero4(hxp);
-  if (act) ld4(ezc, ezo + (int64_t)j0 * pitch + ic);
-  float ezl = (lane == 0 && i0 >= 1) ? ezo[(int64_t)j0 * pitch + i0 - 1] : 0.f;  // Ez(i0-1, j)
-  float ezr = (lane == 31 && i0 + kCols < nx) ? ezo[(int64_t)j0 * pitch + i0 + kCols] : 0.f;
+  if (act) St::ldg4(ezc, ezo + (int64_t)j0 * pitch + ic, sE);
+  float ezl = (lane == 0 && i0 >= 1) ? St::ldg1(ezo + (int64_t)j0 * pitch + i0 - 1, sE) : 0.f;  // Ez(i0-1, j)
+  float ezr = (lane == 31 && i0 + kCols < nx) ? St::ldg1(ezo + (int64_t)j0 * pitch + i0 + kCols, sE) : 0.f;
   if (j0 >= 1) {
     float ezp[4], hxo[4];
     zero4(ezp);
     zero4(hxo);
     if (act) {
-      ld4(ezp, ezo + (int64_t)(j0 - 1) * pitch + ic);
-      ld4(hxo, hxo_p + (int64_t)(j0 - 1) * pitch + ic);
+      St::ldg4(ezp, ezo + (int64_t)(j0 - 1) * pitch + ic, sE);
+      St::ldg4(hxo, hxo_p + (int64_t)(j0 - 1) * pitch + ic, sHx);
     }
     hx_row<0>(S, m, par, ic, j0 - 1, ezp, ezc, hxo, hxp, false);
   }
@@ -272,26 +374,33 @@ __device__ void process_band(const DevShot& S, Ring& R, const float* __restrict_
       if (producer) drain<C>(R);
       return;
     }
-    const float* st = R.stage + s * C::kStageFloats;
+    const unsigned char* st = R.stage + s * C::kStageBytes;
+    const T* sg0 = reinterpret_cast<const T*>(st);                       // Ez(j+1)
+    const T* sg1 = reinterpret_cast<const T*>(st + 1 * C::kSegBytes);    // Hx(j)
+    const T* sg2 = reinterpret_cast<const T*>(st + 2 * C::kSegBytes);    // Hy(j)
+    const T* sg3 = reinterpret_cast<const T*>(st + 3 * C::kSegBytes);    // Jz(j)
+    const T* sg4 = reinterpret_cast<const T*>(st + 4 * C::kSegBytes);    // drive(j)
+    const float* sps = reinterpret_cast<const float*>(st + C::kPsiOffB);  // psi_Hxy, psi_Ezy rows
+    const float* sxs = reinterpret_cast<const float*>(st + C::kXOffB);    // x-strip rows
     float ezn[4], hxo[4], hyo[4], jzo[4];
-    lds4(ezn, st + 0 * C::kSeg + sl);
-    lds4(hxo, st + 1 * C::kSeg + sl);
-    lds4(hyo, st + 2 * C::kSeg + sl);
-    lds4(jzo, st + 3 * C::kSeg + sl);
+    St::lds4(ezn, sg0 + sl, sE);
+    St::lds4(hxo, sg1 + sl, sHx);
+    St::lds4(hyo, sg2 + sl, sHy);
+    St::lds4(jzo, sg3 + sl, sJ);
     if (has_kp) {
-      lds4(m.kp, st + 4 * C::kSeg + sl);
+      St::lds4(m.kp, sg4 + sl, sK);
     } else {
       zero4(m.kp);
     }
     // halo values of row j+1 for the next iteration, and Hy_old(i0-1, j)
-    const float ezl_next = st[0 * C::kSeg + 4 + warp * kCols - 1];
-    const float ezr_next = st[0 * C::kSeg + 4 + warp * kCols + kCols];
-    const float hyo_left = st[2 * C::kSeg + 4 + warp * kCols - 1];
+    const float ezl_next = St::ld1(sg0 + C::kHalo + warp * kCols - 1, sE);
+    const float ezr_next = St::ld1(sg0 + C::kHalo + warp * kCols + kCols, sE);
+    const float hyo_left = St::ld1(sg2 + C::kHalo + warp * kCols - 1, sHy);
     // staged x-strip rows (psi_Hyx, psi_Ezx; side 0, 1): value r at x..[r]
-    const float* xh0 = st + C::kXOff + 0 * kXSlot + (int)(xstrip_off(S, 0, S.o_hyx, 0, j) & 3);
-    const float* xh1 = st + C::kXOff + 1 * kXSlot + (int)(xstrip_off(S, 0, S.o_hyx, 1, j) & 3);
-    const float* xe0 = st + C::kXOff + 2 * kXSlot + (int)(xstrip_off(S, 0, S.o_ezx, 0, j) & 3);
-    const float* xe1 = st + C::kXOff + 3 * kXSlot + (int)(xstrip_off(S, 0, S.o_ezx, 1, j) & 3);
+    const float* xh0 = sxs + 0 * kXSlot + (int)(xstrip_off(S, 0, S.o_hyx, 0, j) & 3);
+    const float* xh1 = sxs + 1 * kXSlot + (int)(xstrip_off(S, 0, S.o_hyx, 1, j) & 3);
+    const float* xe0 = sxs + 2 * kXSlot + (int)(xstrip_off(S, 0, S.o_ezx, 0, j) & 3);
+    const float* xe1 = sxs + 3 * kXSlot + (int)(xstrip_off(S, 0, S.o_ezx, 1, j) & 3);
 
     // ---- H update: Hx bulk + y-strip CPML (psi from the stage)
     const int rh = hxy_row(S, j), re = ezy_row(S, j);
@@ -304,7 +413,7 @@ __device__ void process_band(const DevShot& S, Ring& R, const float* __restrict_
       const float b = cp[(side ? kBhY2 : kBhY1) * P + r];
       const float cc = cp[(side ? kChY2 : kChY1) * P + r];
       float psh[4], pn[4];
-      lds4(psh, st + C::kPsiOff + warp * kCols + 4 * lane);
+      lds4f(psh, sps + warp * kCols + 4 * lane);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         pn[k] = psh[k];
@@ -392,7 +501,7 @@ __device__ void process_band(const DevShot& S, Ring& R, const float* __restrict_
       const float b = cp[(side ? kBeY2 : kBeY1) * P + r];
       const float cc = cp[(side ? kCeY2 : kCeY1) * P + r];
       float pse[4], pn[4];
-      lds4(pse, st + C::kPsiOff + C::kBand + warp * kCols + 4 * lane);
+      lds4f(pse, sps + C::kBand + warp * kCols + 4 * lane);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         pn[k] = pse[k];
@@ -442,10 +551,10 @@ __device__ void process_band(const DevShot& S, Ring& R, const float* __restrict_
 
     if (act) {
       const int64_t o = (int64_t)j * pitch + ic;
-      stcs4(hxw + o, hxn);
-      stcs4(hyw + o, hyn);
-      stcs4(ezw + o, ezw4);
-      stcs4(jzw + o, jzw4);
+      St::stcs4(hxw + o, hxn, S.isc[1]);
+      St::stcs4(hyw + o, hyn, S.isc[2]);
+      St::stcs4(ezw + o, ezw4, S.isc[0]);
+      St::stcs4(jzw + o, jzw4, S.isc[3]);
     }
 
     // Producer: refill this stage with row j + C::kStages.
@@ -477,12 +586,12 @@ template <class C>
 __global__ void __launch_bounds__(C::kThreads, C::kMinBlocks)
 step_tma_kernel(const __grid_constant__ DevShot S, const int4* __restrict__ units, int n_units, int n_global,
                 int* err) {
-  extern __shared__ __align__(128) float smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[C::kStages], empty[C::kStages];
   // The CPML coefficient table (kCpmlRows x P floats) sits after the ring:
   // its reads are per lane (x strips) or per row (y strips) on the critical
   // path, so they come from shared memory instead of the L1/L2.
-  float* cp = smem + C::kStages * C::kStageFloats;
+  float* cp = reinterpret_cast<float*>(smem + C::kStages * C::kStageBytes);
   for (int t = threadIdx.x; t < kCpmlRows * S.npml; t += C::kThreads) cp[t] = S.cpml[t];
   if (threadIdx.x == 0) {
     for (int s = 0; s < C::kStages; ++s) {
@@ -519,7 +628,7 @@ __global__ void __launch_bounds__(C::kThreads, C::kMinBlocks)
 step_tma_batch_kernel(const DevShot* __restrict__ shots, const int4* __restrict__ units,
                       const int* __restrict__ n_units_p, const int* __restrict__ gstep_p, int k, int* counters,
                       int* err) {
-  extern __shared__ __align__(128) float smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[C::kStages], empty[C::kStages];
   __shared__ __align__(16) DevShot sS;
   __shared__ int s_unit;
@@ -540,7 +649,7 @@ step_tma_batch_kernel(const DevShot* __restrict__ shots, const int4* __restrict_
   R.stage = smem;
   R.full = full;
   R.empty = empty;
-  float* cp = smem + C::kStages * C::kStageFloats;   // CPML table of the current shot
+  float* cp = reinterpret_cast<float*>(smem + C::kStages * C::kStageBytes);   // CPML table of the current shot
   int cur = -1;
   for (;;) {
     if (tid == 0) s_unit = *(volatile int*)err ? n_units : atomicAdd(ctr, 1);
@@ -566,16 +675,22 @@ step_tma_batch_kernel(const DevShot* __restrict__ shots, const int4* __restrict_
 using KernelFn = void (*)(DevShot, const int4*, int, int, int*);
 using BatchFn = void (*)(const DevShot*, const int4*, const int*, const int*, int, int*, int*);
 
+// One launch shape: the single-shot kernel per storage type (F32, F16,
+// BF16) and the batched kernel (F32 storage).
 struct ShapeEntry {
   int warps, stages;
-  KernelFn fn;
+  KernelFn fn[3];
+  size_t smem[3];
   BatchFn bfn;
-  size_t smem;
 };
 
 template <int W, int ST>
 constexpr ShapeEntry entry() {
-  return {W, ST, step_tma_kernel<Cfg<W, ST>>, step_tma_batch_kernel<Cfg<W, ST>>, Cfg<W, ST>::kSmem};
+  using C32 = Cfg<W, ST, float>;
+  using C16 = Cfg<W, ST, __half>;
+  using CB16 = Cfg<W, ST, __nv_bfloat16>;
+  return {W, ST, {step_tma_kernel<C32>, step_tma_kernel<C16>, step_tma_kernel<CB16>},
+          {C32::kSmem, C16::kSmem, CB16::kSmem}, step_tma_batch_kernel<C32>};
 }
 
 // Compiled launch shapes; the first is the default.
@@ -598,13 +713,23 @@ void tma_shape_dims(int shape, int* warps, int* stages) {
   *stages = kShapes[shape].stages;
 }
 
+int tma_shape_parse(const char* text) {
+  int w = 0, st = 0;
+  if (!text || std::sscanf(text, "%d,%d", &w, &st) != 2) return -1;
+  return tma_shape_find(w, st);
+}
+
+void tma_shape_name(int shape, const char* kernel, char* out, size_t n) {
+  std::snprintf(out, n, "%s<%d,%d>", kernel, kShapes[shape].warps, kShapes[shape].stages);
+}
+
 int tma_band_cols(int shape) { return kShapes[shape].warps * kCols; }
 
 int tma_max_pml() { return kTmaMaxPml; }
 
 // Dynamic shared memory of one CTA: the ring, then the CPML table.
-static size_t smem_bytes(const ShapeEntry& e, int npml) {
-  return e.smem + (((size_t)kCpmlRows * npml * sizeof(float) + 15) & ~(size_t)15);
+static size_t smem_bytes(size_t ring, int npml) {
+  return ring + (((size_t)kCpmlRows * npml * sizeof(float) + 15) & ~(size_t)15);
 }
 
 cudaError_t launch_step_tma(int shape, const DevShot& shot, const int4* units, int n_units, int n_global,
@@ -612,7 +737,9 @@ cudaError_t launch_step_tma(int shape, const DevShot& shot, const int4* units, i
   const ShapeEntry& e = kShapes[shape];
   const int ctas = max_ctas < n_units ? max_ctas : n_units;
   if (ctas <= 0) return cudaSuccess;
-  e.fn<<<ctas, e.warps * 32, smem_bytes(e, shot.npml), stream>>>(shot, units, n_units, n_global, err);
+  const int st = shot.store;
+  e.fn[st]<<<ctas, e.warps * 32, smem_bytes(e.smem[st], shot.npml), stream>>>(shot, units, n_units, n_global,
+                                                                            err);
   return cudaGetLastError();
 }
 
@@ -620,14 +747,15 @@ cudaError_t launch_step_tma_batch(int shape, const DevShot* shots, const int4* u
                                   const int* gstep, int k, int* counters, int max_pml, int ctas, int* err,
                                   cudaStream_t stream) {
   const ShapeEntry& e = kShapes[shape];
-  e.bfn<<<ctas, e.warps * 32, smem_bytes(e, max_pml), stream>>>(shots, units, n_units, gstep, k, counters, err);
+  e.bfn<<<ctas, e.warps * 32, smem_bytes(e.smem[0], max_pml), stream>>>(shots, units, n_units, gstep, k, counters,
+                                                                         err);
   return cudaGetLastError();
 }
 
 int tma_batch_resident_ctas(int shape, int max_pml, int device) {
   const ShapeEntry& e = kShapes[shape];
-  const size_t smem = smem_bytes(e, max_pml);
-  cudaFuncSetAttribute(e.bfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(e, kTmaMaxPml));
+  const size_t smem = smem_bytes(e.smem[0], max_pml);
+  cudaFuncSetAttribute(e.bfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(e.smem[0], kTmaMaxPml));
   int sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, e.bfn, e.warps * 32, smem);
@@ -635,13 +763,14 @@ int tma_batch_resident_ctas(int shape, int max_pml, int device) {
   return sms * per_sm;
 }
 
-int tma_resident_ctas(int shape, int npml, int device) {
+int tma_resident_ctas(int shape, int npml, int store, int device) {
   const ShapeEntry& e = kShapes[shape];
-  const size_t smem = smem_bytes(e, npml);
-  cudaFuncSetAttribute(e.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(e, kTmaMaxPml));
+  const size_t smem = smem_bytes(e.smem[store], npml);
+  cudaFuncSetAttribute(e.fn[store], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem_bytes(e.smem[store], kTmaMaxPml));
   int sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, e.fn, e.warps * 32, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, e.fn[store], e.warps * 32, smem);
   if (per_sm < 1) per_sm = 1;
   return sms * per_sm;
 }

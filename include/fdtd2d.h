@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define FDTD2D_ABI_VERSION 1
+#define FDTD2D_ABI_VERSION 2
 
 /* ---- status codes -------------------------------------------------------- */
 enum {
@@ -147,6 +147,10 @@ typedef struct fdtd2d_setup {
        here too; 0 means every cell is updated, a negative value none.
        Honoured by the material-ID medium (the Settings.ini path).             */
     int64_t cover[8];
+    /* Reduced field storage (storage = F16 / BF16): expected peak |Ez| used to
+       pick the per-array power-of-two scales (0 = estimated from the source
+       amplitude, the array size, the carrier and the plasma drive).           */
+    double  field_max;
 } fdtd2d_setup;
 
 /* ---- single shot (the reference's plain run) ------------------------------ */
@@ -324,7 +328,8 @@ typedef struct fdtd2d_spec {
     int32_t n_det, det_i, det_j, det_di, det_dj;
     int32_t record_traces;
     double  dft_freq;           /* 0 -> freq                                        */
-    int32_t storage;
+    int32_t storage;            /* FDTD2D_STORE_*                                   */
+    double  field_max;          /* expected peak |Ez| for reduced storage (0 = estimate) */
 } fdtd2d_spec;
 
 /* Fill a spec with the plain 512^2 workload defaults. */

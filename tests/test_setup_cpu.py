@@ -28,7 +28,7 @@ def test_library_exports_every_declared_entry_point():
     missing = declared - exported
     assert not missing, missing
     lib = F.lib()
-    assert lib.fdtd2d_abi_version() == 1
+    assert lib.fdtd2d_abi_version() == 2
     assert lib.fdtd2d_strerror(F.ERR_RANGE).decode() == "index or step out of range"
 
 
