@@ -82,6 +82,14 @@ def allreduce_max(dist, x: float) -> float:
     return float(t.item())
 
 
+def replica_throughput(dist, units: float, seconds: float) -> tuple[float, float]:
+    """Whole-job rate of N replicas: all ranks' units / the slowest rank's
+    time.  Returns (units per second, slowest time)."""
+    t_max = allreduce_max(dist, seconds)
+    total = allreduce_sum(dist, units)
+    return total / t_max, t_max
+
+
 def allreduce_sum(dist, x: float) -> float:
     if dist is None:
         return x
@@ -170,7 +178,9 @@ def workload_config(args) -> dict:
                         "tanh x GRF plasma, nu 2e9/s, 16 elements at 50 GHz steered 15 deg, 16 Ez "
                         "detectors + FP64 DFT",
             "nx": args.size, "ny": args.size, "npml": 32, "shot_steps": 20000, "block_steps": args.block,
-            "dx_mm": 0.25, "courant": 0.99, "bytes_per_cell_update": BYTES_PER_CELL,
+            "dx_mm": 0.25, "courant": 0.99,
+            "bytes_per_cell_update": BYTES_PER_CELL if getattr(args, "storage", "f32") == "f32" else 18,
+            "storage": getattr(args, "storage", "f32"),
             "l2": "no flush: 2.4 GB touched per time step >> 129 MB L2",
             "parallelism": f"replicas x{args.gpus}"}
 
@@ -463,7 +473,9 @@ def run_ours(args, world, rank, local, dist) -> None:
 
     S, K, W = args.block, args.steps, args.warmup
     total_steps = (W + K) * S
-    prob = make_problem(max(20000, total_steps), args.size)
+    store = {"f32": 0, "f16": 1, "bf16": 2}[args.storage]
+    bpc = BYTES_PER_CELL if store == 0 else 18   # 16-bit Ez, Hx, Hy, Jz and drive
+    prob = make_problem(max(20000, total_steps), args.size, storage=store)
     cells = prob.nx * prob.ny
     shot = F.Shot(prob, device=local)
     shot.run(1, W * S)
@@ -481,19 +493,18 @@ def run_ours(args, world, rank, local, dist) -> None:
     clk = clocks.stop()
     ok = shot.check_finite()
     shot.close()
-    t_max = allreduce_max(dist, ms / 1e3)
-    units = allreduce_sum(dist, float(cells) * S * K)
-    value = units / t_max / 1e9
+    rate, t_max = replica_throughput(dist, float(cells) * S * K, ms / 1e3)
+    value = rate / 1e9
 
     # roofline of the step kernel (one launch per time step on this workload)
     per_launch_s = (ms / 1e3) / (K * S)
-    achieved = BYTES_PER_CELL * cells / per_launch_s / 1e9
+    achieved = bpc * cells / per_launch_s / 1e9
     peaks = measured_peaks()
     peak = peaks.get("hbm_gbs")
     peak_src = "measured"
     if not peak:
         peak, peak_src = 6800.0, "fallback"
-    traffic = profile_traffic()
+    traffic = profile_traffic() if (store == 0 and args.size == 8192) else None
 
     # end to end through the C ABI with host buffers
     e2e = None
@@ -538,11 +549,12 @@ def run_ours(args, world, rank, local, dist) -> None:
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
                 "ms_per_step": t_max * 1e3 / K, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(args),
+                "vs_baseline": None, "dtype": "f32" if store == 0 else f"f32 arithmetic, {args.storage} storage",
+                "data": "synthetic", "config": workload_config(args),
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic,
                              "peak_source": peak_src, "kernel": kernel,
-                             "algorithmic_bytes_per_launch": BYTES_PER_CELL * cells},
+                             "algorithmic_bytes_per_launch": bpc * cells},
                 "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk,
                 "finite": ok, "precision": precision, "batched": batched, "serving": serving}
         print(json.dumps(line), flush=True)
@@ -564,6 +576,8 @@ def main() -> None:
                     help="fraction of the 8000..16000 steps each mixed shot runs")
     ap.add_argument("--serve-requests", type=int, default=6, help="requests in the serving sample (0: skip)")
     ap.add_argument("--serve-max-side", type=int, default=4096)
+    ap.add_argument("--storage", choices=["f32", "f16", "bf16"], default="f32",
+                    help="field storage of the main measurement (arithmetic is FP32 in all)")
     ap.add_argument("--prec-steps", type=int, default=2000,
                     help="steps of the F16/BF16 vs FP32 comparison on the production shot (0: skip)")
     args = ap.parse_args()
