@@ -285,12 +285,9 @@ __device__ void drain(Ring& R) {
   for (uint32_t g = R.used; g < R.issued; ++g) mbar_wait(&R.full[g % C::kStages], (g / C::kStages) & 1);
 }
 
-// One unit (band c0, rows [j0, j1)) of step n.  FAST: this warp's columns
-// and its Hy halo column lie outside both x strips and inside [1, nx-2], so
-// the per-column predicates and the x-strip code are compiled out.
-template <class C, bool FAST>
-__device__ __forceinline__ void process_band_impl(const DevShot& S, Ring& R, const float* __restrict__ cp, int c0,
-                                                  int j0, int j1, int n, int* err) {
+template <class C>
+__device__ void process_band(const DevShot& S, Ring& R, const float* __restrict__ cp, int c0, int j0, int j1, int n,
+                             int* err) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nx = S.nx, ny = S.ny, P = S.npml;
   const int64_t pitch = S.pitch;
@@ -311,11 +308,9 @@ __device__ __forceinline__ void process_band_impl(const DevShot& S, Ring& R, con
 
   const int i0 = c0 + warp * kCols;            // this warp's first column
   const int i = i0 + 4 * lane;
-  const bool act = FAST || i < nx;
+  const bool act = i < nx;
   const int ic = act ? i : 0;
   const int sl = C::kHalo + warp * kCols + 4 * lane;  // lane's 4 elements in a staged segment
-  // this warp holds x-strip columns (or the Hy halo column of one)
-  const bool xw = (i0 <= P - 1) || (i0 + kCols - 1 >= nx - P && i0 <= nx - 1);
   const int rows = j1 - j0;
   // The producer thread: lane 0 of a warp with no x-strip columns where the
   // band has one (the first band's strip is in warp 0, the last band's in
@@ -367,8 +362,7 @@ __device__ __forceinline__ void process_band_impl(const DevShot& S, Ring& R, con
   float dhy = __ldg(S.den_hy + j0), dey = __ldg(S.den_ey + j0);
   int p0 = __ldg(S.row_start + j0), p1 = __ldg(S.row_start + j0 + 1);
 
-  int64_t orow = (int64_t)j0 * pitch + ic;   // this lane's cell (ic, j) in a field buffer
-  for (int j = j0; j < j1; ++j, orow += pitch) {
+  for (int j = j0; j < j1; ++j) {
     const int jn = j + 1 < j1 ? j + 1 : j;
     const float dhy_n = __ldg(S.den_hy + jn), dey_n = __ldg(S.den_ey + jn);
     const int p1_n = __ldg(S.row_start + jn + 1);
@@ -403,20 +397,17 @@ __device__ __forceinline__ void process_band_impl(const DevShot& S, Ring& R, con
     const float ezr_next = St::ld1(sg0 + C::kHalo + warp * kCols + kCols, sE);
     const float hyo_left = St::ld1(sg2 + C::kHalo + warp * kCols - 1, sHy);
     // staged x-strip rows (psi_Hyx, psi_Ezx; side 0, 1): value r at x..[r]
-    const float *xh0 = sxs, *xh1 = sxs, *xe0 = sxs, *xe1 = sxs;
-    if (!FAST && xw) {
-      xh0 = sxs + 0 * kXSlot + (int)(xstrip_off(S, 0, S.o_hyx, 0, j) & 3);
-      xh1 = sxs + 1 * kXSlot + (int)(xstrip_off(S, 0, S.o_hyx, 1, j) & 3);
-      xe0 = sxs + 2 * kXSlot + (int)(xstrip_off(S, 0, S.o_ezx, 0, j) & 3);
-      xe1 = sxs + 3 * kXSlot + (int)(xstrip_off(S, 0, S.o_ezx, 1, j) & 3);
-    }
+    const float* xh0 = sxs + 0 * kXSlot + (int)(xstrip_off(S, 0, S.o_hyx, 0, j) & 3);
+    const float* xh1 = sxs + 1 * kXSlot + (int)(xstrip_off(S, 0, S.o_hyx, 1, j) & 3);
+    const float* xe0 = sxs + 2 * kXSlot + (int)(xstrip_off(S, 0, S.o_ezx, 0, j) & 3);
+    const float* xe1 = sxs + 3 * kXSlot + (int)(xstrip_off(S, 0, S.o_ezx, 1, j) & 3);
 
     // ---- H update: Hx bulk + y-strip CPML (psi from the stage)
     const int rh = hxy_row(S, j), re = ezy_row(S, j);
     float hxn[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-      hxn[k] = (FAST || i + k <= nx - 2) ? upd_h(S.da, hxo[k], S.db, ezc[k], ezn[k], dhy) : hxo[k];
+      hxn[k] = (i + k <= nx - 2) ? upd_h(S.da, hxo[k], S.db, ezc[k], ezn[k], dhy) : hxo[k];
     if (rh >= 0) {
       const int side = rh >= P - 1, r = side ? rh - (P - 1) : rh;
       const float b = cp[(side ? kBhY2 : kBhY1) * P + r];
@@ -426,7 +417,7 @@ __device__ __forceinline__ void process_band_impl(const DevShot& S, Ring& R, con
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         pn[k] = psh[k];
-        if (FAST || i + k <= nx - 2) {
+        if (i + k <= nx - 2) {
           pn[k] = upd_psi(b, psh[k], cc, ezc[k], ezn[k]);
           hxn[k] = __fmaf_rn(S.db, pn[k], hxn[k]);
         }
@@ -439,10 +430,8 @@ __device__ __forceinline__ void process_band_impl(const DevShot& S, Ring& R, con
     float hyn[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-      hyn[k] = (FAST || i + k <= nx - 2) ? upd_h(m.day(k), hyo[k], m.dby(k), ezr4[k], ezc[k], dhx[k]) : hyo[k];
-    // x-strip CPML: a warp-uniform test first, so warps with no strip
-    // column branch over the per-lane code instead of running it predicated
-    if (!FAST && xw && act && (i <= P - 2 || i + 3 >= nx - P)) {
+      hyn[k] = (i + k <= nx - 2) ? upd_h(m.day(k), hyo[k], m.dby(k), ezr4[k], ezc[k], dhx[k]) : hyo[k];
+    if (act && (i <= P - 2 || i + 3 >= nx - P)) {
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         const int c = i + k;
@@ -468,7 +457,7 @@ __device__ __forceinline__ void process_band_impl(const DevShot& S, Ring& R, con
         int side = -1, r = 0;
         if (c <= P - 2) { side = 0; r = c; }
         else if (c >= nx - P && c <= nx - 2) { side = 1; r = nx - 2 - c; }
-        if (!FAST && side >= 0) {
+        if (side >= 0) {
           const float b = cp[(side ? kBhX2 : kBhX1) * P + r];
           const float cc = cp[(side ? kChX2 : kChX1) * P + r];
           const float pn = upd_psi(b, (side ? xh1 : xh0)[r], cc, ezc[0], ezl);
@@ -485,13 +474,13 @@ __device__ __forceinline__ void process_band_impl(const DevShot& S, Ring& R, con
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int c = i + k;
-      const bool in = FAST ? row_in : (row_in && c >= 1 && c <= nx - 2);
+      const bool in = row_in && c >= 1 && c <= nx - 2;
       jzw4[k] = in ? upd_j(S.ja, jzo[k], m.kp[k], ezc[k]) : jzo[k];
       ezw4[k] = in ? upd_e(S.ca, ezc[k], S.cb, __fsub_rn(hyn[k], hyl4[k]), dex[k], __fsub_rn(hxp[k], hxn[k]),
                            dey, jzw4[k])
                    : ezc[k];
     }
-    if (!FAST && xw && act && row_in && (i <= P - 1 || i + 3 >= nx - P)) {
+    if (act && row_in && (i <= P - 1 || i + 3 >= nx - P)) {
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         const int c = i + k;
@@ -516,7 +505,7 @@ __device__ __forceinline__ void process_band_impl(const DevShot& S, Ring& R, con
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         pn[k] = pse[k];
-        if (FAST || (i + k >= 1 && i + k <= nx - 2)) {
+        if (i + k >= 1 && i + k <= nx - 2) {
           pn[k] = upd_psi(b, pse[k], cc, hxp[k], hxn[k]);
           ezw4[k] = __fmaf_rn(S.cb, pn[k], ezw4[k]);
         }
@@ -561,7 +550,7 @@ __device__ __forceinline__ void process_band_impl(const DevShot& S, Ring& R, con
     }
 
     if (act) {
-      const int64_t o = orow;
+      const int64_t o = (int64_t)j * pitch + ic;
       St::stcs4(hxw + o, hxn, S.isc[1]);
       St::stcs4(hyw + o, hyn, S.isc[2]);
       St::stcs4(ezw + o, ezw4, S.isc[0]);
@@ -588,17 +577,6 @@ __device__ __forceinline__ void process_band_impl(const DevShot& S, Ring& R, con
     p0 = p1;
     p1 = p1_n;
   }
-}
-
-template <class C>
-__device__ __forceinline__ void process_band(const DevShot& S, Ring& R, const float* __restrict__ cp, int c0, int j0,
-                                             int j1, int n, int* err) {
-  const int i0 = c0 + (int)(threadIdx.x >> 5) * kCols;
-  const int P = S.npml;
-  if (i0 >= P && i0 + kCols - 1 <= S.nx - P - 1)
-    process_band_impl<C, true>(S, R, cp, c0, j0, j1, n, err);
-  else
-    process_band_impl<C, false>(S, R, cp, c0, j0, j1, n, err);
 }
 
 // The shot descriptor is a __grid_constant__ parameter: its fields are read
