@@ -50,7 +50,7 @@ def _stale(out: Path, deps: list[Path]) -> bool:
 def build(verbose: bool = False, force: bool = False) -> dict[str, Path]:
     OBJ.mkdir(exist_ok=True)
     nvcc = _nvcc()
-    headers = list(CSRC.glob("*.h")) + [ROOT / "include" / "fdtd2d.h"]
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "fdtd2d.h"]
     jobs = []
     objs = []
     for src in CUDA_SOURCES:
