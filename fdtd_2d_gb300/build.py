@@ -22,7 +22,7 @@ ORACLE = ROOT / "oracle"
 OBJ = ROOT / "_build"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["step_kernels.cu", "step_tma.cu", "api.cu", "batch.cu", "noalloc.cu"]
+CUDA_SOURCES = ["step_kernels.cu", "step_tma.cu", "step_tmat.cu", "api.cu", "batch.cu", "noalloc.cu"]
 HOST_SOURCES = ["problem.cpp", "ini.cpp", "driver.cpp", "processing.cpp"]
 HOST_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall"]
 

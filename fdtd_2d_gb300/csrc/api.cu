@@ -8,6 +8,7 @@
 
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <climits>
@@ -81,6 +82,71 @@ void set_storage_scales(const fdtd2d_setup* s, double beta, DevShot* h) {
   pow2_scale(em / eta0 * 4, &h->sc[2], &h->isc[2]);
   pow2_scale(jm, &h->sc[3], &h->isc[3]);
   pow2_scale(kmax, &h->sc[4], &h->isc[4]);
+}
+
+// cuTensorMapEncodeTiled from the driver (no link-time dependency on it).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// Tensor maps of a shot for a tensor shape: boxes of bx columns x rows rows.
+bool encode_maps(const DevShot& h, int nx, int ny, int bx, int rows, TensorMaps* m) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_encoder();
+  if (!enc) return false;
+  const int es = store_bytes(h.store);
+  const CUtensorMapDataType dt = h.store == FDTD2D_STORE_F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                 : h.store == FDTD2D_STORE_F16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                               : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  const cuuint32_t est[3] = {1, 1, 1};
+  for (int b = 0; b < 2; ++b) {
+    const cuuint64_t dims3[3] = {(cuuint64_t)nx, (cuuint64_t)ny, 3};
+    const cuuint64_t str3[2] = {(cuuint64_t)h.pitch * es, (cuuint64_t)2 * h.cells * es};
+    const cuuint32_t box3[3] = {(cuuint32_t)bx, (cuuint32_t)rows, 3};
+    void* hx = es == 4 ? (void*)field_ptr_t<float>(h, kHx, b) : (void*)field_ptr_t<uint16_t>(h, kHx, b);
+    if (enc(&m->hj[b], dt, 3, hx, dims3, str3, box3, est, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+    const cuuint64_t dims2[2] = {(cuuint64_t)nx, (cuuint64_t)ny};
+    const cuuint64_t str2[1] = {(cuuint64_t)h.pitch * es};
+    const cuuint32_t box2[2] = {(cuuint32_t)bx, (cuuint32_t)rows};
+    void* ez = es == 4 ? (void*)field_ptr_t<float>(h, kEz, b) : (void*)field_ptr_t<uint16_t>(h, kEz, b);
+    if (enc(&m->e[b], dt, 2, ez, dims2, str2, box2, est, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  std::memset(&m->k, 0, sizeof m->k);
+  if (h.kp) {
+    const cuuint64_t dims2[2] = {(cuuint64_t)nx, (cuuint64_t)ny};
+    const cuuint64_t str2[1] = {(cuuint64_t)h.pitch * es};
+    const cuuint32_t box2[2] = {(cuuint32_t)bx, (cuuint32_t)rows};
+    if (enc(&m->k, dt, 2, const_cast<float*>(h.kp), dims2, str2, box2, est, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  return true;
+}
+
+// Units (0, c0, j0, j1) over columns [ca, cb) in bands of `band`, rows
+// [ra, rb) in `strips` strips.
+void add_units(std::vector<int4>& u, int ca, int cb, int band, int ra, int rb, int strips) {
+  if (cb <= ca || rb <= ra) return;
+  strips = std::max(1, std::min(strips, rb - ra));
+  for (int k = 0; k < strips; ++k) {
+    const int j0 = ra + (int)((int64_t)(rb - ra) * k / strips), j1 = ra + (int)((int64_t)(rb - ra) * (k + 1) / strips);
+    if (j1 <= j0) continue;
+    for (int c = ca; c < cb; c += band) u.push_back(make_int4(0, c, j0, j1));
+  }
 }
 
 // Keep freed shot memory in this process's pool of the device (default
@@ -217,6 +283,129 @@ int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
 
 }  // extern "C"
 
+namespace {
+
+// Multi-row tensor path (step_tmat.cu) for the interior of the shot, beside
+// the staged kernel on the CPML bands and rows.  Times every tensor shape that
+// fits the grid (tensor kernel on the interior units + staged kernel on the
+// rest, one step with traces and DFT off, re-run idempotently) against the
+// staged kernel alone, and keeps the faster.  FDTD2D_TMAT=0 leaves it off,
+// FDTD2D_TMAT=W,R,ST forces a shape.
+int setup_tmat(fdtd2d_ctx* c, int device) {
+  const char* env = std::getenv("FDTD2D_TMAT");
+  if (env && std::strcmp(env, "0") == 0) return FDTD2D_OK;
+  if (!tensor_encoder()) return FDTD2D_OK;
+  int forced = -1;
+  if (env) {
+    int w = 0, r = 0, st = 0;
+    if (std::sscanf(env, "%d,%d,%d", &w, &r, &st) == 3)
+      for (int k = 0; k < tmat_shape_count(); ++k) {
+        int a, b, d;
+        tmat_shape_dims(k, &a, &b, &d);
+        if (a == w && b == r && d == st) forced = k;
+      }
+  }
+  const DevShot& h = c->h;
+  const int nx = c->nx, ny = c->ny, P = c->npml;
+  const int b1 = tma_band_cols(c->tma_shape);
+  DevShot t = h;
+  t.record = 0;
+  t.dft = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return FDTD2D_ERR_CUDA;
+  auto timed = [&](auto&& step) -> float {
+    cudaError_t e = step();
+    if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+    for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = step();
+    if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = -1.f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    return e == cudaSuccess ? ms : -1.f;
+  };
+  const int n1 = t.base_n + 1;
+  float best = 1e30f;
+  if (forced < 0) {
+    best = timed([&] { return launch_step_tma(c->tma_shape, t, c->d_units, c->n_units, n1, c->grid_warps, c->d_err,
+                                              c->stream); });
+    if (best < 0) best = 1e30f;
+  }
+  int best_k = -1;
+  std::vector<int4> best_t, best_e;
+  TensorMaps best_m{};
+  for (int k = 0; k < tmat_shape_count(); ++k) {
+    if (forced >= 0 && k != forced) continue;
+    const int bt = tmat_band_cols(k), big = std::max(bt, b1), R = tmat_rows(k);
+    const int ci0 = (P + big - 1) / big * big, ci1 = (nx - P) / big * big;
+    if (ci1 - ci0 < bt || ny - 2 * P < 4 * R) continue;
+    TensorMaps maps{};
+    if (!encode_maps(h, nx, ny, tmat_box_cols(k), R, &maps)) continue;
+    const int tctas = tmat_resident_ctas(k, h.store, device);
+    std::vector<int4> tu, eu;
+    const int nbt = (ci1 - ci0) / bt;
+    add_units(tu, ci0, ci1, bt, P, ny - P, std::min(std::max(1, tctas / nbt), (ny - 2 * P) / (2 * R)));
+    // the staged kernel: edge bands over all rows, interior bands over the CPML rows
+    const int neb = (ci0 + b1 - 1) / b1 + (nx - ci1 + b1 - 1) / b1;
+    const int se = std::min(std::max(1, c->grid_warps / std::max(1, neb)), std::max(1, (ny - 1) / 8));
+    add_units(eu, 0, ci0, b1, 0, ny - 1, se);
+    add_units(eu, ci1, nx, b1, 0, ny - 1, se);
+    add_units(eu, ci0, ci1, b1, 0, P, 1);
+    add_units(eu, ci0, ci1, b1, ny - P, ny - 1, 1);
+    int4 *dt = nullptr, *de = nullptr;
+    cudaError_t e = cudaMallocAsync(&dt, tu.size() * sizeof(int4), c->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync(&de, eu.size() * sizeof(int4), c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dt, tu.data(), tu.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(de, eu.data(), eu.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
+    float ms = -1.f;
+    if (e == cudaSuccess)
+      ms = timed([&] {
+        cudaError_t x = launch_step_tmat(k, t, maps, dt, (int)tu.size(), n1, tctas, c->d_err, c->stream);
+        if (x == cudaSuccess)
+          x = launch_step_tma(c->tma_shape, t, de, (int)eu.size(), n1, c->grid_warps, c->d_err, c->stream);
+        return x;
+      });
+    if (dt) cudaFreeAsync(dt, c->stream);
+    if (de) cudaFreeAsync(de, c->stream);
+    if (ms >= 0 && ms < best) {
+      best = ms;
+      best_k = k;
+      best_t = tu;
+      best_e = eu;
+      best_m = maps;
+      c->tmat_ctas = tctas;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  int derr = 0;
+  if (cudaMemcpy(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return FDTD2D_ERR_CUDA;
+  if (derr != kErrNone) return FDTD2D_ERR_TIMEOUT;
+  if (best_k < 0) return FDTD2D_OK;
+  cudaError_t e = dalloc(c, &c->d_tunits, best_t.size());
+  if (e == cudaSuccess) e = dalloc(c, &c->d_eunits, best_e.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->d_tunits, best_t.data(), best_t.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->d_eunits, best_e.data(), best_e.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  c->tmat = true;
+  c->tmat_shape = best_k;
+  c->n_tunits = (int)best_t.size();
+  c->n_eunits = (int)best_e.size();
+  c->maps = best_m;
+  int w, r, st;
+  tmat_shape_dims(best_k, &w, &r, &st);
+  char one[48];
+  tma_shape_name(c->tma_shape, "step_tma_kernel", one, sizeof one);
+  std::snprintf(c->kernel_name, sizeof c->kernel_name, "step_tmat_kernel<%d,%d,%d>+%s", w, r, st, one);
+  return FDTD2D_OK;
+}
+
+}  // namespace
+
 void fdtd2d::adopt_ctx(fdtd2d_ctx* c, cudaStream_t batch_stream) {
   cudaSetDevice(c->device);
   if (c->stream && !c->batch) {
@@ -267,6 +456,14 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
     cudaError_t _e = (expr);         \
     if (_e != cudaSuccess) {         \
       rc = fail_cuda(c, _e);         \
+      fdtd2d_destroy(c);             \
+      return rc;                     \
+    }                                \
+  } while (0)
+#define CK_RC(expr)                  \
+  do {                               \
+    rc = (expr);                     \
+    if (rc != FDTD2D_OK) {           \
       fdtd2d_destroy(c);             \
       return rc;                     \
     }                                \
@@ -569,9 +766,11 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
   CK(dalloc(c, &c->d_units, units.size()));
   CK(cudaMemcpyAsync(c->d_units, units.data(), units.size() * sizeof(int4), cudaMemcpyHostToDevice,
                      c->stream));
+  if (c->tma && !member) CK_RC(setup_tmat(c, device));
   CK(dalloc(c, &c->d_flag, 1));
   CK(cudaStreamSynchronize(c->stream));
 #undef CK
+#undef CK_RC
   *out = c;
   return FDTD2D_OK;
 }
@@ -584,8 +783,19 @@ int fdtd2d_run(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
   if (n_first != c->step + 1 || n_last < n_first - 1 || n_last > c->n_steps) return FDTD2D_ERR_RANGE;
   cudaSetDevice(c->device);
   for (int32_t n = n_first; n <= n_last; ++n) {
-    cudaError_t e = c->tma ? launch_step_tma(c->tma_shape, c->h, c->d_units, c->n_units, n, c->grid_warps, c->d_err, c->stream)
-                           : launch_step(c->h, c->d_units, c->n_units, n, c->medium, c->grid_warps, c->stream);
+    cudaError_t e;
+    if (c->tmat) {
+      // interior on the multi-row tensor kernel, CPML bands and rows on the staged one
+      e = launch_step_tmat(c->tmat_shape, c->h, c->maps, c->d_tunits, c->n_tunits, n, c->tmat_ctas, c->d_err,
+                           c->stream);
+      if (e == cudaSuccess) {
+        ++c->launches;
+        e = launch_step_tma(c->tma_shape, c->h, c->d_eunits, c->n_eunits, n, c->grid_warps, c->d_err, c->stream);
+      }
+    } else {
+      e = c->tma ? launch_step_tma(c->tma_shape, c->h, c->d_units, c->n_units, n, c->grid_warps, c->d_err, c->stream)
+                 : launch_step(c->h, c->d_units, c->n_units, n, c->medium, c->grid_warps, c->stream);
+    }
     if (e != cudaSuccess) return fail_cuda(c, e);
     ++c->launches;
     const float* ez_now = field_ptr(c->h, kEz, n & 1);

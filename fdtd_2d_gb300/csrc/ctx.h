@@ -31,7 +31,16 @@ struct fdtd2d_ctx {
   int* d_err = nullptr;     // device error word (bounded waits)
   bool tma = false;         // shared-memory staged kernel (uniform medium)
   int tma_shape = 0;        // its launch shape (index into the compiled shapes)
-  char kernel_name[48] = {0};
+  // multi-row tensor path for the interior (step_tmat.cu) beside the staged
+  // kernel on the CPML bands and rows
+  bool tmat = false;
+  int tmat_shape = 0, tmat_ctas = 0;
+  int4* d_tunits = nullptr;   // interior units (tensor kernel)
+  int n_tunits = 0;
+  int4* d_eunits = nullptr;   // the rest (staged kernel)
+  int n_eunits = 0;
+  fdtd2d::TensorMaps maps{};
+  char kernel_name[96] = {0};
   // wave-front tracker and line probe
   int n_rc = 0, rc_j_cut = 0;
   float rc_level = 0;

@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace fdtd2d {
@@ -142,6 +143,27 @@ void tma_shape_name(int shape, const char* kernel, char* out, size_t n);
 int tma_band_cols(int shape);
 int tma_max_pml();   // largest CPML depth the staged kernel takes
 int tma_resident_ctas(int shape, int npml, int store, int device);
+
+// Tensor maps of one shot for the multi-row staged kernel (step_tmat.cu):
+// Hx, Hy, Jz of field buffer b as one rank-3 tensor (column, row, field),
+// Ez of buffer b and the drive map as rank-2 tensors (column, row); column 0
+// of row 0 is the origin, columns outside [0, nx) and rows outside [0, ny)
+// read as zero.
+struct TensorMaps {
+  CUtensorMap hj[2], e[2], k;
+};
+
+// Multi-row staged kernel for the interior of a shot: units (0, c0, j0, j1)
+// whose band and halo column lie outside the x strips and whose rows lie in
+// [npml, ny - npml).  Shapes: (warps, rows per stage, stages).
+int tmat_shape_count();
+void tmat_shape_dims(int shape, int* warps, int* rows, int* stages);
+int tmat_band_cols(int shape);
+int tmat_box_cols(int shape);   // columns per tensor box (band + 16 halo = boxes x box_cols)
+int tmat_rows(int shape);
+int tmat_resident_ctas(int shape, int store, int device);
+cudaError_t launch_step_tmat(int shape, const DevShot& shot, const TensorMaps& maps, const int4* units,
+                             int n_units, int n_global, int max_ctas, int* err, cudaStream_t stream);
 // Launches the instantiation for shot.store.
 cudaError_t launch_step_tma(int shape, const DevShot& shot, const int4* units, int n_units, int n_global,
                             int max_ctas, int* err, cudaStream_t stream);

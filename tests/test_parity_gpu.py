@@ -128,6 +128,51 @@ def test_every_launch_shape(gpu, monkeypatch, shape):
         assert _random_state_case(gpu, nx, ny, P) == f"step_tma_kernel<{shape}>"
 
 
+# Multi-row tensor shapes (warps, rows per stage, stages) of step_tmat.cu.
+TMAT_SHAPES = ["4,4,2", "4,2,3", "4,4,3", "2,8,2", "4,8,2", "8,2,2"]
+
+
+def _stepped_state(gpu, prob, st, steps):
+    with F.Shot(prob, gpu) as shot:
+        name = shot.kernel_name()
+        load_state([shot], st)
+        shot.run(1, steps)
+        out = {w: shot.read_field(w) for w in FIELDS + PSI_FIELDS}
+        out["det"] = shot.traces()["det_ez"]
+    return name, out
+
+
+@pytest.mark.parametrize("shape", TMAT_SHAPES)
+@pytest.mark.parametrize("storage", [F.STORE_F32, F.STORE_F16])
+def test_tensor_interior_equals_staged(gpu, monkeypatch, shape, storage):
+    """The multi-row tensor kernel on the interior (forced through
+    FDTD2D_TMAT) gives every cell the same bits as the one-row staged kernel
+    alone (FDTD2D_TMAT=0): same arithmetic, different staging.  Random state,
+    a source and a detector inside the interior, width not a multiple of the
+    band, rows not a multiple of the stage rows."""
+    monkeypatch.delenv("FDTD2D_KERNEL", raising=False)
+    monkeypatch.delenv("FDTD2D_TMA", raising=False)
+    nx, ny, P, steps = 2600, 301, 11, 25
+    prob = F.Problem.from_spec(nx=nx, ny=ny, npml=P, n_steps=steps, profile=1, x_lo=nx // 3, x_hi=nx - 3,
+                               ne_peak=2e19, nu=3e9, src_i=1300, src_j=150, det_i=1303, det_j=151, n_det=1,
+                               storage=storage, field_max=100.0)
+    rng = np.random.default_rng(11)
+    st = {}
+    for w in FIELDS:
+        a = (rng.standard_normal(F.field_shape(w, nx, ny, P)) * 0.5).astype(np.float32)
+        st[w] = a / np.float32(377.0) if w in (F.FIELD_HX, F.FIELD_HY) else a
+    for w in PSI_FIELDS:
+        st[w] = (rng.standard_normal(F.field_shape(w, nx, ny, P)) * 1e-3).astype(np.float32)
+    monkeypatch.setenv("FDTD2D_TMAT", "0")
+    name0, ref = _stepped_state(gpu, prob, st, steps)
+    assert "tmat" not in name0
+    monkeypatch.setenv("FDTD2D_TMAT", shape)
+    name1, got = _stepped_state(gpu, prob, st, steps)
+    assert name1.startswith(f"step_tmat_kernel<{shape}>+step_tma_kernel<"), name1
+    for k in ref:
+        assert np.array_equal(ref[k], got[k]), (shape, k)
+
+
 def test_autotuned_shape_and_deep_cpml(gpu, monkeypatch):
     """Without FDTD2D_TMA the create call times the shapes and keeps one; a
     CPML deeper than the staged kernel's x-strip slots streams instead."""
