@@ -308,6 +308,13 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   const DevShot& h = c->h;
   const int nx = c->nx, ny = c->ny, P = c->npml;
   const int b1 = tma_band_cols(c->tma_shape);
+  if (!c->side) {
+    cudaError_t e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_t, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_e, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_m, cudaEventDisableTiming);
+    if (e != cudaSuccess) return fail_cuda(c, e);
+  }
   DevShot t = h;
   t.record = 0;
   t.dft = nullptr;
@@ -359,11 +366,19 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(de, eu.data(), eu.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
     float ms = -1.f;
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev_m, c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_m, 0);
+    // one trial step as fdtd2d_run issues it: the two kernels on two streams
     if (e == cudaSuccess)
       ms = timed([&] {
-        cudaError_t x = launch_step_tmat(k, t, maps, dt, (int)tu.size(), n1, tctas, c->d_err, c->stream);
+        cudaError_t x = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
+        if (x == cudaSuccess) x = launch_step_tmat(k, t, maps, dt, (int)tu.size(), n1, tctas, c->d_err, c->stream);
+        if (x == cudaSuccess) x = cudaStreamWaitEvent(c->side, c->ev_t, 0);
+        if (x == cudaSuccess) x = cudaEventRecord(c->ev_t, c->stream);
         if (x == cudaSuccess)
-          x = launch_step_tma(c->tma_shape, t, de, (int)eu.size(), n1, c->grid_warps, c->d_err, c->stream);
+          x = launch_step_tma(c->tma_shape, t, de, (int)eu.size(), n1, c->grid_warps, c->d_err, c->side);
+        if (x == cudaSuccess) x = cudaEventRecord(c->ev_e, c->side);
+        if (x == cudaSuccess) x = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
         return x;
       });
     if (dt) cudaFreeAsync(dt, c->stream);
@@ -412,6 +427,12 @@ void fdtd2d::adopt_ctx(fdtd2d_ctx* c, cudaStream_t batch_stream) {
     cudaStreamSynchronize(c->stream);
     cudaStreamDestroy(c->stream);
   }
+  if (c->side) {
+    cudaStreamSynchronize(c->side);
+    cudaStreamDestroy(c->side);
+  }
+  for (cudaEvent_t ev : {c->ev_t, c->ev_e, c->ev_m})
+    if (ev) cudaEventDestroy(ev);
   c->stream = batch_stream;
   c->batch = true;
 }
@@ -782,16 +803,33 @@ int fdtd2d_run(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
   if (c->batch) return FDTD2D_ERR_STATE;   // stepped by its batch
   if (n_first != c->step + 1 || n_last < n_first - 1 || n_last > c->n_steps) return FDTD2D_ERR_RANGE;
   cudaSetDevice(c->device);
+  if (c->tmat && n_first <= n_last) {
+    // the side stream starts after the shot stream's earlier work (uploads, writes)
+    cudaError_t e = cudaEventRecord(c->ev_m, c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_m, 0);
+    if (e != cudaSuccess) return fail_cuda(c, e);
+  }
   for (int32_t n = n_first; n <= n_last; ++n) {
     cudaError_t e;
     if (c->tmat) {
-      // interior on the multi-row tensor kernel, CPML bands and rows on the staged one
-      e = launch_step_tmat(c->tmat_shape, c->h, c->maps, c->d_tunits, c->n_tunits, n, c->tmat_ctas, c->d_err,
-                           c->stream);
+      // Interior on the multi-row tensor kernel (shot stream), CPML bands and
+      // rows on the staged kernel (side stream), both kernels of a step at
+      // once.  Each waits for the other's kernel of the previous step: it
+      // overwrites the buffer that kernel read.
+      e = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
+      if (e == cudaSuccess)
+        e = launch_step_tmat(c->tmat_shape, c->h, c->maps, c->d_tunits, c->n_tunits, n, c->tmat_ctas, c->d_err,
+                             c->stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_t, 0);
+      if (e == cudaSuccess) e = cudaEventRecord(c->ev_t, c->stream);
       if (e == cudaSuccess) {
         ++c->launches;
-        e = launch_step_tma(c->tma_shape, c->h, c->d_eunits, c->n_eunits, n, c->grid_warps, c->d_err, c->stream);
+        e = launch_step_tma(c->tma_shape, c->h, c->d_eunits, c->n_eunits, n, c->grid_warps, c->d_err, c->side);
       }
+      if (e == cudaSuccess) e = cudaEventRecord(c->ev_e, c->side);
+      // what follows on the shot stream (tracker, line probe, reads) sees the whole step
+      if (e == cudaSuccess && (c->n_rc > 0 || c->line_n > 0 || n == n_last))
+        e = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
     } else {
       e = c->tma ? launch_step_tma(c->tma_shape, c->h, c->d_units, c->n_units, n, c->grid_warps, c->d_err, c->stream)
                  : launch_step(c->h, c->d_units, c->n_units, n, c->medium, c->grid_warps, c->stream);
@@ -1120,12 +1158,19 @@ int fdtd2d_destroy(fdtd2d_ctx* c) {
   // A batch member's memory is freed behind the batch's queued kernels (no
   // wait); a single shot waits for its stream and releases it.
   if (c->stream) {
+    if (c->side) cudaStreamWaitEvent(c->stream, c->ev_e, 0);   // the side stream's last kernel
     for (void* p : c->allocs) cudaFreeAsync(p, c->stream);
   }
   if (c->stream && !c->batch) {
     cudaStreamSynchronize(c->stream);
     cudaStreamDestroy(c->stream);
   }
+  if (c->side) {
+    cudaStreamSynchronize(c->side);
+    cudaStreamDestroy(c->side);
+  }
+  for (cudaEvent_t ev : {c->ev_t, c->ev_e, c->ev_m})
+    if (ev) cudaEventDestroy(ev);
   delete c;
   return FDTD2D_OK;
 }

@@ -40,6 +40,11 @@ struct fdtd2d_ctx {
   int4* d_eunits = nullptr;   // the rest (staged kernel)
   int n_eunits = 0;
   fdtd2d::TensorMaps maps{};
+  // the CPML-band kernel runs on a second stream beside the interior one:
+  // ev_t marks the interior kernel of the last step, ev_e the CPML kernel,
+  // ev_m the shot stream's work before a run
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_t = nullptr, ev_e = nullptr, ev_m = nullptr;
   char kernel_name[96] = {0};
   // wave-front tracker and line probe
   int n_rc = 0, rc_j_cut = 0;

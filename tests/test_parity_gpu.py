@@ -124,6 +124,7 @@ def test_every_launch_shape(gpu, monkeypatch, shape):
     CPML strips fall inside the first and last bands."""
     monkeypatch.delenv("FDTD2D_KERNEL", raising=False)
     monkeypatch.setenv("FDTD2D_TMA", shape)
+    monkeypatch.setenv("FDTD2D_TMAT", "0")   # the one-row kernel on the whole grid
     for nx, ny, P in ((1100, 90, 9), (203, 157, 7)):
         assert _random_state_case(gpu, nx, ny, P) == f"step_tma_kernel<{shape}>"
 
@@ -178,7 +179,8 @@ def test_autotuned_shape_and_deep_cpml(gpu, monkeypatch):
     CPML deeper than the staged kernel's x-strip slots streams instead."""
     monkeypatch.delenv("FDTD2D_KERNEL", raising=False)
     monkeypatch.delenv("FDTD2D_TMA", raising=False)
-    assert _random_state_case(gpu, 700, 130, 16).startswith("step_tma_kernel<")
+    assert _random_state_case(gpu, 700, 130, 16).startswith(("step_tma_kernel<", "step_tmat_kernel<"))
+    _random_state_case(gpu, 1600, 140, 12)   # interior bands: the tensor pair competes in the timing
     assert _random_state_case(gpu, 300, 260, 121, steps=20) == "step_stream_kernel<0>"
 
 
