@@ -307,7 +307,6 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   }
   const DevShot& h = c->h;
   const int nx = c->nx, ny = c->ny, P = c->npml;
-  const int b1 = tma_band_cols(c->tma_shape);
   if (!c->side) {
     cudaError_t e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_t, cudaEventDisableTiming);
@@ -337,59 +336,65 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
                                               c->stream); });
     if (best < 0) best = 1e30f;
   }
-  int best_k = -1;
+  int best_k = -1, best_q = -1, best_ectas = 0;
   std::vector<int4> best_t, best_e;
   TensorMaps best_m{};
   for (int k = 0; k < tmat_shape_count(); ++k) {
     if (forced >= 0 && k != forced) continue;
-    const int bt = tmat_band_cols(k), big = std::max(bt, b1), R = tmat_rows(k);
-    const int ci0 = (P + big - 1) / big * big, ci1 = (nx - P) / big * big;
-    if (ci1 - ci0 < bt || ny - 2 * P < 4 * R) continue;
+    const int bt = tmat_band_cols(k), R = tmat_rows(k);
     TensorMaps maps{};
-    if (!encode_maps(h, nx, ny, tmat_box_cols(k), R, &maps)) continue;
+    if (ny - 2 * P < 4 * R || !encode_maps(h, nx, ny, tmat_box_cols(k), R, &maps)) continue;
     const int tctas = tmat_resident_ctas(k, h.store, device);
-    std::vector<int4> tu, eu;
-    const int nbt = (ci1 - ci0) / bt;
-    add_units(tu, ci0, ci1, bt, P, ny - P, std::min(std::max(1, tctas / nbt), (ny - 2 * P) / (2 * R)));
-    // the staged kernel: edge bands over all rows, interior bands over the CPML rows
-    const int neb = (ci0 + b1 - 1) / b1 + (nx - ci1 + b1 - 1) / b1;
-    const int se = std::min(std::max(1, c->grid_warps / std::max(1, neb)), std::max(1, (ny - 1) / 8));
-    add_units(eu, 0, ci0, b1, 0, ny - 1, se);
-    add_units(eu, ci1, nx, b1, 0, ny - 1, se);
-    add_units(eu, ci0, ci1, b1, 0, P, 1);
-    add_units(eu, ci0, ci1, b1, ny - P, ny - 1, 1);
-    int4 *dt = nullptr, *de = nullptr;
-    cudaError_t e = cudaMallocAsync(&dt, tu.size() * sizeof(int4), c->stream);
-    if (e == cudaSuccess) e = cudaMallocAsync(&de, eu.size() * sizeof(int4), c->stream);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(dt, tu.data(), tu.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(de, eu.data(), eu.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
-    float ms = -1.f;
-    if (e == cudaSuccess) e = cudaEventRecord(c->ev_m, c->stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_m, 0);
-    // one trial step as fdtd2d_run issues it: the two kernels on two streams
-    if (e == cudaSuccess)
-      ms = timed([&] {
-        cudaError_t x = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
-        if (x == cudaSuccess) x = launch_step_tmat(k, t, maps, dt, (int)tu.size(), n1, tctas, c->d_err, c->stream);
-        if (x == cudaSuccess) x = cudaStreamWaitEvent(c->side, c->ev_t, 0);
-        if (x == cudaSuccess) x = cudaEventRecord(c->ev_t, c->stream);
-        if (x == cudaSuccess)
-          x = launch_step_tma(c->tma_shape, t, de, (int)eu.size(), n1, c->grid_warps, c->d_err, c->side);
-        if (x == cudaSuccess) x = cudaEventRecord(c->ev_e, c->side);
-        if (x == cudaSuccess) x = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
-        return x;
-      });
-    if (dt) cudaFreeAsync(dt, c->stream);
-    if (de) cudaFreeAsync(de, c->stream);
-    if (ms >= 0 && ms < best) {
-      best = ms;
-      best_k = k;
-      best_t = tu;
-      best_e = eu;
-      best_m = maps;
-      c->tmat_ctas = tctas;
+    // every one-row shape is a candidate for the CPML bands and rows
+    for (int q = 0; q < tma_shape_count(); ++q) {
+      const int b1 = tma_band_cols(q), big = std::max(bt, b1);
+      const int ci0 = (P + big - 1) / big * big, ci1 = (nx - P) / big * big;
+      if (ci1 - ci0 < bt) continue;
+      const int ectas = tma_resident_ctas(q, P, h.store, device);
+      std::vector<int4> tu, eu;
+      const int nbt = (ci1 - ci0) / bt;
+      add_units(tu, ci0, ci1, bt, P, ny - P, std::min(std::max(1, tctas / nbt), (ny - 2 * P) / (2 * R)));
+      // the one-row kernel: edge bands over all rows, interior bands over the CPML rows
+      const int neb = (ci0 + b1 - 1) / b1 + (nx - ci1 + b1 - 1) / b1;
+      const int se = std::min(std::max(1, ectas / std::max(1, neb)), std::max(1, (ny - 1) / 8));
+      add_units(eu, 0, ci0, b1, 0, ny - 1, se);
+      add_units(eu, ci1, nx, b1, 0, ny - 1, se);
+      add_units(eu, ci0, ci1, b1, 0, P, 1);
+      add_units(eu, ci0, ci1, b1, ny - P, ny - 1, 1);
+      int4 *dt = nullptr, *de = nullptr;
+      cudaError_t e = cudaMallocAsync(&dt, tu.size() * sizeof(int4), c->stream);
+      if (e == cudaSuccess) e = cudaMallocAsync(&de, eu.size() * sizeof(int4), c->stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dt, tu.data(), tu.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(de, eu.data(), eu.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
+      float ms = -1.f;
+      if (e == cudaSuccess) e = cudaEventRecord(c->ev_m, c->stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_m, 0);
+      // one trial step as fdtd2d_run issues it: the two kernels on two streams
+      if (e == cudaSuccess)
+        ms = timed([&] {
+          cudaError_t x = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
+          if (x == cudaSuccess) x = launch_step_tmat(k, t, maps, dt, (int)tu.size(), n1, tctas, c->d_err, c->stream);
+          if (x == cudaSuccess) x = cudaStreamWaitEvent(c->side, c->ev_t, 0);
+          if (x == cudaSuccess) x = cudaEventRecord(c->ev_t, c->stream);
+          if (x == cudaSuccess) x = launch_step_tma(q, t, de, (int)eu.size(), n1, ectas, c->d_err, c->side);
+          if (x == cudaSuccess) x = cudaEventRecord(c->ev_e, c->side);
+          if (x == cudaSuccess) x = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
+          return x;
+        });
+      if (dt) cudaFreeAsync(dt, c->stream);
+      if (de) cudaFreeAsync(de, c->stream);
+      if (ms >= 0 && ms < best) {
+        best = ms;
+        best_k = k;
+        best_q = q;
+        best_ectas = ectas;
+        best_t = tu;
+        best_e = eu;
+        best_m = maps;
+        c->tmat_ctas = tctas;
+      }
     }
   }
   cudaEventDestroy(e0);
@@ -408,6 +413,8 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   if (e != cudaSuccess) return fail_cuda(c, e);
   c->tmat = true;
   c->tmat_shape = best_k;
+  c->tma_shape = best_q;          // the one-row kernel's shape on the CPML bands and rows
+  c->grid_warps = best_ectas;
   c->n_tunits = (int)best_t.size();
   c->n_eunits = (int)best_e.size();
   c->maps = best_m;
