@@ -346,9 +346,15 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
     if (ny - 2 * P < 4 * R || !encode_maps(h, nx, ny, tmat_box_cols(k), R, &maps)) continue;
     const int tctas = tmat_resident_ctas(k, h.store, device);
     // every one-row shape is a candidate for the CPML bands and rows
+    // (FDTD2D_TMA=W,ST forces one)
+    const int q_forced = tma_shape_parse(std::getenv("FDTD2D_TMA"));
     for (int q = 0; q < tma_shape_count(); ++q) {
-      const int b1 = tma_band_cols(q), big = std::max(bt, b1);
-      const int ci0 = (P + big - 1) / big * big, ci1 = (nx - P) / big * big;
+      if (q_forced >= 0 && q != q_forced) continue;
+      // interior columns [ci0, ci1): ci0 the first multiple of the one-row
+      // band at or past the CPML, then whole tensor bands up to nx - P
+      const int b1 = tma_band_cols(q);
+      const int ci0 = (P + b1 - 1) / b1 * b1;
+      const int ci1 = ci0 + std::max(0, (nx - P - ci0) / bt) * bt;
       if (ci1 - ci0 < bt) continue;
       const int ectas = tma_resident_ctas(q, P, h.store, device);
       std::vector<int4> tu, eu;

@@ -547,7 +547,8 @@ constexpr ShapeEntry entry() {
 
 // Compiled launch shapes; the first is the default.
 const ShapeEntry kShapes[] = {entry<4, 3>(), entry<4, 2>(), entry<4, 4>(), entry<4, 6>(),
-                              entry<8, 2>(), entry<8, 3>(), entry<8, 4>(), entry<2, 4>(), entry<2, 6>()};
+                              entry<8, 2>(), entry<8, 3>(), entry<8, 4>(), entry<2, 4>(), entry<2, 6>(),
+                              entry<2, 2>(), entry<2, 3>()};
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
 }  // namespace
