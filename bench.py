@@ -163,10 +163,11 @@ def measured_peaks() -> dict:
     return {}
 
 
-def profile_traffic() -> float | None:
-    """DRAM bytes per launch of the step kernel on this workload, from the
-    committed ncu summary (scaled to the full launch as stated there)."""
-    f = ROOT / "profiles" / "step_tma_8192_production.md"
+def profile_traffic(kernel: str) -> float | None:
+    """DRAM bytes per step of the step kernel(s) on this workload, from the
+    committed ncu summary of that kernel family."""
+    name = "step_tmat_8192_production.md" if kernel.startswith("step_tmat") else "step_tma_8192_production.md"
+    f = ROOT / "profiles" / name
     if not f.exists():
         return None
     m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read_text())
@@ -504,7 +505,7 @@ def run_ours(args, world, rank, local, dist) -> None:
     peak_src = "measured"
     if not peak:
         peak, peak_src = 6800.0, "fallback"
-    traffic = profile_traffic() if (store == 0 and args.size == 8192) else None
+    traffic = profile_traffic(kernel) if (store == 0 and args.size == 8192) else None
 
     # end to end through the C ABI with host buffers
     e2e = None
