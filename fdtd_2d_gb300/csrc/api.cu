@@ -110,7 +110,7 @@ bool encode_maps(const DevShot& h, int nx, int ny, int bx, int rows, TensorMaps*
   const cuuint32_t est[3] = {1, 1, 1};
   for (int b = 0; b < 2; ++b) {
     const cuuint64_t dims3[3] = {(cuuint64_t)nx, (cuuint64_t)ny, 3};
-    const cuuint64_t str3[2] = {(cuuint64_t)h.pitch * es, (cuuint64_t)2 * h.cells * es};
+    const cuuint64_t str3[2] = {(cuuint64_t)h.pitch * es, (cuuint64_t)h.cells * es};
     const cuuint32_t box3[3] = {(cuuint32_t)bx, (cuuint32_t)rows, 3};
     void* hx = es == 4 ? (void*)field_ptr_t<float>(h, kHx, b) : (void*)field_ptr_t<uint16_t>(h, kHx, b);
     if (enc(&m->hj[b], dt, 3, hx, dims3, str3, box3, est, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -507,7 +507,12 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
   h.store = s->storage;
   for (int a = 0; a < 5; ++a) h.sc[a] = h.isc[a] = 1.f;
   const int es = store_bytes(h.store);
-  CK(dalloc(c, &h.fld, (size_t)cells * 8 * es / 4));
+  {
+    float* slab = nullptr;
+    CK(dalloc(c, &slab, (size_t)cells * 8 * es / 4));
+    h.fb[0] = slab;
+    h.fb[1] = reinterpret_cast<float*>(reinterpret_cast<char*>(slab) + (size_t)cells * 4 * es);
+  }
   h.o_ezy = (int64_t)2 * (P - 1) * pitch;
   h.o_hyx = h.o_ezy + (int64_t)2 * P * pitch;
   h.o_ezx = h.o_hyx + (int64_t)2 * ny * P;

@@ -43,11 +43,13 @@ struct DevShot {
   const MatE* mat_e;          // [256]
   const MatH* mat_h;          // [256]
 
-  // Field slab [4 fields (Ez, Hx, Hy, Jz)][2 ping-pong buffers][cells]: each
-  // buffer holds ny rows of `pitch` floats; column 0 of row 0 sits kMargin
-  // floats into the buffer, so every row has a zero margin on both sides that
-  // bulk row copies may read as halo.  field_ptr() points at column 0.
-  float* fld;
+  // Field buffers: fb[b] holds [4 fields (Ez, Hx, Hy, Jz)][cells]; each
+  // field array holds ny rows of `pitch` elements; column 0 of row 0 sits
+  // kMargin elements into it, so every row has a zero margin on both sides
+  // that bulk row copies may read as halo.  field_ptr() points at column 0.
+  // Step n reads fb[(n-1)&1] and writes fb[n&1]; a launch may be given a
+  // descriptor whose fb points elsewhere.
+  float* fb[2];
   int64_t cells;
   // CPML psi slab [2 ping-pong buffers][psi_buf]; within a buffer (side s = 0
   // low edge, 1 high edge):
@@ -81,7 +83,7 @@ struct DevShot {
   // a cell update with reference thread index l >= cov[k] is skipped.
   long long cov[8];
   // Field storage (FDTD2D_STORE_*): Ez, Hx, Hy, Jz and the drive map hold
-  // F32, F16 or BF16 elements (fld and kp point at elements of that type);
+  // F32, F16 or BF16 elements (fb and kp point at elements of that type);
   // stored = value * isc[a], value = stored * sc[a], sc a power of two per
   // array a in (Ez, Hx, Hy, Jz, drive).  Arithmetic is FP32 throughout.
   int store;
@@ -94,13 +96,13 @@ enum FieldId : int { kEz = 0, kHx = 1, kHy = 2, kJz = 3 };
 constexpr int kMargin = 32;
 
 __host__ __device__ inline float* field_ptr(const DevShot& S, int f, int b) {
-  return S.fld + (int64_t)(2 * f + b) * S.cells + kMargin;
+  return S.fb[b] + (int64_t)f * S.cells + kMargin;
 }
 
 // The same for storage element type T (F32 storage: T = float).
 template <class T>
 __host__ __device__ inline T* field_ptr_t(const DevShot& S, int f, int b) {
-  return reinterpret_cast<T*>(S.fld) + (int64_t)(2 * f + b) * S.cells + kMargin;
+  return reinterpret_cast<T*>(S.fb[b]) + (int64_t)f * S.cells + kMargin;
 }
 
 // Bytes per stored field element.
