@@ -108,7 +108,8 @@ bool encode_maps(const DevShot& h, int nx, int ny, int bx, int rows, TensorMaps*
                                  : h.store == FDTD2D_STORE_F16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
                                                                : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
   const cuuint32_t est[3] = {1, 1, 1};
-  for (int b = 0; b < 2; ++b) {
+  for (int b = 0; b < 3; ++b) {
+    if (!h.fb[b]) continue;
     const cuuint64_t dims3[3] = {(cuuint64_t)nx, (cuuint64_t)ny, 3};
     const cuuint64_t str3[2] = {(cuuint64_t)h.pitch * es, (cuuint64_t)h.cells * es};
     const cuuint32_t box3[3] = {(cuuint32_t)bx, (cuuint32_t)rows, 3};
@@ -285,12 +286,54 @@ int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
 
 namespace {
 
+// Field-buffer slots a and b of a descriptor and its tensor maps traded.
+void swap_slots(DevShot& h, TensorMaps& m, int a, int b) {
+  std::swap(h.fb[a], h.fb[b]);
+  std::swap(m.hj[a], m.hj[b]);
+  std::swap(m.e[a], m.e[b]);
+}
+
+// Steps n and n+1 on the two-step path.  The interior kernel (shot stream)
+// runs beside the CPML-band kernel's step n (side stream); the band kernel's
+// step n+1 follows once the interior kernel has written the ring of state n
+// it reads.  h and m come back with state n+1 in slot (n+1)&1 and the
+// buffer of state n-1 moved to slot 2.  Each kernel waits for the previous
+// work that read what it overwrites: the interior kernel for the side
+// stream's last kernel (ev_e), the band kernel's step n for the previous
+// interior kernel (ev_t as recorded before this call).
+cudaError_t issue_pair(fdtd2d_ctx* c, int k, int q, DevShot& h, TensorMaps& m, const int4* tu, int ntu, int tctas,
+                       const int4* eu, int neu, int ectas, int n) {
+  const int a = (n - 1) & 1, b = n & 1;
+  DevShot t = h;
+  TensorMaps tm = m;
+  // the two-step kernel's slots: 0 state n-1, 1 state n (ring), 2 state n+1
+  t.fb[0] = h.fb[a];
+  t.fb[1] = h.fb[b];
+  tm.hj[0] = m.hj[a];
+  tm.hj[1] = m.hj[b];
+  tm.e[0] = m.e[a];
+  tm.e[1] = m.e[b];
+  cudaError_t x = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
+  if (x == cudaSuccess) x = launch_step_tmat2(k, t, tm, tu, ntu, n, tctas, c->d_err, c->stream);
+  if (x == cudaSuccess) x = cudaStreamWaitEvent(c->side, c->ev_t, 0);
+  if (x == cudaSuccess) x = cudaEventRecord(c->ev_t, c->stream);
+  if (x == cudaSuccess) x = launch_step_tma(q, h, eu, neu, n, ectas, c->d_err, c->side);
+  if (x == cudaSuccess) x = cudaStreamWaitEvent(c->side, c->ev_t, 0);
+  swap_slots(h, m, a, 2);
+  if (x == cudaSuccess) x = launch_step_tma(q, h, eu, neu, n + 1, ectas, c->d_err, c->side);
+  if (x == cudaSuccess) x = cudaEventRecord(c->ev_e, c->side);
+  return x;
+}
+
 // Multi-row tensor path (step_tmat.cu) for the interior of the shot, beside
 // the staged kernel on the CPML bands and rows.  Times every tensor shape that
 // fits the grid (tensor kernel on the interior units + staged kernel on the
-// rest, one step with traces and DFT off, re-run idempotently) against the
-// staged kernel alone, and keeps the faster.  FDTD2D_TMAT=0 leaves it off,
-// FDTD2D_TMAT=W,R,ST forces a shape.
+// rest, issued as fdtd2d_run issues them, traces and DFT off, re-run
+// idempotently) against the staged kernel alone, and keeps the fastest per
+// step.  Each tensor shape is tried in its one-step form and in its two-step
+// form (two time steps per pass over the fields; a third field buffer).
+// FDTD2D_TMAT=0 leaves the tensor path off, FDTD2D_TMAT=W,R,ST forces a
+// shape; FDTD2D_TB=0 leaves the two-step form out, FDTD2D_TB=1 keeps only it.
 int setup_tmat(fdtd2d_ctx* c, int device) {
   const char* env = std::getenv("FDTD2D_TMAT");
   if (env && std::strcmp(env, "0") == 0) return FDTD2D_OK;
@@ -305,13 +348,29 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
         if (a == w && b == r && d == st) forced = k;
       }
   }
-  const DevShot& h = c->h;
+  const char* tbe = std::getenv("FDTD2D_TB");
+  const int tb_mode = tbe ? std::atoi(tbe) : -1;   // -1 both forms, 0 one-step only, 1 two-step only
+  DevShot& h = c->h;
   const int nx = c->nx, ny = c->ny, P = c->npml;
   if (!c->side) {
     cudaError_t e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_t, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_e, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_m, cudaEventDisableTiming);
+    if (e != cudaSuccess) return fail_cuda(c, e);
+  }
+  // Two-step form: a third field buffer, a copy of the first (cells that no
+  // kernel writes keep their values in every buffer), and a scratch psi slab
+  // for the trials (a trial pair's second step writes psi buffer 0).
+  const bool try2 = tb_mode != 0 && c->n_steps >= 2 && ny - 2 * P - 2 >= 8;
+  float* psi_trial = nullptr;
+  const size_t psi_floats = (size_t)h.psi_buf * 2 + 1024;
+  if (try2) {
+    const size_t fbytes = (size_t)h.cells * 4 * store_bytes(h.store);
+    cudaError_t e = dalloc(c, &h.fb[2], fbytes / 4);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.fb[2], h.fb[0], fbytes, cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync(&psi_trial, psi_floats * 4, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(psi_trial, h.psi, psi_floats * 4, cudaMemcpyDeviceToDevice, c->stream);
     if (e != cudaSuccess) return fail_cuda(c, e);
   }
   DevShot t = h;
@@ -330,81 +389,118 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
     return e == cudaSuccess ? ms : -1.f;
   };
   const int n1 = t.base_n + 1;
-  float best = 1e30f;
-  if (forced < 0) {
+  float best = 1e30f;   // per step
+  if (forced < 0 && tb_mode != 1) {
     best = timed([&] { return launch_step_tma(c->tma_shape, t, c->d_units, c->n_units, n1, c->grid_warps, c->d_err,
                                               c->stream); });
     if (best < 0) best = 1e30f;
   }
-  int best_k = -1, best_q = -1, best_ectas = 0;
+  int best_k = -1, best_q = -1, best_ectas = 0, best_l = 1;
   std::vector<int4> best_t, best_e;
   TensorMaps best_m{};
   for (int k = 0; k < tmat_shape_count(); ++k) {
     if (forced >= 0 && k != forced) continue;
     const int bt = tmat_band_cols(k), R = tmat_rows(k);
     TensorMaps maps{};
-    if (ny - 2 * P < 4 * R || !encode_maps(h, nx, ny, tmat_box_cols(k), R, &maps)) continue;
-    const int tctas = tmat_resident_ctas(k, h.store, device);
+    if (ny - 2 * P < 4 * R + 2 || !encode_maps(h, nx, ny, tmat_box_cols(k), R, &maps)) continue;
     // every one-row shape is a candidate for the CPML bands and rows
     // (FDTD2D_TMA=W,ST forces one)
     const int q_forced = tma_shape_parse(std::getenv("FDTD2D_TMA"));
-    for (int q = 0; q < tma_shape_count(); ++q) {
-      if (q_forced >= 0 && q != q_forced) continue;
-      // interior columns [ci0, ci1): ci0 the first multiple of the one-row
-      // band at or past the CPML, then whole tensor bands up to nx - P
-      const int b1 = tma_band_cols(q);
-      const int ci0 = (P + b1 - 1) / b1 * b1;
-      const int ci1 = ci0 + std::max(0, (nx - P - ci0) / bt) * bt;
-      if (ci1 - ci0 < bt) continue;
-      const int ectas = tma_resident_ctas(q, P, h.store, device);
-      std::vector<int4> tu, eu;
-      const int nbt = (ci1 - ci0) / bt;
-      add_units(tu, ci0, ci1, bt, P, ny - P, std::min(std::max(1, tctas / nbt), (ny - 2 * P) / (2 * R)));
-      // the one-row kernel: edge bands over all rows, interior bands over the CPML rows
-      const int neb = (ci0 + b1 - 1) / b1 + (nx - ci1 + b1 - 1) / b1;
-      const int se = std::min(std::max(1, ectas / std::max(1, neb)), std::max(1, (ny - 1) / 8));
-      add_units(eu, 0, ci0, b1, 0, ny - 1, se);
-      add_units(eu, ci1, nx, b1, 0, ny - 1, se);
-      add_units(eu, ci0, ci1, b1, 0, P, 1);
-      add_units(eu, ci0, ci1, b1, ny - P, ny - 1, 1);
-      int4 *dt = nullptr, *de = nullptr;
-      cudaError_t e = cudaMallocAsync(&dt, tu.size() * sizeof(int4), c->stream);
-      if (e == cudaSuccess) e = cudaMallocAsync(&de, eu.size() * sizeof(int4), c->stream);
-      if (e == cudaSuccess)
-        e = cudaMemcpyAsync(dt, tu.data(), tu.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
-      if (e == cudaSuccess)
-        e = cudaMemcpyAsync(de, eu.data(), eu.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
-      float ms = -1.f;
-      if (e == cudaSuccess) e = cudaEventRecord(c->ev_m, c->stream);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_m, 0);
-      // one trial step as fdtd2d_run issues it: the two kernels on two streams
-      if (e == cudaSuccess)
-        ms = timed([&] {
-          cudaError_t x = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
-          if (x == cudaSuccess) x = launch_step_tmat(k, t, maps, dt, (int)tu.size(), n1, tctas, c->d_err, c->stream);
-          if (x == cudaSuccess) x = cudaStreamWaitEvent(c->side, c->ev_t, 0);
-          if (x == cudaSuccess) x = cudaEventRecord(c->ev_t, c->stream);
-          if (x == cudaSuccess) x = launch_step_tma(q, t, de, (int)eu.size(), n1, ectas, c->d_err, c->side);
-          if (x == cudaSuccess) x = cudaEventRecord(c->ev_e, c->side);
-          if (x == cudaSuccess) x = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
-          return x;
-        });
-      if (dt) cudaFreeAsync(dt, c->stream);
-      if (de) cudaFreeAsync(de, c->stream);
-      if (ms >= 0 && ms < best) {
-        best = ms;
-        best_k = k;
-        best_q = q;
-        best_ectas = ectas;
-        best_t = tu;
-        best_e = eu;
-        best_m = maps;
-        c->tmat_ctas = tctas;
+    // both forms' launch attributes are set here: the two-step path also
+    // runs single steps (an odd step, a step the line probe reads)
+    const int tctas1 = tmat_resident_ctas(k, h.store, device);
+    const int tctas2 = try2 ? tmat2_resident_ctas(k, h.store, device) : 0;
+    for (int lv = 1; lv <= 2; ++lv) {
+      if ((lv == 2 && !try2) || (lv == 1 && tb_mode == 1)) continue;
+      const int tctas = lv == 1 ? tctas1 : tctas2;
+      // interior region: rows [ri0, ri1), columns [ci0, ci1) with ci0 the
+      // first multiple of the one-row band at or past the CPML (two-step
+      // form: one cell further in on every side), then whole tensor bands
+      const int ri0 = lv == 1 ? P : P + 1, ri1 = ny - ri0;
+      for (int q = 0; q < tma_shape_count(); ++q) {
+        if (q_forced >= 0 && q != q_forced) continue;
+        const int b1 = tma_band_cols(q);
+        const int ci0 = (ri0 + b1 - 1) / b1 * b1;
+        const int ci1 = ci0 + std::max(0, (nx - ri0 - ci0) / bt) * bt;
+        if (ci1 - ci0 < bt) continue;
+        const int ectas = tma_resident_ctas(q, P, h.store, device);
+        std::vector<int4> tu, eu;
+        const int nbt = (ci1 - ci0) / bt;
+        add_units(tu, ci0, ci1, bt, ri0, ri1, std::min(std::max(1, tctas / nbt), (ri1 - ri0) / (2 * R)));
+        if (lv == 2)
+          for (int4& u : tu)
+            u.x = (u.z == ri0 ? kRingTop : 0) | (u.w == ri1 ? kRingBottom : 0) | (u.y == ci0 ? kRingLeft : 0) |
+                  (u.y + bt == ci1 ? kRingRight : 0);
+        // the one-row kernel: edge bands over all rows, interior bands over the CPML rows
+        const int neb = (ci0 + b1 - 1) / b1 + (nx - ci1 + b1 - 1) / b1;
+        const int se = std::min(std::max(1, ectas / std::max(1, neb)), std::max(1, (ny - 1) / 8));
+        add_units(eu, 0, ci0, b1, 0, ny - 1, se);
+        add_units(eu, ci1, nx, b1, 0, ny - 1, se);
+        add_units(eu, ci0, ci1, b1, 0, ri0, 1);
+        add_units(eu, ci0, ci1, b1, ri1, ny - 1, 1);
+        int4 *dt = nullptr, *de = nullptr;
+        cudaError_t e = cudaMallocAsync(&dt, tu.size() * sizeof(int4), c->stream);
+        if (e == cudaSuccess) e = cudaMallocAsync(&de, eu.size() * sizeof(int4), c->stream);
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(dt, tu.data(), tu.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(de, eu.data(), eu.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
+        float ms = -1.f;
+        if (e == cudaSuccess) e = cudaEventRecord(c->ev_m, c->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_m, 0);
+        // one trial step (pair) as fdtd2d_run issues it: the two kernels on two streams
+        if (e == cudaSuccess && lv == 1) {
+          ms = timed([&] {
+            cudaError_t x = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
+            if (x == cudaSuccess) x = launch_step_tmat(k, t, maps, dt, (int)tu.size(), n1, tctas, c->d_err, c->stream);
+            if (x == cudaSuccess) x = cudaStreamWaitEvent(c->side, c->ev_t, 0);
+            if (x == cudaSuccess) x = cudaEventRecord(c->ev_t, c->stream);
+            if (x == cudaSuccess) x = launch_step_tma(q, t, de, (int)eu.size(), n1, ectas, c->d_err, c->side);
+            if (x == cudaSuccess) x = cudaEventRecord(c->ev_e, c->side);
+            if (x == cudaSuccess) x = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
+            return x;
+          });
+        } else if (e == cudaSuccess) {
+          // slots of the trial descriptor: state 0 in slot 0 stays untouched
+          // (the pair writes slots 1 and 2), psi goes to the scratch slab
+          ms = timed([&] {
+            DevShot t2 = t;
+            t2.psi = psi_trial;
+            TensorMaps m2 = maps;
+            cudaError_t x = issue_pair(c, k, q, t2, m2, dt, (int)tu.size(), tctas, de, (int)eu.size(), ectas, n1);
+            if (x == cudaSuccess) x = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
+            return x;
+          });
+          if (ms >= 0) ms *= 0.5f;
+        }
+        if (dt) cudaFreeAsync(dt, c->stream);
+        if (de) cudaFreeAsync(de, c->stream);
+        if (ms >= 0 && ms < best) {
+          best = ms;
+          best_k = k;
+          best_q = q;
+          best_l = lv;
+          best_ectas = ectas;
+          best_t = tu;
+          best_e = eu;
+          best_m = maps;
+          c->tmat_ctas = tctas1;
+          c->tmat2_ctas = tctas2;
+        }
       }
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (psi_trial) cudaFreeAsync(psi_trial, c->stream);
+  if (h.fb[2] && !(best_k >= 0 && best_l == 2)) {
+    // the two-step form lost: give its buffer back
+    cudaFreeAsync(h.fb[2], c->stream);
+    c->allocs.erase(std::find(c->allocs.begin(), c->allocs.end(), (void*)h.fb[2]));
+    h.fb[2] = nullptr;
+    std::memset(&best_m.hj[2], 0, sizeof best_m.hj[2]);
+    std::memset(&best_m.e[2], 0, sizeof best_m.e[2]);
+  }
   int derr = 0;
   if (cudaMemcpy(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return FDTD2D_ERR_CUDA;
   if (derr != kErrNone) return FDTD2D_ERR_TIMEOUT;
@@ -418,6 +514,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return fail_cuda(c, e);
   c->tmat = true;
+  c->tb = best_l == 2;
   c->tmat_shape = best_k;
   c->tma_shape = best_q;          // the one-row kernel's shape on the CPML bands and rows
   c->grid_warps = best_ectas;
@@ -428,7 +525,8 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   tmat_shape_dims(best_k, &w, &r, &st);
   char one[48];
   tma_shape_name(c->tma_shape, "step_tma_kernel", one, sizeof one);
-  std::snprintf(c->kernel_name, sizeof c->kernel_name, "step_tmat_kernel<%d,%d,%d>+%s", w, r, st, one);
+  std::snprintf(c->kernel_name, sizeof c->kernel_name, "%s<%d,%d,%d>+%s", c->tb ? "step_tmat2_kernel" : "step_tmat_kernel",
+                w, r, st, one);
   return FDTD2D_OK;
 }
 
@@ -829,6 +927,18 @@ int fdtd2d_run(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
   }
   for (int32_t n = n_first; n <= n_last; ++n) {
     cudaError_t e;
+    // Two steps per pass where nothing reads the fields between them (the
+    // tracker and the line probe read every step's Ez).
+    if (c->tb && n < n_last && c->n_rc == 0 &&
+        !(c->line_n > 0 && n + 1 >= c->line_first && n <= c->line_last)) {
+      e = issue_pair(c, c->tmat_shape, c->tma_shape, c->h, c->maps, c->d_tunits, c->n_tunits, c->tmat2_ctas,
+                     c->d_eunits, c->n_eunits, c->grid_warps, n);
+      if (e == cudaSuccess && n + 1 == n_last) e = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
+      if (e != cudaSuccess) return fail_cuda(c, e);
+      c->launches += 3;
+      c->step = ++n;
+      continue;
+    }
     if (c->tmat) {
       // Interior on the multi-row tensor kernel (shot stream), CPML bands and
       // rows on the staged kernel (side stream), both kernels of a step at
@@ -1106,7 +1216,8 @@ int read_field16(fdtd2d_ctx* c, int which, float* host) {
 int write_field16(fdtd2d_ctx* c, int which, const float* host) {
   cudaSetDevice(c->device);
   cudaError_t e = cudaStreamSynchronize(c->stream);
-  for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+  for (int b = 0; b < 3 && e == cudaSuccess; ++b) {
+    if (!c->h.fb[b]) continue;
     View16 v;
     if (!view16(c, which, b, &v)) return FDTD2D_ERR_INVALID;
     std::vector<uint16_t> buf((size_t)v.rows * v.cols);
@@ -1139,7 +1250,9 @@ int fdtd2d_write_field(fdtd2d_ctx* c, int which, const float* host) {
   if (c->h.store != FDTD2D_STORE_F32 && which <= FDTD2D_FIELD_JZ) return write_field16(c, which, host);
   cudaSetDevice(c->device);
   cudaError_t e = cudaStreamSynchronize(c->stream);
-  for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+  for (int b = 0; b < 3 && e == cudaSuccess; ++b) {
+    if (which <= FDTD2D_FIELD_JZ && !c->h.fb[b]) continue;
+    if (which > FDTD2D_FIELD_JZ && b == 2) break;   // psi: two buffers
     FieldView v;
     if (!field_view(c, which, b, &v)) return FDTD2D_ERR_INVALID;
     e = cudaMemcpy2D(v.base, v.dpitch * 4, host, v.hpitch * 4, (size_t)v.cols * 4, v.rows,

@@ -34,7 +34,8 @@ struct fdtd2d_ctx {
   // multi-row tensor path for the interior (step_tmat.cu) beside the staged
   // kernel on the CPML bands and rows
   bool tmat = false;
-  int tmat_shape = 0, tmat_ctas = 0;
+  bool tb = false;            // its two-step form (third field buffer h.fb[2])
+  int tmat_shape = 0, tmat_ctas = 0, tmat2_ctas = 0;
   int4* d_tunits = nullptr;   // interior units (tensor kernel)
   int n_tunits = 0;
   int4* d_eunits = nullptr;   // the rest (staged kernel)

@@ -46,6 +46,7 @@ struct TCfg {
   static constexpr uint32_t kStageBytes = kKOff + kBoxes * kEBytes;
   static constexpr size_t kSmem = (size_t)ST * kStageBytes;
   static constexpr int kMinBlocks = W <= 2 ? 6 : (W <= 4 ? 4 : 2);
+  static constexpr int kMinBlocks2 = W <= 2 ? 5 : (W <= 4 ? 3 : 1);   // two-step form: more registers
   static_assert(kSpan % kBoxes == 0 && kBX % 8 == 0 && kBX <= 256, "box tiling of the staged span");
 };
 
@@ -285,6 +286,294 @@ __device__ void tband(const DevShot& S, const TensorMaps& M, TRing& R, int c0, i
   }
 }
 
+// Sources of step n, then its detectors when `rec`, on the cells i..i+3 of
+// one row (the point loop of tband), plus the sources at column xc, which
+// are applied to ezx: the edge column a two-step unit recomputes.
+__device__ __forceinline__ void pts2(const DevShot& S, int p0, int p1, int i, int n, bool rec, float (&ez)[4],
+                                     const float (&hx)[4], const float (&hy)[4], int xc, float& ezx) {
+  for (int p = p0; p < p1; ++p) {
+    const int4 pt = __ldg(S.pts + p);
+    if (pt.y == kPointSource && pt.x == xc) ezx = __fsub_rn(ezx, __ldg(S.src_val + (int64_t)n * S.n_src + pt.z));
+    const int kk = pt.x - i;
+    if (kk < 0 || kk > 3) continue;
+    float e = 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) if (q == kk) e = ez[q];
+    if (pt.y == kPointSource) {
+      e = __fsub_rn(e, __ldg(S.src_val + (int64_t)n * S.n_src + pt.z));
+#pragma unroll
+      for (int q = 0; q < 4; ++q) if (q == kk) ez[q] = e;
+    } else if (!rec) {
+      continue;
+    } else if (pt.y == kPointDetEz) {
+      if (S.record) S.trace[(int64_t)(n - 1) * S.n_det + pt.z] = e;
+      if (S.dft) {
+        const double2 tw = __ldg(S.twiddle + n);
+        double2 acc = S.dft[pt.z];
+        acc.x = fma((double)e, tw.x, acc.x);
+        acc.y = fma(-(double)e, tw.y, acc.y);
+        S.dft[pt.z] = acc;
+      }
+    } else {
+      float hxv = 0.f, hyv = 0.f;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) if (q == kk) { hxv = hx[q]; hyv = hy[q]; }
+      if (S.record) {
+        float* dst = S.ctrace + ((int64_t)(n - 1) * S.n_comp + pt.z) * 3;
+        dst[0] = e; dst[1] = hxv; dst[2] = hyv;
+      }
+    }
+  }
+}
+
+// Two time steps of one unit (ring, c0, j0, j1) in one pass over state n-1
+// (slot 0).  Step n runs over rows j0-1 .. j1 and, per warp, one column
+// beyond each side of its 128 (lane 0 the left one, lane 31 the right one),
+// so that step n+1 over the warp's cells [i0, i0+128) x [j0, j1) needs
+// nothing from other warps or units; step n+1 of row j-1 follows step n of
+// row j.  Step-n values reach step n+1 as a store and reload would give
+// them (Sto::rt*), and every update is the one-step kernel's, operation for
+// operation, so the two steps give the bits of two one-step launches.
+// State n+1 goes to slot 2; state n of the unit's cells on R's edge rows and
+// columns (ring flags) to slot 1, where the CPML-band kernel's step n+1
+// reads it.
+template <class C>
+__device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const int4 ud, int n, int* err) {
+  using T = typename C::Elem;
+  using St = Sto<T>;
+  const int ring = ud.x, c0 = ud.y, j0 = ud.z, j1 = ud.w;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t pitch = S.pitch;
+  const bool has_kp = S.kp != nullptr;
+  const T* __restrict__ ezo = field_ptr_t<T>(S, kEz, 0);
+  const T* __restrict__ hxo_p = field_ptr_t<T>(S, kHx, 0);
+  T* __restrict__ ezm = field_ptr_t<T>(S, kEz, 1);
+  T* __restrict__ hxm = field_ptr_t<T>(S, kHx, 1);
+  T* __restrict__ hym = field_ptr_t<T>(S, kHy, 1);
+  T* __restrict__ jzm = field_ptr_t<T>(S, kJz, 1);
+  T* __restrict__ ezw = field_ptr_t<T>(S, kEz, 2);
+  T* __restrict__ hxw = field_ptr_t<T>(S, kHx, 2);
+  T* __restrict__ hyw = field_ptr_t<T>(S, kHy, 2);
+  T* __restrict__ jzw = field_ptr_t<T>(S, kJz, 2);
+  const float sE = S.sc[0], sHx = S.sc[1], sHy = S.sc[2], sJ = S.sc[3], sK = S.sc[4];
+  const float iE = S.isc[0], iHx = S.isc[1], iHy = S.isc[2], iJ = S.isc[3];
+  const float da = S.da, db = S.db, ca = S.ca, cb = S.cb, ja = S.ja;
+
+  const int i0 = c0 + warp * kCols;            // this warp's first column
+  const int i = i0 + 4 * lane;                 // this lane's first column
+  const int xr = C::kHalo + warp * kCols + 4 * lane;   // its staged column
+  // the warp's edge column: lane 0 the one left of the warp, the other lanes
+  // (for use: lane 31) the one right of it
+  const int xc = lane == 0 ? i0 - 1 : i0 + kCols;
+  const int sx = C::kHalo + (xc - c0);         // its staged column
+  const int jb = j0 - 1;                       // first step-n row
+  const int rows_n = j1 - j0 + 2;              // step-n rows jb .. j1
+  const int nst = (rows_n + C::kRows - 1) / C::kRows;
+  const bool producer = tid == 0;
+  R.issued = R.used;
+
+  if (producer) {
+    for (int k = 0; k < nst && k < C::kStages; ++k)
+      if (!issue_stage<C>(R, M, 0, c0, jb + k * C::kRows, has_kp)) {
+        atomicExch(err, kErrWaitTimeout);
+        tdrain<C>(R);
+        return;
+      }
+  }
+
+  float dex[4], dhx[4];
+  ld4(dex, S.den_ex + i);
+  ld4(dhx, S.den_hx + i);
+  const float dhxA = __ldg(S.den_hx + xc - 1), dhxB = __ldg(S.den_hx + xc), dexE = __ldg(S.den_ex + xc);
+
+  // Row jb state: Ez_{n-1}(jb) here and at the edge column and its
+  // neighbours, Hx_n(jb - 1) recomputed (row jb - 1 >= npml - 1: no CPML).
+  float ezc[4], hxp[4];
+  St::ldg4(ezc, ezo + (int64_t)jb * pitch + i, sE);
+  float e_m = St::ldg1(ezo + (int64_t)jb * pitch + xc - 1, sE);
+  float e_0 = St::ldg1(ezo + (int64_t)jb * pitch + xc, sE);
+  float e_p = St::ldg1(ezo + (int64_t)jb * pitch + xc + 1, sE);
+  float hxe_p;                                 // Hx_n(xc, j - 1)
+  {
+    float ezp[4], hxo[4];
+    const int64_t o = (int64_t)(jb - 1) * pitch;
+    St::ldg4(ezp, ezo + o + i, sE);
+    St::ldg4(hxo, hxo_p + o + i, sHx);
+    const float dhy0 = __ldg(S.den_hy + jb - 1);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) hxp[q] = upd_h(da, hxo[q], db, ezp[q], ezc[q], dhy0);
+    hxe_p = upd_h(da, St::ldg1(hxo_p + o + xc, sHx), db, St::ldg1(ezo + o + xc, sE), e_0, dhy0);
+  }
+
+  // state n of the previous row as stored, for step n+1
+  float ez1[4], hx1[4], hy1[4], jz1[4], kp1[4], hx2p[4];
+  float eze1 = 0.f, hye1 = 0.f;                // Ez_n(xc, j-1), Hy_n(xc, j-1) as stored
+#pragma unroll
+  for (int q = 0; q < 4; ++q) ez1[q] = hx1[q] = hy1[q] = jz1[q] = kp1[q] = hx2p[q] = 0.f;
+  float dhy1 = 0.f, dey1 = 0.f;
+  int q0 = 0, q1 = 0;
+  float dhy = __ldg(S.den_hy + jb), dey = __ldg(S.den_ey + jb);
+  int p0 = __ldg(S.row_start + jb), p1 = __ldg(S.row_start + jb + 1);
+
+  for (int k = 0; k < nst; ++k) {
+    const uint32_t g = R.used;
+    const int s = g % C::kStages;
+    if (!mbar_wait(&R.full[s], (g / C::kStages) & 1)) {
+      atomicExch(err, kErrWaitTimeout);
+      if (producer) tdrain<C>(R);
+      return;
+    }
+    const unsigned char* st = R.stage + s * C::kStageBytes;
+    const int jr = jb + k * C::kRows;
+    const int rows_here = min(C::kRows, jb + rows_n - jr);
+    for (int r = 0; r < rows_here; ++r) {
+      const int j = jr + r;
+      const int jn = j + 1 <= j1 ? j + 1 : j;
+      const float dhy_n = __ldg(S.den_hy + jn), dey_n = __ldg(S.den_ey + jn);
+      const int p1_n = __ldg(S.row_start + jn + 1);
+
+      // ---- staged state n-1: row j (Ez row j+1)
+      float ezn[4], hxo[4], hyo[4], jzo[4], kp[4];
+      St::lds4(ezn, at<C>(st, 3, r, xr), sE);
+      St::lds4(hxo, at<C>(st, 0, r, xr), sHx);
+      St::lds4(hyo, at<C>(st, 1, r, xr), sHy);
+      St::lds4(jzo, at<C>(st, 2, r, xr), sJ);
+      if (has_kp) {
+        St::lds4(kp, at<C>(st, 4, r, xr), sK);
+      } else {
+        zero4(kp);
+      }
+      const float f_m = St::ld1(at<C>(st, 3, r, sx - 1), sE);
+      const float f_0 = St::ld1(at<C>(st, 3, r, sx), sE);
+      const float f_p = St::ld1(at<C>(st, 3, r, sx + 1), sE);
+      const float hyoA = St::ld1(at<C>(st, 1, r, sx - 1), sHy);
+      const float hyoB = St::ld1(at<C>(st, 1, r, sx), sHy);
+      const float hxoE = St::ld1(at<C>(st, 0, r, sx), sHx);
+      const float jzoE = St::ld1(at<C>(st, 2, r, sx), sJ);
+      const float kpE = has_kp ? St::ld1(at<C>(st, 4, r, sx), sK) : 0.f;
+
+      // ---- step n, row j
+      float hxn[4], hyn[4], jzn[4], ezs_n[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) hxn[q] = upd_h(da, hxo[q], db, ezc[q], ezn[q], dhy);
+      float ezr_k = __shfl_down_sync(0xffffffffu, ezc[0], 1);
+      if (lane == 31) ezr_k = e_0;
+      const float ezr4[4] = {ezc[1], ezc[2], ezc[3], ezr_k};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) hyn[q] = upd_h(da, hyo[q], db, ezr4[q], ezc[q], dhx[q]);
+      // edge column: Hy at xc-1 and xc, then Hx, Jz, Ez at xc
+      const float hyA = upd_h(da, hyoA, db, e_0, e_m, dhxA);
+      const float hyB = upd_h(da, hyoB, db, e_p, e_0, dhxB);
+      float hyl = __shfl_up_sync(0xffffffffu, hyn[3], 1);
+      if (lane == 0) hyl = hyB;
+      const float hxE = upd_h(da, hxoE, db, e_0, f_0, dhy);
+      const float jzE = upd_j(ja, jzoE, kpE, e_0);
+      float ezE = upd_e(ca, e_0, cb, __fsub_rn(hyB, hyA), dexE, __fsub_rn(hxe_p, hxE), dey, jzE);
+      const float hyl4[4] = {hyl, hyn[0], hyn[1], hyn[2]};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        jzn[q] = upd_j(ja, jzo[q], kp[q], ezc[q]);
+        ezs_n[q] = upd_e(ca, ezc[q], cb, __fsub_rn(hyn[q], hyl4[q]), dex[q], __fsub_rn(hxp[q], hxn[q]), dey, jzn[q]);
+      }
+      const bool own = j >= j0 && j < j1;
+      pts2(S, p0, p1, i, n, own, ezs_n, hxn, hyn, xc, ezE);
+      if (own) {
+        const int64_t o = (int64_t)j * pitch + i;
+        if (((ring & kRingTop) && j == j0) || ((ring & kRingBottom) && j == j1 - 1)) {
+          St::stcs4(ezm + o, ezs_n, iE);
+          St::stcs4(hxm + o, hxn, iHx);
+          St::stcs4(hym + o, hyn, iHy);
+          St::stcs4(jzm + o, jzn, iJ);
+        } else if ((ring & kRingLeft) && warp == 0 && lane == 0) {
+          St::st1(ezm + o, ezs_n[0], iE);
+          St::st1(hxm + o, hxn[0], iHx);
+          St::st1(hym + o, hyn[0], iHy);
+          St::st1(jzm + o, jzn[0], iJ);
+        } else if ((ring & kRingRight) && warp == C::kWarps - 1 && lane == 31) {
+          St::st1(ezm + o + 3, ezs_n[3], iE);
+          St::st1(hxm + o + 3, hxn[3], iHx);
+          St::st1(hym + o + 3, hyn[3], iHy);
+          St::st1(jzm + o + 3, jzn[3], iJ);
+        }
+      }
+
+      // ---- step n+1, row j-1 (row jb: its Hx only)
+      float ezs[4], hxs[4], hys[4], jzs[4];       // state n of row j as stored
+      St::rt4(ezs, ezs_n, iE, sE);
+      St::rt4(hxs, hxn, iHx, sHx);
+      St::rt4(hys, hyn, iHy, sHy);
+      St::rt4(jzs, jzn, iJ, sJ);
+      if (j > jb) {
+        float hx2[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) hx2[q] = upd_h(da, hx1[q], db, ez1[q], ezs[q], dhy1);
+        if (j > j0) {
+          float rk = __shfl_down_sync(0xffffffffu, ez1[0], 1);
+          if (lane == 31) rk = eze1;
+          const float er4[4] = {ez1[1], ez1[2], ez1[3], rk};
+          float hy2[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) hy2[q] = upd_h(da, hy1[q], db, er4[q], ez1[q], dhx[q]);
+          float hl = __shfl_up_sync(0xffffffffu, hy2[3], 1);
+          if (lane == 0) hl = upd_h(da, hye1, db, ez1[0], eze1, dhxB);
+          const float hl4[4] = {hl, hy2[0], hy2[1], hy2[2]};
+          float ez2[4], jz2[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            jz2[q] = upd_j(ja, jz1[q], kp1[q], ez1[q]);
+            ez2[q] = upd_e(ca, ez1[q], cb, __fsub_rn(hy2[q], hl4[q]), dex[q], __fsub_rn(hx2p[q], hx2[q]), dey1,
+                           jz2[q]);
+          }
+          float unused = 0.f;
+          pts2(S, q0, q1, i, n + 1, true, ez2, hx2, hy2, -1, unused);
+          const int64_t o = (int64_t)(j - 1) * pitch + i;
+          St::stcs4(hxw + o, hx2, iHx);
+          St::stcs4(hyw + o, hy2, iHy);
+          St::stcs4(ezw + o, ez2, iE);
+          St::stcs4(jzw + o, jz2, iJ);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) hx2p[q] = hx2[q];
+      }
+
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        ez1[q] = ezs[q];
+        hx1[q] = hxs[q];
+        hy1[q] = hys[q];
+        jz1[q] = jzs[q];
+        kp1[q] = kp[q];
+        hxp[q] = hxn[q];
+        ezc[q] = ezn[q];
+      }
+      eze1 = St::rt1(ezE, iE, sE);
+      hye1 = St::rt1(hyB, iHy, sHy);
+      hxe_p = hxE;
+      e_m = f_m;
+      e_0 = f_0;
+      e_p = f_p;
+      dhy1 = dhy;
+      dey1 = dey;
+      q0 = p0;
+      q1 = p1;
+      dhy = dhy_n;
+      dey = dey_n;
+      p0 = p1;
+      p1 = p1_n;
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&R.empty[s]);
+    R.used++;
+    if (producer && k + C::kStages < nst) {
+      if (!issue_stage<C>(R, M, 0, c0, jb + (k + C::kStages) * C::kRows, has_kp)) {
+        atomicExch(err, kErrWaitTimeout);
+        tdrain<C>(R);
+        return;
+      }
+    }
+  }
+}
+
 template <class C>
 __global__ void __launch_bounds__(C::kThreads, C::kMinBlocks)
 step_tmat_kernel(const __grid_constant__ DevShot S, const __grid_constant__ TensorMaps M,
@@ -312,6 +601,32 @@ step_tmat_kernel(const __grid_constant__ DevShot S, const __grid_constant__ Tens
   }
 }
 
+template <class C>
+__global__ void __launch_bounds__(C::kThreads, C::kMinBlocks2)
+step_tmat2_kernel(const __grid_constant__ DevShot S, const __grid_constant__ TensorMaps M,
+                  const int4* __restrict__ units, int n_units, int n_global, int* err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t full[C::kStages], empty[C::kStages];
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < C::kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], C::kWarps);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  TRing R;
+  R.stage = smem;
+  R.full = full;
+  R.empty = empty;
+  const int n = n_global - S.base_n;
+  if (n < 1 || n + 1 > S.n_steps) return;
+  for (int u = blockIdx.x; u < n_units; u += gridDim.x) {
+    tband2<C>(S, M, R, __ldg(units + u), n, err);
+    if (*(volatile int*)err) return;
+  }
+}
+
 using TKernelFn = void (*)(DevShot, TensorMaps, const int4*, int, int, int*);
 
 struct TShape {
@@ -319,6 +634,7 @@ struct TShape {
   TKernelFn fn[3];
   size_t smem[3];
   int bx;
+  TKernelFn fn2[3];   // two-step form
 };
 
 template <int W, int R, int ST>
@@ -327,7 +643,8 @@ constexpr TShape tentry() {
   using C16 = TCfg<W, R, ST, __half>;
   using CB16 = TCfg<W, R, ST, __nv_bfloat16>;
   return {W, R, ST, {step_tmat_kernel<C32>, step_tmat_kernel<C16>, step_tmat_kernel<CB16>},
-          {C32::kSmem, C16::kSmem, CB16::kSmem}, C32::kBX};
+          {C32::kSmem, C16::kSmem, CB16::kSmem}, C32::kBX,
+          {step_tmat2_kernel<C32>, step_tmat2_kernel<C16>, step_tmat2_kernel<CB16>}};
 }
 
 // Compiled shapes (warps, rows per stage, stages); the first is the default.
@@ -359,6 +676,26 @@ cudaError_t launch_step_tmat(int shape, const DevShot& shot, const TensorMaps& m
   const int st = shot.store;
   e.fn[st]<<<ctas, e.warps * 32, e.smem[st], stream>>>(shot, maps, units, n_units, n_global, err);
   return cudaGetLastError();
+}
+
+cudaError_t launch_step_tmat2(int shape, const DevShot& shot, const TensorMaps& maps, const int4* units,
+                              int n_units, int n_global, int max_ctas, int* err, cudaStream_t stream) {
+  const TShape& e = kTShapes[shape];
+  const int ctas = max_ctas < n_units ? max_ctas : n_units;
+  if (ctas <= 0) return cudaSuccess;
+  const int st = shot.store;
+  e.fn2[st]<<<ctas, e.warps * 32, e.smem[st], stream>>>(shot, maps, units, n_units, n_global, err);
+  return cudaGetLastError();
+}
+
+int tmat2_resident_ctas(int shape, int store, int device) {
+  const TShape& e = kTShapes[shape];
+  cudaFuncSetAttribute(e.fn2[store], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.smem[store]);
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, e.fn2[store], e.warps * 32, e.smem[store]);
+  if (per_sm < 1) per_sm = 1;
+  return sms * per_sm;
 }
 
 int tmat_resident_ctas(int shape, int store, int device) {

@@ -34,6 +34,12 @@ struct Sto<float> {
   __device__ static __forceinline__ void stcs4(float* p, const float (&d)[4], float) {
     __stcs(reinterpret_cast<float4*>(p), make_float4(d[0], d[1], d[2], d[3]));
   }
+  __device__ static __forceinline__ void st1(float* p, float v, float) { *p = v; }
+  // The value a store followed by a load gives back (F32: the value itself).
+  __device__ static __forceinline__ void rt4(float (&o)[4], const float (&d)[4], float, float) {
+    o[0] = d[0]; o[1] = d[1]; o[2] = d[2]; o[3] = d[3];
+  }
+  __device__ static __forceinline__ float rt1(float v, float, float) { return v; }
 };
 
 template <class T, class T2>
@@ -96,6 +102,21 @@ struct Sto16Ops {
     v.x = B::from_f2(d[0] * isc, d[1] * isc);
     v.y = B::from_f2(d[2] * isc, d[3] * isc);
     __stcs(reinterpret_cast<uint2*>(p), v);
+  }
+  __device__ static __forceinline__ void st1(T* p, float v, float isc) {
+    const uint16_t u = (uint16_t)(B::from_f2(v * isc, 0.f) & 0xffffu);
+    memcpy(p, &u, 2);
+  }
+  // stcs4 then lds4 (st1 then ld1) of the same element, without the memory
+  // round trip: the same conversions, so the same bits.
+  __device__ static __forceinline__ void rt4(float (&o)[4], const float (&d)[4], float isc, float sc) {
+    uint2 v;
+    v.x = B::from_f2(d[0] * isc, d[1] * isc);
+    v.y = B::from_f2(d[2] * isc, d[3] * isc);
+    cvt(o, v, sc);
+  }
+  __device__ static __forceinline__ float rt1(float v, float isc, float sc) {
+    return B::to_f2(B::from_f2(v * isc, 0.f) & 0xffffu).x * sc;
   }
 };
 

@@ -168,10 +168,101 @@ def test_tensor_interior_equals_staged(gpu, monkeypatch, shape, storage):
     name0, ref = _stepped_state(gpu, prob, st, steps)
     assert "tmat" not in name0
     monkeypatch.setenv("FDTD2D_TMAT", shape)
+    monkeypatch.setenv("FDTD2D_TB", "0")
     name1, got = _stepped_state(gpu, prob, st, steps)
     assert name1.startswith(f"step_tmat_kernel<{shape}>+step_tma_kernel<"), name1
     for k in ref:
         assert np.array_equal(ref[k], got[k]), (shape, k)
+
+
+def _random_fields(nx, ny, P, seed):
+    rng = np.random.default_rng(seed)
+    st = {}
+    for w in FIELDS:
+        a = (rng.standard_normal(F.field_shape(w, nx, ny, P)) * 0.5).astype(np.float32)
+        st[w] = a / np.float32(377.0) if w in (F.FIELD_HX, F.FIELD_HY) else a
+    for w in PSI_FIELDS:
+        st[w] = (rng.standard_normal(F.field_shape(w, nx, ny, P)) * 1e-3).astype(np.float32)
+    return st
+
+
+def _stepped_all(gpu, prob, st, steps, chunks):
+    """Fields, psi, traces, DFT and line probe after `steps` steps run as
+    fdtd2d_run calls over the given chunk lengths."""
+    with F.Shot(prob, gpu) as shot:
+        name = shot.kernel_name()
+        load_state([shot], st)
+        n = 1
+        for c in chunks:
+            shot.run(n, n + c - 1)
+            n += c
+        assert n == steps + 1
+        out = {w: shot.read_field(w) for w in FIELDS + PSI_FIELDS}
+        tr = shot.traces()
+        out["det"] = tr["det_ez"]
+        out["dft"] = shot.dft()
+        s = prob.setup
+        if s.line_n > 0:
+            out["line"] = shot.line(s.line_first, s.line_last)
+    return name, out
+
+
+@pytest.mark.parametrize("shape", TMAT_SHAPES)
+@pytest.mark.parametrize("storage", [F.STORE_F32, F.STORE_F16])
+def test_two_step_equals_one_step(gpu, monkeypatch, shape, storage):
+    """The two-step form (FDTD2D_TB=1: two time steps per pass over the
+    interior, the CPML-band kernel stepping the rest once per step between)
+    gives every cell, psi value, trace sample and DFT sum the bits of the
+    one-row kernel alone.  80 sources and 80 detectors on a diagonal whose
+    columns step by 31 and 29 (every residue mod 128: warp and band edges),
+    down to the first interior row; random state; run calls of odd and even
+    length (a single step after the pairs); a line probe over steps 9-10
+    (single steps in the middle of a call)."""
+    monkeypatch.delenv("FDTD2D_KERNEL", raising=False)
+    monkeypatch.delenv("FDTD2D_TMA", raising=False)
+    nx, ny, P, steps = 2600, 301, 11, 25
+    prob = F.Problem.from_spec(nx=nx, ny=ny, npml=P, n_steps=steps, profile=1, x_lo=nx // 3, x_hi=nx - 3,
+                               ne_peak=2e19, nu=3e9, n_elem=80, src_i=P + 1, src_j=P + 1, src_di=31, src_dj=3,
+                               n_det=80, det_i=P + 3, det_j=P + 2, det_di=29, det_dj=3, dft_freq=40e9,
+                               storage=storage, field_max=100.0)
+    s = prob.setup
+    s.line_n, s.line_i0, s.line_j, s.line_first, s.line_last = 300, 200, 150, 9, 10
+    st = _random_fields(nx, ny, P, 12)
+    chunks = (7, 2, 9, 1, 6)
+    monkeypatch.setenv("FDTD2D_TMAT", "0")
+    name0, ref = _stepped_all(gpu, prob, st, steps, chunks)
+    assert "tmat" not in name0
+    monkeypatch.setenv("FDTD2D_TMAT", shape)
+    monkeypatch.setenv("FDTD2D_TB", "1")
+    name1, got = _stepped_all(gpu, prob, st, steps, chunks)
+    assert name1.startswith(f"step_tmat2_kernel<{shape}>+step_tma_kernel<"), name1
+    for k in ref:
+        assert np.array_equal(ref[k], got[k]), (shape, k)
+
+
+def test_two_step_against_oracle(gpu, monkeypatch):
+    """The two-step form against the FP64 oracle on a CPML-absorbed pulse
+    from a steered array (fields, traces, DFT phase)."""
+    monkeypatch.delenv("FDTD2D_KERNEL", raising=False)
+    monkeypatch.delenv("FDTD2D_TMA", raising=False)
+    monkeypatch.delenv("FDTD2D_TMAT", raising=False)
+    monkeypatch.setenv("FDTD2D_TB", "1")
+    n_elem = 8
+    prob = F.Problem.from_spec(nx=1400, ny=260, npml=16, n_steps=400, dx=0.25e-3, dy=0.25e-3, courant=0.99,
+                               profile=3, ne_peak=3e19, x_center=900, width=60, grf_rms=0.05, grf_corr=10, seed=7,
+                               nu=2e9, n_elem=n_elem, src_i=300, src_j=100, src_dj=5, src_di=0, freq=50e9,
+                               steer_deg=15, pulse=1, pulse_width=0.2e-9, n_det=n_elem, det_i=300, det_j=100,
+                               det_dj=5, det_di=0, dft_freq=50e9)
+    ref = O.Oracle(prob.setup_ptr)
+    ref32 = O.Oracle(prob.setup_ptr, fp32=True)
+    ref.run(1, prob.n_steps)
+    ref32.run(1, prob.n_steps)
+    with F.Shot(prob, gpu) as shot:
+        assert shot.kernel_name().startswith("step_tmat2_kernel<"), shot.kernel_name()
+        shot.run(1, prob.n_steps)
+        compare_fields(shot, ref, FIELDS + PSI_FIELDS, tol=FIELD_TOL, ref32=ref32)
+        assert rel(shot.traces()["det_ez"], ref.traces()["det_ez"]) <= FIELD_TOL
+        assert dft_phase_error(shot, ref) <= 1e-4
 
 
 def test_autotuned_shape_and_deep_cpml(gpu, monkeypatch):
@@ -179,7 +270,8 @@ def test_autotuned_shape_and_deep_cpml(gpu, monkeypatch):
     CPML deeper than the staged kernel's x-strip slots streams instead."""
     monkeypatch.delenv("FDTD2D_KERNEL", raising=False)
     monkeypatch.delenv("FDTD2D_TMA", raising=False)
-    assert _random_state_case(gpu, 700, 130, 16).startswith(("step_tma_kernel<", "step_tmat_kernel<"))
+    assert _random_state_case(gpu, 700, 130, 16).startswith(("step_tma_kernel<", "step_tmat_kernel<",
+                                                             "step_tmat2_kernel<"))
     _random_state_case(gpu, 1600, 140, 12)   # interior bands: the tensor pair competes in the timing
     assert _random_state_case(gpu, 300, 260, 121, steps=20) == "step_stream_kernel<0>"
 
