@@ -150,6 +150,44 @@ void add_units(std::vector<int4>& u, int ca, int cb, int band, int ra, int rb, i
   }
 }
 
+// Units of the one-row kernel on the rest of the grid beside the interior
+// region [ci0, ci1) x [ri0, ri1): bands of `band` columns over [0, ci0) and
+// [ci1, nx) on every row, and over [ci0, ci1) on rows [0, ri0) and [ri1,
+// ny - 1).  Each band's rows are cut into strips of about equal cost (a row
+// of the CPML row strips costs about 1.5 plain rows, a row of a band that
+// holds an x strip about 1.3) so that the strips fill `ctas` CTAs in one
+// wave: the band kernel's step between two interior passes runs alone, and
+// its time is that of its longest CTA.
+std::vector<int4> edge_units(int nx, int ny, int P, int ci0, int ci1, int ri0, int ri1, int band, int ctas) {
+  struct Seg {
+    int c0, j0, j1;
+    double w;
+  };
+  std::vector<Seg> segs;
+  auto xw = [&](int c) { return (c == 0 || c + band - 1 >= nx - P) ? 1.3 : 1.0; };
+  for (int c = ci0; c < ci1; c += band) {
+    segs.push_back({c, 0, ri0, 1.5});
+    segs.push_back({c, ri1, ny - 1, 1.5});
+  }
+  for (int c = 0; c < ci0; c += band) segs.push_back({c, 0, ny - 1, xw(c)});
+  for (int c = ci1; c < nx; c += band) segs.push_back({c, 0, ny - 1, xw(c)});
+  double total = 0;
+  for (const Seg& g : segs) total += std::max(0, g.j1 - g.j0) * g.w;
+  const int slots = std::max(1, ctas - (int)segs.size());   // room for every band's rounding up
+  const double per = std::max(4.0, total / slots);
+  std::vector<int4> u;
+  for (const Seg& g : segs) {
+    const int r = g.j1 - g.j0;
+    if (r <= 0) continue;
+    const int k = std::max(1, std::min(r, (int)std::ceil(r * g.w / per)));
+    for (int s = 0; s < k; ++s) {
+      const int a = g.j0 + (int)((int64_t)r * s / k), b = g.j0 + (int)((int64_t)r * (s + 1) / k);
+      if (b > a) u.push_back(make_int4(0, g.c0, a, b));
+    }
+  }
+  return u;
+}
+
 // Keep freed shot memory in this process's pool of the device (default
 // release threshold 0 hands it back at every synchronisation, and the next
 // shot pays to map it again).  A property of this process's pool only.
@@ -431,13 +469,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
           for (int4& u : tu)
             u.x = (u.z == ri0 ? kRingTop : 0) | (u.w == ri1 ? kRingBottom : 0) | (u.y == ci0 ? kRingLeft : 0) |
                   (u.y + bt == ci1 ? kRingRight : 0);
-        // the one-row kernel: edge bands over all rows, interior bands over the CPML rows
-        const int neb = (ci0 + b1 - 1) / b1 + (nx - ci1 + b1 - 1) / b1;
-        const int se = std::min(std::max(1, ectas / std::max(1, neb)), std::max(1, (ny - 1) / 8));
-        add_units(eu, 0, ci0, b1, 0, ny - 1, se);
-        add_units(eu, ci1, nx, b1, 0, ny - 1, se);
-        add_units(eu, ci0, ci1, b1, 0, ri0, 1);
-        add_units(eu, ci0, ci1, b1, ri1, ny - 1, 1);
+        eu = edge_units(nx, ny, P, ci0, ci1, ri0, ri1, b1, ectas);
         int4 *dt = nullptr, *de = nullptr;
         cudaError_t e = cudaMallocAsync(&dt, tu.size() * sizeof(int4), c->stream);
         if (e == cudaSuccess) e = cudaMallocAsync(&de, eu.size() * sizeof(int4), c->stream);

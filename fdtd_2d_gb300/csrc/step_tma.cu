@@ -53,7 +53,7 @@ struct Cfg {
   static constexpr uint32_t kXOffB = kPsiOffB + 2 * kPsiBytes;
   static constexpr uint32_t kStageBytes = kXOffB + 4 * kXSlot * 4;
   static constexpr size_t kSmem = (size_t)ST * kStageBytes;
-  static constexpr int kMinBlocks = W <= 4 ? 4 : 2;   // caps registers at 128 per thread
+  static constexpr int kMinBlocks = W <= 4 ? 4 : 2;   // W = 8: caps registers at 128 per thread
   static_assert(kSegBytes % 16 == 0 && kPsiOffB % 16 == 0 && kXOffB % 16 == 0 && kStageBytes % 16 == 0,
                 "16-byte aligned stage slots");
 };
@@ -548,7 +548,7 @@ constexpr ShapeEntry entry() {
 // Compiled launch shapes; the first is the default.
 const ShapeEntry kShapes[] = {entry<4, 3>(), entry<4, 2>(), entry<4, 4>(), entry<4, 6>(),
                               entry<8, 2>(), entry<8, 3>(), entry<8, 4>(), entry<2, 4>(), entry<2, 6>(),
-                              entry<2, 2>(), entry<2, 3>()};
+                              entry<2, 2>(), entry<2, 3>(), entry<1, 2>(), entry<1, 3>(), entry<1, 4>()};
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
 }  // namespace

@@ -114,7 +114,7 @@ def _random_state_case(gpu, nx, ny, P, steps=60):
 
 
 # Launch shapes (warps per CTA, ring stages) compiled into the staged kernel.
-TMA_SHAPES = ["4,3", "4,2", "4,4", "4,6", "8,2", "8,3", "8,4", "2,4", "2,6", "2,2", "2,3"]
+TMA_SHAPES = ["4,3", "4,2", "4,4", "4,6", "8,2", "8,3", "8,4", "2,4", "2,6", "2,2", "2,3", "1,2", "1,3", "1,4"]
 
 
 @pytest.mark.parametrize("shape", TMA_SHAPES)
