@@ -108,7 +108,7 @@ bool encode_maps(const DevShot& h, int nx, int ny, int bx, int rows, TensorMaps*
                                  : h.store == FDTD2D_STORE_F16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
                                                                : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
   const cuuint32_t est[3] = {1, 1, 1};
-  for (int b = 0; b < 3; ++b) {
+  for (int b = 0; b < 4; ++b) {
     if (!h.fb[b]) continue;
     const cuuint64_t dims3[3] = {(cuuint64_t)nx, (cuuint64_t)ny, 3};
     const cuuint64_t str3[2] = {(cuuint64_t)h.pitch * es, (cuuint64_t)h.cells * es};
@@ -331,35 +331,52 @@ void swap_slots(DevShot& h, TensorMaps& m, int a, int b) {
   std::swap(m.e[a], m.e[b]);
 }
 
-// Steps n and n+1 on the two-step path.  The interior kernel (shot stream)
-// runs beside the CPML-band kernel's step n (side stream); the band kernel's
-// step n+1 follows once the interior kernel has written the ring of state n
-// it reads.  h and m come back with state n+1 in slot (n+1)&1 and the
-// buffer of state n-1 moved to slot 2.  Each kernel waits for the previous
-// work that read what it overwrites: the interior kernel for the side
-// stream's last kernel (ev_e), the band kernel's step n for the previous
-// interior kernel (ev_t as recorded before this call).
-cudaError_t issue_pair(fdtd2d_ctx* c, int k, int q, DevShot& h, TensorMaps& m, const int4* tu, int ntu, int tctas,
-                       const int4* eu, int neu, int ectas, int n) {
+// What one two-step pair launches: the interior kernel's shape, units and
+// CTAs, the CPML-band kernel's, and the interior region.
+struct PairPlan {
+  int k, tctas, ntu;
+  const int4* tu;
+  int q, ectas, neu;
+  const int4* eu;
+  int ci0, ci1, ri0, ri1;
+};
+
+// Steps n and n+1 on the two-step path.  Shot stream: the interior kernel
+// (both steps of R), then, once the CPML-band kernel's step n is done, the
+// frame kernel (step n+1 of the 2-cell frame around R: all that the next
+// interior pass reads outside R).  Side stream: the band kernel's step n,
+// then, once the interior kernel is done, its step n+1, which so runs beside
+// the next pair's interior kernel.  Slots: state n-1 in a = (n-1)&1, state n
+// (band cells and R's ring) into b = n&1, state n+1 into slot 2; slot 3 holds
+// the previous pair's state-n buffer, which that pair's band step n+1 may
+// still be reading.  h and m come back with state n+1 in slot a (= (n+1)&1),
+// the next pair's state-n buffer in slot b, the old state n-1 buffer in slot
+// 2 and this pair's state-n buffer in slot 3.  Every buffer a kernel here
+// overwrites was last read by work the stream order or these waits put
+// before it (the interior kernel's output by the band kernel's step n of the
+// previous pair, waited for by that pair's frame kernel).
+cudaError_t issue_pair(fdtd2d_ctx* c, const PairPlan& p, DevShot& h, TensorMaps& m, int n) {
   const int a = (n - 1) & 1, b = n & 1;
-  DevShot t = h;
+  DevShot ti = h;
   TensorMaps tm = m;
-  // the two-step kernel's slots: 0 state n-1, 1 state n (ring), 2 state n+1
-  t.fb[0] = h.fb[a];
-  t.fb[1] = h.fb[b];
+  ti.fb[0] = h.fb[a];
+  ti.fb[1] = h.fb[b];
   tm.hj[0] = m.hj[a];
-  tm.hj[1] = m.hj[b];
   tm.e[0] = m.e[a];
-  tm.e[1] = m.e[b];
-  cudaError_t x = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
-  if (x == cudaSuccess) x = launch_step_tmat2(k, t, tm, tu, ntu, n, tctas, c->d_err, c->stream);
-  if (x == cudaSuccess) x = cudaStreamWaitEvent(c->side, c->ev_t, 0);
+  DevShot t2 = h;          // step n+1: reads slot b, writes slot a = the state n+1 buffer
+  t2.fb[a] = h.fb[2];
+  cudaError_t x = cudaStreamWaitEvent(c->side, c->ev_t, 0);
+  if (x == cudaSuccess) x = launch_step_tmat2(p.k, ti, tm, p.tu, p.ntu, n, p.tctas, c->d_ctr, c->d_err, c->stream);
   if (x == cudaSuccess) x = cudaEventRecord(c->ev_t, c->stream);
-  if (x == cudaSuccess) x = launch_step_tma(q, h, eu, neu, n, ectas, c->d_err, c->side);
+  if (x == cudaSuccess) x = launch_step_tma(p.q, h, p.eu, p.neu, n, p.ectas, c->d_err, c->side);
+  if (x == cudaSuccess) x = cudaEventRecord(c->ev_a, c->side);
+  if (x == cudaSuccess) x = cudaStreamWaitEvent(c->stream, c->ev_a, 0);
+  if (x == cudaSuccess) x = launch_frame(t2, p.ci0, p.ci1, p.ri0, p.ri1, n + 1, c->d_ctr, c->stream);
   if (x == cudaSuccess) x = cudaStreamWaitEvent(c->side, c->ev_t, 0);
-  swap_slots(h, m, a, 2);
-  if (x == cudaSuccess) x = launch_step_tma(q, h, eu, neu, n + 1, ectas, c->d_err, c->side);
+  if (x == cudaSuccess) x = launch_step_tma(p.q, t2, p.eu, p.neu, n + 1, p.ectas, c->d_err, c->side);
   if (x == cudaSuccess) x = cudaEventRecord(c->ev_e, c->side);
+  swap_slots(h, m, a, 2);
+  swap_slots(h, m, b, 3);
   return x;
 }
 
@@ -395,18 +412,23 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_t, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_e, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_m, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming);
     if (e != cudaSuccess) return fail_cuda(c, e);
   }
-  // Two-step form: a third field buffer, a copy of the first (cells that no
-  // kernel writes keep their values in every buffer), and a scratch psi slab
-  // for the trials (a trial pair's second step writes psi buffer 0).
-  const bool try2 = tb_mode != 0 && c->n_steps >= 2 && ny - 2 * P - 2 >= 8;
+  // Two-step form: two more field buffers, copies of the first (cells that
+  // no kernel writes keep their values in every buffer), its unit counter,
+  // and a scratch psi slab for the trials (a trial pair's second step writes
+  // psi buffer 0).
+  const bool try2 = tb_mode != 0 && c->n_steps >= 2 && ny - 2 * P - 4 >= 8;
   float* psi_trial = nullptr;
   const size_t psi_floats = (size_t)h.psi_buf * 2 + 1024;
   if (try2) {
     const size_t fbytes = (size_t)h.cells * 4 * store_bytes(h.store);
     cudaError_t e = dalloc(c, &h.fb[2], fbytes / 4);
+    if (e == cudaSuccess) e = dalloc(c, &h.fb[3], fbytes / 4);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h.fb[2], h.fb[0], fbytes, cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.fb[3], h.fb[0], fbytes, cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess && !c->d_ctr) e = dalloc(c, &c->d_ctr, 1);
     if (e == cudaSuccess) e = cudaMallocAsync(&psi_trial, psi_floats * 4, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(psi_trial, h.psi, psi_floats * 4, cudaMemcpyDeviceToDevice, c->stream);
     if (e != cudaSuccess) return fail_cuda(c, e);
@@ -420,6 +442,20 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
     cudaError_t e = step();
     if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
     for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = step();
+    if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = -1.f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    return e == cudaSuccess ? ms : -1.f;
+  };
+  // a pair trial: pairs issued back to back (the band kernel's second step
+  // of one beside the next one's interior kernel), timed to the last kernel
+  auto timed2 = [&](auto&& pair) -> float {
+    cudaError_t e = pair();
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+    for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = pair();
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
     if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
     if (e == cudaSuccess) e = cudaEventSynchronize(e1);
     float ms = -1.f;
@@ -453,8 +489,9 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
       const int tctas = lv == 1 ? tctas1 : tctas2;
       // interior region: rows [ri0, ri1), columns [ci0, ci1) with ci0 the
       // first multiple of the one-row band at or past the CPML (two-step
-      // form: one cell further in on every side), then whole tensor bands
-      const int ri0 = lv == 1 ? P : P + 1, ri1 = ny - ri0;
+      // form: two cells further in on every side, so that the frame kernel's
+      // cells and their neighbours have no CPML), then whole tensor bands
+      const int ri0 = lv == 1 ? P : P + 2, ri1 = ny - ri0;
       for (int q = 0; q < tma_shape_count(); ++q) {
         if (q_forced >= 0 && q != q_forced) continue;
         const int b1 = tma_band_cols(q);
@@ -464,7 +501,9 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
         const int ectas = tma_resident_ctas(q, P, h.store, device);
         std::vector<int4> tu, eu;
         const int nbt = (ci1 - ci0) / bt;
-        add_units(tu, ci0, ci1, bt, ri0, ri1, std::min(std::max(1, tctas / nbt), (ri1 - ri0) / (2 * R)));
+        // (two-step form: about three units per CTA, taken in turn)
+        add_units(tu, ci0, ci1, bt, ri0, ri1,
+                  std::min((lv == 1 ? 1 : 3) * std::max(1, tctas / nbt), (ri1 - ri0) / (2 * R)));
         if (lv == 2)
           for (int4& u : tu)
             u.x = (u.z == ri0 ? kRingTop : 0) | (u.w == ri1 ? kRingBottom : 0) | (u.y == ci0 ? kRingLeft : 0) |
@@ -493,15 +532,15 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
             return x;
           });
         } else if (e == cudaSuccess) {
-          // slots of the trial descriptor: state 0 in slot 0 stays untouched
-          // (the pair writes slots 1 and 2), psi goes to the scratch slab
-          ms = timed([&] {
+          // every trial pair starts from the state in slot (n1-1)&1, which no
+          // pair writes, and computes the same values into the other slots;
+          // psi goes to the scratch slab
+          const PairPlan pl{k, tctas, (int)tu.size(), dt, q, ectas, (int)eu.size(), de, ci0, ci1, ri0, ri1};
+          ms = timed2([&] {
             DevShot t2 = t;
             t2.psi = psi_trial;
             TensorMaps m2 = maps;
-            cudaError_t x = issue_pair(c, k, q, t2, m2, dt, (int)tu.size(), tctas, de, (int)eu.size(), ectas, n1);
-            if (x == cudaSuccess) x = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
-            return x;
+            return issue_pair(c, pl, t2, m2, n1);
           });
           if (ms >= 0) ms *= 0.5f;
         }
@@ -518,6 +557,10 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
           best_m = maps;
           c->tmat_ctas = tctas1;
           c->tmat2_ctas = tctas2;
+          c->reg[0] = ci0;
+          c->reg[1] = ci1;
+          c->reg[2] = ri0;
+          c->reg[3] = ri1;
         }
       }
     }
@@ -526,12 +569,14 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   cudaEventDestroy(e1);
   if (psi_trial) cudaFreeAsync(psi_trial, c->stream);
   if (h.fb[2] && !(best_k >= 0 && best_l == 2)) {
-    // the two-step form lost: give its buffer back
-    cudaFreeAsync(h.fb[2], c->stream);
-    c->allocs.erase(std::find(c->allocs.begin(), c->allocs.end(), (void*)h.fb[2]));
-    h.fb[2] = nullptr;
-    std::memset(&best_m.hj[2], 0, sizeof best_m.hj[2]);
-    std::memset(&best_m.e[2], 0, sizeof best_m.e[2]);
+    // the two-step form lost: give its buffers back
+    for (int b = 2; b < 4; ++b) {
+      cudaFreeAsync(h.fb[b], c->stream);
+      c->allocs.erase(std::find(c->allocs.begin(), c->allocs.end(), (void*)h.fb[b]));
+      h.fb[b] = nullptr;
+      std::memset(&best_m.hj[b], 0, sizeof best_m.hj[b]);
+      std::memset(&best_m.e[b], 0, sizeof best_m.e[b]);
+    }
   }
   int derr = 0;
   if (cudaMemcpy(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return FDTD2D_ERR_CUDA;
@@ -574,7 +619,7 @@ void fdtd2d::adopt_ctx(fdtd2d_ctx* c, cudaStream_t batch_stream) {
     cudaStreamSynchronize(c->side);
     cudaStreamDestroy(c->side);
   }
-  for (cudaEvent_t ev : {c->ev_t, c->ev_e, c->ev_m})
+  for (cudaEvent_t ev : {c->ev_t, c->ev_e, c->ev_m, c->ev_a})
     if (ev) cudaEventDestroy(ev);
   c->stream = batch_stream;
   c->batch = true;
@@ -957,20 +1002,26 @@ int fdtd2d_run(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_m, 0);
     if (e != cudaSuccess) return fail_cuda(c, e);
   }
+  bool paired = false;   // the last iteration issued a pair
   for (int32_t n = n_first; n <= n_last; ++n) {
     cudaError_t e;
     // Two steps per pass where nothing reads the fields between them (the
     // tracker and the line probe read every step's Ez).
     if (c->tb && n < n_last && c->n_rc == 0 &&
         !(c->line_n > 0 && n + 1 >= c->line_first && n <= c->line_last)) {
-      e = issue_pair(c, c->tmat_shape, c->tma_shape, c->h, c->maps, c->d_tunits, c->n_tunits, c->tmat2_ctas,
-                     c->d_eunits, c->n_eunits, c->grid_warps, n);
+      const PairPlan pl{c->tmat_shape, c->tmat2_ctas, c->n_tunits, c->d_tunits, c->tma_shape, c->grid_warps,
+                        c->n_eunits, c->d_eunits, c->reg[0], c->reg[1], c->reg[2], c->reg[3]};
+      // after single steps the interior kernel waits for their band kernel
+      e = paired ? cudaSuccess : cudaStreamWaitEvent(c->stream, c->ev_e, 0);
+      if (e == cudaSuccess) e = issue_pair(c, pl, c->h, c->maps, n);
       if (e == cudaSuccess && n + 1 == n_last) e = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
       if (e != cudaSuccess) return fail_cuda(c, e);
-      c->launches += 3;
+      c->launches += 4;
       c->step = ++n;
+      paired = true;
       continue;
     }
+    paired = false;
     if (c->tmat) {
       // Interior on the multi-row tensor kernel (shot stream), CPML bands and
       // rows on the staged kernel (side stream), both kernels of a step at
@@ -1248,7 +1299,7 @@ int read_field16(fdtd2d_ctx* c, int which, float* host) {
 int write_field16(fdtd2d_ctx* c, int which, const float* host) {
   cudaSetDevice(c->device);
   cudaError_t e = cudaStreamSynchronize(c->stream);
-  for (int b = 0; b < 3 && e == cudaSuccess; ++b) {
+  for (int b = 0; b < 4 && e == cudaSuccess; ++b) {
     if (!c->h.fb[b]) continue;
     View16 v;
     if (!view16(c, which, b, &v)) return FDTD2D_ERR_INVALID;
@@ -1282,9 +1333,9 @@ int fdtd2d_write_field(fdtd2d_ctx* c, int which, const float* host) {
   if (c->h.store != FDTD2D_STORE_F32 && which <= FDTD2D_FIELD_JZ) return write_field16(c, which, host);
   cudaSetDevice(c->device);
   cudaError_t e = cudaStreamSynchronize(c->stream);
-  for (int b = 0; b < 3 && e == cudaSuccess; ++b) {
+  for (int b = 0; b < 4 && e == cudaSuccess; ++b) {
     if (which <= FDTD2D_FIELD_JZ && !c->h.fb[b]) continue;
-    if (which > FDTD2D_FIELD_JZ && b == 2) break;   // psi: two buffers
+    if (which > FDTD2D_FIELD_JZ && b >= 2) break;   // psi: two buffers
     FieldView v;
     if (!field_view(c, which, b, &v)) return FDTD2D_ERR_INVALID;
     e = cudaMemcpy2D(v.base, v.dpitch * 4, host, v.hpitch * 4, (size_t)v.cols * 4, v.rows,
@@ -1332,7 +1383,7 @@ int fdtd2d_destroy(fdtd2d_ctx* c) {
     cudaStreamSynchronize(c->side);
     cudaStreamDestroy(c->side);
   }
-  for (cudaEvent_t ev : {c->ev_t, c->ev_e, c->ev_m})
+  for (cudaEvent_t ev : {c->ev_t, c->ev_e, c->ev_m, c->ev_a})
     if (ev) cudaEventDestroy(ev);
   delete c;
   return FDTD2D_OK;

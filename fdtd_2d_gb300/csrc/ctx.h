@@ -34,8 +34,10 @@ struct fdtd2d_ctx {
   // multi-row tensor path for the interior (step_tmat.cu) beside the staged
   // kernel on the CPML bands and rows
   bool tmat = false;
-  bool tb = false;            // its two-step form (third field buffer h.fb[2])
+  bool tb = false;            // its two-step form (field buffers h.fb[2], h.fb[3])
   int tmat_shape = 0, tmat_ctas = 0, tmat2_ctas = 0;
+  int reg[4] = {0, 0, 0, 0};  // interior region [reg0, reg1) x [reg2, reg3)
+  int* d_ctr = nullptr;       // the two-step kernel's unit counter
   int4* d_tunits = nullptr;   // interior units (tensor kernel)
   int n_tunits = 0;
   int4* d_eunits = nullptr;   // the rest (staged kernel)
@@ -44,8 +46,10 @@ struct fdtd2d_ctx {
   // the CPML-band kernel runs on a second stream beside the interior one:
   // ev_t marks the interior kernel of the last step, ev_e the CPML kernel,
   // ev_m the shot stream's work before a run
+  // (two-step path: ev_t the interior kernel, ev_a the band kernel's first
+  // step of the pair, ev_e its second)
   cudaStream_t side = nullptr;
-  cudaEvent_t ev_t = nullptr, ev_e = nullptr, ev_m = nullptr;
+  cudaEvent_t ev_t = nullptr, ev_e = nullptr, ev_m = nullptr, ev_a = nullptr;
   char kernel_name[96] = {0};
   // wave-front tracker and line probe
   int n_rc = 0, rc_j_cut = 0;

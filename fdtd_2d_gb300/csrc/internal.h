@@ -48,11 +48,11 @@ struct DevShot {
   // kMargin elements into it, so every row has a zero margin on both sides
   // that bulk row copies may read as halo.  field_ptr() points at column 0.
   // Step n reads fb[(n-1)&1] and writes fb[n&1]; a launch may be given a
-  // descriptor whose fb points elsewhere.  fb[2] is the third buffer of the
-  // two-step (temporally blocked) path, null without it: a two-step launch
-  // reads fb[0] (state n-1) and writes fb[2] (state n+1), and fb[1] (state
-  // n) on the ring cells its neighbours read.
-  float* fb[3];
+  // descriptor whose fb points elsewhere.  fb[2] and fb[3] are the extra
+  // buffers of the two-step (temporally blocked) path, null without it: a
+  // two-step launch reads fb[0] (state n-1) and writes fb[2] (state n+1),
+  // and fb[1] (state n) on the ring cells its neighbours read.
+  float* fb[4];
   int64_t cells;
   // CPML psi slab [2 ping-pong buffers][psi_buf]; within a buffer (side s = 0
   // low edge, 1 high edge):
@@ -155,7 +155,7 @@ int tma_resident_ctas(int shape, int npml, int store, int device);
 // of row 0 is the origin, columns outside [0, nx) and rows outside [0, ny)
 // read as zero.
 struct TensorMaps {
-  CUtensorMap hj[3], e[3], k;   // per field-buffer slot, as DevShot::fb
+  CUtensorMap hj[4], e[4], k;   // per field-buffer slot, as DevShot::fb
 };
 
 // Multi-row staged kernel for the interior of a shot: units (0, c0, j0, j1)
@@ -173,13 +173,21 @@ cudaError_t launch_step_tmat(int shape, const DevShot& shot, const TensorMaps& m
 // Two-step (temporally blocked) form of the same kernel: steps n and n+1 of
 // units (ring, c0, j0, j1) in one pass over state n-1, with n = n_global -
 // base_n.  The units tile a region R whose cells and 1-cell surround have no
-// CPML (columns and rows in [npml+1, n-npml-1)); each unit recomputes step n
-// one cell around itself, and writes state n+1 to slot 2 and, on the cells
-// of R next to the rest of the grid (ring flags kRing*), state n to slot 1.
+// CPML; each unit recomputes step n one cell around itself, and writes state
+// n+1 to slot 2 and, on the cells of R next to the rest of the grid (ring
+// flags kRing*), state n to slot 1.  CTAs take units in turn from *ctr,
+// which must be 0 at launch (launch_frame resets it).
 enum RingFlags : int { kRingTop = 1, kRingBottom = 2, kRingLeft = 4, kRingRight = 8 };
 int tmat2_resident_ctas(int shape, int store, int device);
 cudaError_t launch_step_tmat2(int shape, const DevShot& shot, const TensorMaps& maps, const int4* units,
-                              int n_units, int n_global, int max_ctas, int* err, cudaStream_t stream);
+                              int n_units, int n_global, int max_ctas, int* ctr, int* err, cudaStream_t stream);
+// Step n (n_global - base_n) of the 2-cell frame around R = [ci0, ci1) x
+// [ri0, ri1) (columns [ci0-2, ci1+2) x rows [ri0-2, ri1+2), minus R) from
+// slot (n-1)&1 into slot n&1, sources applied, detectors left to the CPML
+// band kernel; the frame and its 1-cell surround must lie outside the CPML.
+// Sets *ctr = 0.
+cudaError_t launch_frame(const DevShot& shot, int ci0, int ci1, int ri0, int ri1, int n_global, int* ctr,
+                         cudaStream_t stream);
 // Launches the instantiation for shot.store.
 cudaError_t launch_step_tma(int shape, const DevShot& shot, const int4* units, int n_units, int n_global,
                             int max_ctas, int* err, cudaStream_t stream);

@@ -16,6 +16,8 @@
 //
 // Every wait is bounded as in step_tma.cu (1 s without progress: the error
 // word is set, the copies in flight are waited for, the kernel returns).
+#include <algorithm>
+
 #include "internal.h"
 #include "step_common.cuh"
 #include "tma_common.cuh"
@@ -604,9 +606,10 @@ step_tmat_kernel(const __grid_constant__ DevShot S, const __grid_constant__ Tens
 template <class C>
 __global__ void __launch_bounds__(C::kThreads, C::kMinBlocks2)
 step_tmat2_kernel(const __grid_constant__ DevShot S, const __grid_constant__ TensorMaps M,
-                  const int4* __restrict__ units, int n_units, int n_global, int* err) {
+                  const int4* __restrict__ units, int n_units, int n_global, int* ctr, int* err) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[C::kStages], empty[C::kStages];
+  __shared__ int next;
   if (threadIdx.x == 0) {
     for (int s = 0; s < C::kStages; ++s) {
       mbar_init(&full[s], 1);
@@ -621,20 +624,85 @@ step_tmat2_kernel(const __grid_constant__ DevShot S, const __grid_constant__ Ten
   R.empty = empty;
   const int n = n_global - S.base_n;
   if (n < 1 || n + 1 > S.n_steps) return;
-  for (int u = blockIdx.x; u < n_units; u += gridDim.x) {
+  // Units are taken in turn, so that CTAs that start late (the SM still
+  // held by the CPML-band kernel running beside this one) take fewer.
+  for (;;) {
+    if (threadIdx.x == 0) next = *(volatile int*)err ? n_units : atomicAdd(ctr, 1);
+    __syncthreads();
+    const int u = next;
+    __syncthreads();
+    if (u >= n_units) return;
     tband2<C>(S, M, R, __ldg(units + u), n, err);
-    if (*(volatile int*)err) return;
+  }
+}
+
+// One frame cell (i, j) of step n: the one-step kernels' updates of Hx, Hy
+// (and the Hx, Hy the Ez update takes from the cells above and to the left),
+// Jz and Ez, operation for operation, from the stored state n-1.
+template <class T>
+__device__ __forceinline__ void frame_cell(const DevShot& S, int i, int j, int n) {
+  using St = Sto<T>;
+  const int par = (n - 1) & 1;
+  const int64_t p = S.pitch, o = (int64_t)j * p + i;
+  const float sE = S.sc[0], sHx = S.sc[1], sHy = S.sc[2], sJ = S.sc[3], sK = S.sc[4];
+  const T* ez = field_ptr_t<T>(S, kEz, par);
+  const T* hx = field_ptr_t<T>(S, kHx, par);
+  const T* hy = field_ptr_t<T>(S, kHy, par);
+  const T* jz = field_ptr_t<T>(S, kJz, par);
+  const float e_c = St::ldg1(ez + o, sE), e_r = St::ldg1(ez + o + 1, sE), e_l = St::ldg1(ez + o - 1, sE);
+  const float e_d = St::ldg1(ez + o + p, sE), e_u = St::ldg1(ez + o - p, sE);
+  const float da = S.da, db = S.db;
+  const float hx_c = upd_h(da, St::ldg1(hx + o, sHx), db, e_c, e_d, __ldg(S.den_hy + j));
+  const float hx_u = upd_h(da, St::ldg1(hx + o - p, sHx), db, e_u, e_c, __ldg(S.den_hy + j - 1));
+  const float hy_c = upd_h(da, St::ldg1(hy + o, sHy), db, e_r, e_c, __ldg(S.den_hx + i));
+  const float hy_l = upd_h(da, St::ldg1(hy + o - 1, sHy), db, e_c, e_l, __ldg(S.den_hx + i - 1));
+  const float kp = S.kp ? St::ldg1(reinterpret_cast<const T*>(S.kp) + o, sK) : 0.f;
+  const float jz_n = upd_j(S.ja, St::ldg1(jz + o, sJ), kp, e_c);
+  float e = upd_e(S.ca, e_c, S.cb, __fsub_rn(hy_c, hy_l), __ldg(S.den_ex + i), __fsub_rn(hx_u, hx_c),
+                  __ldg(S.den_ey + j), jz_n);
+  for (int q = __ldg(S.row_start + j), q1 = __ldg(S.row_start + j + 1); q < q1; ++q) {
+    const int4 pt = __ldg(S.pts + q);
+    if (pt.y == kPointSource && pt.x == i) e = __fsub_rn(e, __ldg(S.src_val + (int64_t)n * S.n_src + pt.z));
+  }
+  St::st1(field_ptr_t<T>(S, kEz, par ^ 1) + o, e, S.isc[0]);
+  St::st1(field_ptr_t<T>(S, kHx, par ^ 1) + o, hx_c, S.isc[1]);
+  St::st1(field_ptr_t<T>(S, kHy, par ^ 1) + o, hy_c, S.isc[2]);
+  St::st1(field_ptr_t<T>(S, kJz, par ^ 1) + o, jz_n, S.isc[3]);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) frame_kernel(const __grid_constant__ DevShot S, int ci0, int ci1, int ri0,
+                                                    int ri1, int n_global, int* ctr) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) *ctr = 0;
+  const int n = n_global - S.base_n;
+  if (n < 1 || n > S.n_steps) return;
+  const int w = ci1 - ci0 + 4;          // frame row width
+  const int h = ri1 - ri0;              // side column height
+  const int n_tb = 4 * w, n_all = n_tb + 4 * h;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_all; t += gridDim.x * blockDim.x) {
+    int i, j;
+    if (t < n_tb) {
+      const int r = t / w;                     // rows ri0-2, ri0-1, ri1, ri1+1
+      i = ci0 - 2 + t % w;
+      j = r < 2 ? ri0 - 2 + r : ri1 + r - 2;
+    } else {
+      const int q = t - n_tb, r = q / h;       // columns ci0-2, ci0-1, ci1, ci1+1
+      j = ri0 + q % h;
+      i = r < 2 ? ci0 - 2 + r : ci1 + r - 2;
+    }
+    frame_cell<T>(S, i, j, n);
   }
 }
 
 using TKernelFn = void (*)(DevShot, TensorMaps, const int4*, int, int, int*);
+using TKernelFn2 = void (*)(DevShot, TensorMaps, const int4*, int, int, int*, int*);
 
 struct TShape {
   int warps, rows, stages;
   TKernelFn fn[3];
   size_t smem[3];
   int bx;
-  TKernelFn fn2[3];   // two-step form
+  TKernelFn2 fn2[3];   // two-step form
 };
 
 template <int W, int R, int ST>
@@ -679,12 +747,25 @@ cudaError_t launch_step_tmat(int shape, const DevShot& shot, const TensorMaps& m
 }
 
 cudaError_t launch_step_tmat2(int shape, const DevShot& shot, const TensorMaps& maps, const int4* units,
-                              int n_units, int n_global, int max_ctas, int* err, cudaStream_t stream) {
+                              int n_units, int n_global, int max_ctas, int* ctr, int* err, cudaStream_t stream) {
   const TShape& e = kTShapes[shape];
   const int ctas = max_ctas < n_units ? max_ctas : n_units;
   if (ctas <= 0) return cudaSuccess;
   const int st = shot.store;
-  e.fn2[st]<<<ctas, e.warps * 32, e.smem[st], stream>>>(shot, maps, units, n_units, n_global, err);
+  e.fn2[st]<<<ctas, e.warps * 32, e.smem[st], stream>>>(shot, maps, units, n_units, n_global, ctr, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_frame(const DevShot& shot, int ci0, int ci1, int ri0, int ri1, int n_global, int* ctr,
+                         cudaStream_t stream) {
+  const int64_t cells = 4 * (int64_t)(ci1 - ci0 + 4) + 4 * (int64_t)(ri1 - ri0);
+  const int blocks = (int)std::min<int64_t>((cells + 255) / 256, 1024);
+  if (shot.store == 0)
+    frame_kernel<float><<<blocks, 256, 0, stream>>>(shot, ci0, ci1, ri0, ri1, n_global, ctr);
+  else if (shot.store == 1)
+    frame_kernel<__half><<<blocks, 256, 0, stream>>>(shot, ci0, ci1, ri0, ri1, n_global, ctr);
+  else
+    frame_kernel<__nv_bfloat16><<<blocks, 256, 0, stream>>>(shot, ci0, ci1, ri0, ri1, n_global, ctr);
   return cudaGetLastError();
 }
 
