@@ -163,14 +163,22 @@ def measured_peaks() -> dict:
     return {}
 
 
-def profile_traffic(kernel: str) -> float | None:
-    """DRAM bytes per step of the step kernel(s) on this workload, from the
-    committed ncu summary of that kernel family."""
-    name = "step_tmat_8192_production.md" if kernel.startswith("step_tmat") else "step_tma_8192_production.md"
+def profile_traffic(kernel: str, cells: int) -> float | None:
+    """DRAM bytes per launch of the interior step kernel on this workload,
+    from the committed ncu summary of that kernel family: its bytes per cell
+    of the launch's region (the region depends on the CPML-band shape the
+    autotuner keeps; traffic grows with it in proportion) times `cells`, or
+    the per-launch figure when the summary has no per-cell one."""
+    name = ("step_tmat2_8192_production.md" if kernel.startswith("step_tmat2") else
+            "step_tmat_8192_production.md" if kernel.startswith("step_tmat") else "step_tma_8192_production.md")
     f = ROOT / "profiles" / name
     if not f.exists():
         return None
-    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read_text())
+    text = f.read_text()
+    m = re.search(r"traffic_bytes_per_cell:\s*([0-9.eE+]+)", text)
+    if m:
+        return float(m.group(1)) * cells
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", text)
     return float(m.group(1)) if m else None
 
 
@@ -487,8 +495,11 @@ def run_ours(args, world, rank, local, dist) -> None:
     shot.synchronize()
     launches0 = shot.launches()
     kernel = shot.kernel_name()
+    shot.time_step_kernel(True)   # event pair around each interior-kernel launch
     ms = shot.run_timed(W * S + 1, W * S + K * S)  # one event pair around the K blocks
     shot.synchronize()
+    kt = shot.step_kernel_time()
+    shot.time_step_kernel(False)
     barrier(dist)
     launches = shot.launches() - launches0
     clk = clocks.stop()
@@ -497,15 +508,20 @@ def run_ours(args, world, rank, local, dist) -> None:
     rate, t_max = replica_throughput(dist, float(cells) * S * K, ms / 1e3)
     value = rate / 1e9
 
-    # roofline of the step kernel (one launch per time step on this workload)
-    per_launch_s = (ms / 1e3) / (K * S)
-    achieved = bpc * cells / per_launch_s / 1e9
+    # roofline of the interior step kernel: algorithmic bytes of one launch
+    # (bpc per cell of its region: each field read and written once per
+    # launch, whether it advances them one time step or two) over its mean
+    # event-timed launch duration
+    per_launch_s = kt["ms"] / 1e3 / max(kt["launches"], 1)
+    alg_bytes = bpc * kt["cells"]
+    achieved = alg_bytes / per_launch_s / 1e9
+    step_gbs = bpc * cells / ((ms / 1e3) / (K * S)) / 1e9   # bpc per cell-update at the whole-step rate
     peaks = measured_peaks()
     peak = peaks.get("hbm_gbs")
     peak_src = "measured"
     if not peak:
         peak, peak_src = 6800.0, "fallback"
-    traffic = profile_traffic(kernel) if (store == 0 and args.size == 8192) else None
+    traffic = profile_traffic(kernel, kt["cells"]) if (store == 0 and args.size == 8192) else None
 
     # end to end through the C ABI with host buffers
     e2e = None
@@ -555,7 +571,13 @@ def run_ours(args, world, rank, local, dist) -> None:
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic,
                              "peak_source": peak_src, "kernel": kernel,
-                             "algorithmic_bytes_per_launch": bpc * cells},
+                             "algorithmic_bytes_per_launch": alg_bytes,
+                             "cells_per_launch": kt["cells"], "steps_per_launch": kt["steps"],
+                             "launches_timed": kt["launches"], "mean_launch_us": per_launch_s * 1e6,
+                             "step_rate_gbs_at_36_b_per_cell_update": step_gbs,
+                             "note": "achieved: the interior kernel alone (event-timed on its stream); "
+                                     "step_rate: whole steps at bpc per cell-update, above the copy peak "
+                                     "when a launch advances its cells two steps"},
                 "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk,
                 "finite": ok, "precision": precision, "batched": batched, "serving": serving}
         print(json.dumps(line), flush=True)

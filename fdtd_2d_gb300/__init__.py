@@ -173,6 +173,9 @@ def _lib():
         "fdtd2d_write_rc_lines": (C.c_int, [vp, _ip, C.c_int32, C.c_char_p]),
         "fdtd2d_write_tof": (C.c_int, [vp, _fp, C.c_int32, C.c_char_p]),
         "fdtd2d_run_timed": (C.c_int, [vp, C.c_int32, C.c_int32, _fp]),
+        "fdtd2d_time_step_kernel": (C.c_int, [vp, C.c_int]),
+        "fdtd2d_step_kernel_time": (C.c_int, [vp, _dp, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                              C.POINTER(C.c_int32)]),
         "fdtd2d_stability": (C.c_double, [C.POINTER(Setup)]),
         "fdtd2d_check_finite_noalloc": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int64), C.c_void_p]),
     }
@@ -340,6 +343,18 @@ class Shot:
         ms = C.c_float()
         _check(_lib().fdtd2d_run_timed(self._h, n_first, n_last, C.byref(ms)), "run_timed")
         return float(ms.value)
+
+    def time_step_kernel(self, on: bool = True) -> None:
+        """Start (or stop and clear) event timing of the interior step kernel."""
+        _check(_lib().fdtd2d_time_step_kernel(self._h, int(on)), "time_step_kernel")
+
+    def step_kernel_time(self) -> dict:
+        """Device time of the interior step kernel's timed launches: total ms,
+        launches, cells one launch updates and the time steps it advances."""
+        ms, n, cells, steps = C.c_double(), C.c_int64(), C.c_int64(), C.c_int32()
+        _check(_lib().fdtd2d_step_kernel_time(self._h, C.byref(ms), C.byref(n), C.byref(cells), C.byref(steps)),
+               "step_kernel_time")
+        return {"ms": ms.value, "launches": n.value, "cells": cells.value, "steps": steps.value}
 
     def synchronize(self) -> None:
         _check(_lib().fdtd2d_synchronize(self._h), "synchronize")

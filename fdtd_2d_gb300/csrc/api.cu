@@ -11,6 +11,10 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -331,6 +335,56 @@ void swap_slots(DevShot& h, TensorMaps& m, int a, int b) {
   std::swap(m.e[a], m.e[b]);
 }
 
+// Interior-kernel timing (fdtd2d_time_step_kernel): an event pair around a
+// launch on the shot stream.  Pending pairs are folded into the totals when
+// read, or when many have piled up.
+cudaEvent_t prof_event(fdtd2d_ctx* c) {
+  if (!c->prof_pool.empty()) {
+    cudaEvent_t e = c->prof_pool.back();
+    c->prof_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  return cudaEventCreate(&e) == cudaSuccess ? e : nullptr;
+}
+
+cudaError_t prof_fold(fdtd2d_ctx* c) {
+  cudaError_t r = cudaSuccess;
+  for (auto& pr : c->prof_pending) {
+    float ms = 0.f;
+    cudaError_t e = cudaEventSynchronize(pr.second);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, pr.first, pr.second);
+    if (e == cudaSuccess) {
+      c->prof_ms += ms;
+      ++c->prof_n;
+    } else {
+      r = e;
+    }
+    c->prof_pool.push_back(pr.first);
+    c->prof_pool.push_back(pr.second);
+  }
+  c->prof_pending.clear();
+  return r;
+}
+
+// Start (e0 = nullptr) or end a timed launch; returns the start event.
+cudaEvent_t prof_mark(fdtd2d_ctx* c, cudaEvent_t e0, int64_t cells, int steps) {
+  if (!c->prof) return nullptr;
+  if (!e0) {
+    cudaEvent_t e = prof_event(c);
+    if (e) cudaEventRecord(e, c->stream);
+    return e;
+  }
+  cudaEvent_t e1 = prof_event(c);
+  if (!e1) return nullptr;
+  cudaEventRecord(e1, c->stream);
+  c->prof_pending.emplace_back(e0, e1);
+  c->prof_cells = cells;
+  c->prof_steps = steps;
+  if (c->prof_pending.size() >= 4096) prof_fold(c);
+  return nullptr;
+}
+
 // What one two-step pair launches: the interior kernel's shape, units and
 // CTAs, the CPML-band kernel's, and the interior region.
 struct PairPlan {
@@ -366,7 +420,9 @@ cudaError_t issue_pair(fdtd2d_ctx* c, const PairPlan& p, DevShot& h, TensorMaps&
   DevShot t2 = h;          // step n+1: reads slot b, writes slot a = the state n+1 buffer
   t2.fb[a] = h.fb[2];
   cudaError_t x = cudaStreamWaitEvent(c->side, c->ev_t, 0);
+  cudaEvent_t p0 = prof_mark(c, nullptr, 0, 2);
   if (x == cudaSuccess) x = launch_step_tmat2(p.k, ti, tm, p.tu, p.ntu, n, p.tctas, c->d_ctr, c->d_err, c->stream);
+  if (p0) prof_mark(c, p0, (int64_t)(p.ci1 - p.ci0) * (p.ri1 - p.ri0), 2);
   if (x == cudaSuccess) x = cudaEventRecord(c->ev_t, c->stream);
   if (x == cudaSuccess) x = launch_step_tma(p.q, h, p.eu, p.neu, n, p.ectas, c->d_err, c->side);
   if (x == cudaSuccess) x = cudaEventRecord(c->ev_a, c->side);
@@ -380,15 +436,54 @@ cudaError_t issue_pair(fdtd2d_ctx* c, const PairPlan& p, DevShot& h, TensorMaps&
   return x;
 }
 
+// Kernel choices found by the create-time timing, per shot class (device,
+// grid, CPML depth, storage, drive map, the FDTD2D_* overrides): later shots
+// of the same class take the stored choice without timing.  `k` is the
+// tensor shape (-1: the one-row kernel alone), `q` the one-row shape, `lv`
+// the tensor path's steps per pass.
+struct KernelChoice {
+  int k = -1, q = 0, lv = 1;
+};
+using ChoiceKey = std::tuple<int, int, int, int, int, int, std::string>;
+std::mutex g_choice_mu;
+std::map<ChoiceKey, KernelChoice> g_choice;
+
+ChoiceKey choice_key(const fdtd2d_ctx* c, int device, const char* what) {
+  std::string env = what;
+  for (const char* v : {"FDTD2D_TMAT", "FDTD2D_TB", "FDTD2D_TMA", "FDTD2D_TMA_AUTOTUNE", "FDTD2D_TMAT_AUTOTUNE"}) {
+    const char* x = std::getenv(v);
+    env += '|';
+    env += x ? x : "-";
+  }
+  return ChoiceKey{device, c->nx, c->ny, c->npml, c->h.store, c->h.kp != nullptr, env};
+}
+
+bool find_choice(const ChoiceKey& key, KernelChoice* out) {
+  std::lock_guard<std::mutex> lock(g_choice_mu);
+  auto it = g_choice.find(key);
+  if (it == g_choice.end()) return false;
+  *out = it->second;
+  return true;
+}
+
+void keep_choice(const ChoiceKey& key, const KernelChoice& ch) {
+  std::lock_guard<std::mutex> lock(g_choice_mu);
+  g_choice[key] = ch;
+}
+
 // Multi-row tensor path (step_tmat.cu) for the interior of the shot, beside
 // the staged kernel on the CPML bands and rows.  Times every tensor shape that
 // fits the grid (tensor kernel on the interior units + staged kernel on the
 // rest, issued as fdtd2d_run issues them, traces and DFT off, re-run
 // idempotently) against the staged kernel alone, and keeps the fastest per
 // step.  Each tensor shape is tried in its one-step form and in its two-step
-// form (two time steps per pass over the fields; a third field buffer).
-// FDTD2D_TMAT=0 leaves the tensor path off, FDTD2D_TMAT=W,R,ST forces a
-// shape; FDTD2D_TB=0 leaves the two-step form out, FDTD2D_TB=1 keeps only it.
+// form (two time steps per pass over the fields; two more field buffers).
+// The trials cover the shapes that win on GB300 (two tensor shapes, three
+// one-row shapes for the CPML bands) unless FDTD2D_TMAT_AUTOTUNE=full asks
+// for every compiled pair; a shot of a class timed before takes the stored
+// choice.  FDTD2D_TMAT=0 leaves the tensor path off, FDTD2D_TMAT=W,R,ST
+// forces a shape; FDTD2D_TB=0 leaves the two-step form out, FDTD2D_TB=1
+// keeps only it.
 int setup_tmat(fdtd2d_ctx* c, int device) {
   const char* env = std::getenv("FDTD2D_TMAT");
   if (env && std::strcmp(env, "0") == 0) return FDTD2D_OK;
@@ -404,7 +499,17 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
       }
   }
   const char* tbe = std::getenv("FDTD2D_TB");
-  const int tb_mode = tbe ? std::atoi(tbe) : -1;   // -1 both forms, 0 one-step only, 1 two-step only
+  int tb_mode = tbe ? std::atoi(tbe) : -1;   // -1 both forms, 0 one-step only, 1 two-step only
+  const ChoiceKey key = choice_key(c, device, "tmat");
+  KernelChoice known;
+  const bool have = find_choice(key, &known);
+  if (have && known.k < 0) return FDTD2D_OK;   // the one-row kernel alone won for this class
+  if (have) {
+    forced = known.k;
+    tb_mode = known.lv == 2 ? 1 : 0;
+  }
+  const char* full_env = std::getenv("FDTD2D_TMAT_AUTOTUNE");
+  const bool full = full_env && std::strcmp(full_env, "full") == 0;
   DevShot& h = c->h;
   const int nx = c->nx, ny = c->ny, P = c->npml;
   if (!c->side) {
@@ -464,7 +569,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   };
   const int n1 = t.base_n + 1;
   float best = 1e30f;   // per step
-  if (forced < 0 && tb_mode != 1) {
+  if (!have && forced < 0 && tb_mode != 1) {
     best = timed([&] { return launch_step_tma(c->tma_shape, t, c->d_units, c->n_units, n1, c->grid_warps, c->d_err,
                                               c->stream); });
     if (best < 0) best = 1e30f;
@@ -472,14 +577,16 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   int best_k = -1, best_q = -1, best_ectas = 0, best_l = 1;
   std::vector<int4> best_t, best_e;
   TensorMaps best_m{};
+  const int quick_q[3] = {tma_shape_find(2, 2), tma_shape_find(4, 2), tma_shape_find(4, 3)};
   for (int k = 0; k < tmat_shape_count(); ++k) {
     if (forced >= 0 && k != forced) continue;
+    if (forced < 0 && !full && k >= 2) continue;   // shapes 0 and 1: the ones that win
     const int bt = tmat_band_cols(k), R = tmat_rows(k);
     TensorMaps maps{};
     if (ny - 2 * P < 4 * R + 2 || !encode_maps(h, nx, ny, tmat_box_cols(k), R, &maps)) continue;
     // every one-row shape is a candidate for the CPML bands and rows
     // (FDTD2D_TMA=W,ST forces one)
-    const int q_forced = tma_shape_parse(std::getenv("FDTD2D_TMA"));
+    const int q_forced = have ? known.q : tma_shape_parse(std::getenv("FDTD2D_TMA"));
     // both forms' launch attributes are set here: the two-step path also
     // runs single steps (an odd step, a step the line probe reads)
     const int tctas1 = tmat_resident_ctas(k, h.store, device);
@@ -494,6 +601,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
       const int ri0 = lv == 1 ? P : P + 2, ri1 = ny - ri0;
       for (int q = 0; q < tma_shape_count(); ++q) {
         if (q_forced >= 0 && q != q_forced) continue;
+        if (q_forced < 0 && !full && q != quick_q[0] && q != quick_q[1] && q != quick_q[2]) continue;
         const int b1 = tma_band_cols(q);
         const int ci0 = (ri0 + b1 - 1) / b1 * b1;
         const int ci1 = ci0 + std::max(0, (nx - ri0 - ci0) / bt) * bt;
@@ -520,7 +628,9 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
         if (e == cudaSuccess) e = cudaEventRecord(c->ev_m, c->stream);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_m, 0);
         // one trial step (pair) as fdtd2d_run issues it: the two kernels on two streams
-        if (e == cudaSuccess && lv == 1) {
+        if (e == cudaSuccess && have) {
+          ms = 0.f;   // the stored choice
+        } else if (e == cudaSuccess && lv == 1) {
           ms = timed([&] {
             cudaError_t x = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
             if (x == cudaSuccess) x = launch_step_tmat(k, t, maps, dt, (int)tu.size(), n1, tctas, c->d_err, c->stream);
@@ -581,6 +691,13 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   int derr = 0;
   if (cudaMemcpy(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return FDTD2D_ERR_CUDA;
   if (derr != kErrNone) return FDTD2D_ERR_TIMEOUT;
+  if (!have) {
+    KernelChoice ch;
+    ch.k = best_k;
+    ch.q = best_q;
+    ch.lv = best_l;
+    keep_choice(key, ch);
+  }
   if (best_k < 0) return FDTD2D_OK;
   cudaError_t e = dalloc(c, &c->d_tunits, best_t.size());
   if (e == cudaSuccess) e = dalloc(c, &c->d_eunits, best_e.size());
@@ -916,10 +1033,14 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
     // unless FDTD2D_TMA_AUTOTUNE=0 (then shape 0).
     const int forced = tma_shape_parse(std::getenv("FDTD2D_TMA"));
     const char* at = std::getenv("FDTD2D_TMA_AUTOTUNE");
+    KernelChoice known;
     if (member) {
       // batch members are stepped by the batch's kernel
     } else if (forced >= 0) {
       c->tma_shape = forced;
+    } else if (!(at && std::strcmp(at, "0") == 0) && c->n_steps >= 1 &&
+               find_choice(choice_key(c, device, "tma"), &known)) {
+      c->tma_shape = known.q;   // timed for a shot of this class before
     } else if (!(at && std::strcmp(at, "0") == 0) && c->n_steps >= 1) {
       // Each trial re-runs step 1 with traces and the DFT switched off: a
       // step reads one buffer set and overwrites the other with values that
@@ -967,6 +1088,9 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
         return FDTD2D_ERR_TIMEOUT;
       }
       c->tma_shape = best_k;
+      KernelChoice ch;
+      ch.q = best_k;
+      keep_choice(choice_key(c, device, "tma"), ch);
     }
     c->grid_warps = tma_resident_ctas(c->tma_shape, P, h.store, device);  // CTAs for this path
     units = make_units(0, nx, ny, c->grid_warps, tma_band_cols(c->tma_shape));
@@ -1028,9 +1152,11 @@ int fdtd2d_run(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
       // once.  Each waits for the other's kernel of the previous step: it
       // overwrites the buffer that kernel read.
       e = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
+      cudaEvent_t p0 = c->tb ? nullptr : prof_mark(c, nullptr, 0, 1);
       if (e == cudaSuccess)
         e = launch_step_tmat(c->tmat_shape, c->h, c->maps, c->d_tunits, c->n_tunits, n, c->tmat_ctas, c->d_err,
                              c->stream);
+      if (p0) prof_mark(c, p0, (int64_t)(c->reg[1] - c->reg[0]) * (c->reg[3] - c->reg[2]), 1);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_t, 0);
       if (e == cudaSuccess) e = cudaEventRecord(c->ev_t, c->stream);
       if (e == cudaSuccess) {
@@ -1042,8 +1168,10 @@ int fdtd2d_run(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
       if (e == cudaSuccess && (c->n_rc > 0 || c->line_n > 0 || n == n_last))
         e = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
     } else {
+      cudaEvent_t p0 = prof_mark(c, nullptr, 0, 1);
       e = c->tma ? launch_step_tma(c->tma_shape, c->h, c->d_units, c->n_units, n, c->grid_warps, c->d_err, c->stream)
                  : launch_step(c->h, c->d_units, c->n_units, n, c->medium, c->grid_warps, c->stream);
+      if (p0) prof_mark(c, p0, (int64_t)c->nx * c->ny, 1);
     }
     if (e != cudaSuccess) return fail_cuda(c, e);
     ++c->launches;
@@ -1097,6 +1225,29 @@ int fdtd2d_run_timed(fdtd2d_ctx* c, int32_t n_first, int32_t n_last, float* elap
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   return rc;
+}
+
+int fdtd2d_time_step_kernel(fdtd2d_ctx* c, int on) {
+  if (!c) return FDTD2D_ERR_INVALID;
+  if (c->batch) return FDTD2D_ERR_STATE;
+  cudaSetDevice(c->device);
+  cudaError_t e = prof_fold(c);
+  c->prof = on != 0;
+  c->prof_ms = 0;
+  c->prof_n = 0;
+  return e == cudaSuccess ? FDTD2D_OK : fail_cuda(c, e);
+}
+
+int fdtd2d_step_kernel_time(fdtd2d_ctx* c, double* ms, int64_t* launches, int64_t* cells, int32_t* steps) {
+  if (!c || !ms || !launches || !cells || !steps) return FDTD2D_ERR_INVALID;
+  cudaSetDevice(c->device);
+  cudaError_t e = prof_fold(c);
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  *ms = c->prof_ms;
+  *launches = c->prof_n;
+  *cells = c->prof_cells;
+  *steps = c->prof_steps;
+  return FDTD2D_OK;
 }
 
 double fdtd2d_stability(const fdtd2d_setup* s) {
@@ -1385,6 +1536,8 @@ int fdtd2d_destroy(fdtd2d_ctx* c) {
   }
   for (cudaEvent_t ev : {c->ev_t, c->ev_e, c->ev_m, c->ev_a})
     if (ev) cudaEventDestroy(ev);
+  for (auto& pr : c->prof_pending) c->prof_pool.insert(c->prof_pool.end(), {pr.first, pr.second});
+  for (cudaEvent_t ev : c->prof_pool) cudaEventDestroy(ev);
   delete c;
   return FDTD2D_OK;
 }

@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cstdint>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -51,6 +52,13 @@ struct fdtd2d_ctx {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_t = nullptr, ev_e = nullptr, ev_m = nullptr, ev_a = nullptr;
   char kernel_name[96] = {0};
+  // event timing of the interior kernel (fdtd2d_time_step_kernel)
+  bool prof = false;
+  std::vector<cudaEvent_t> prof_pool;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_pending;
+  double prof_ms = 0;
+  int64_t prof_n = 0, prof_cells = 0;
+  int prof_steps = 1;
   // wave-front tracker and line probe
   int n_rc = 0, rc_j_cut = 0;
   float rc_level = 0;

@@ -285,6 +285,18 @@ int fdtd2d_device_count(void);
    context's stream; *elapsed_ms receives the device time of the whole range. */
 int fdtd2d_run_timed(fdtd2d_ctx *ctx, int32_t n_first, int32_t n_last, float *elapsed_ms);
 
+/* Event timing of the kernel that steps the interior of the grid, the one
+   that sets the step time: the two-step tensor kernel when the context runs
+   two steps per pass (its launches only), else the one-step tensor kernel,
+   else the kernel that steps the whole grid.  on = 1 records a CUDA event
+   pair on the shot stream around each of its launches from then on; on = 0
+   stops and clears the totals.  fdtd2d_step_kernel_time reports the summed
+   device time of the launches timed so far (*ms), their number (*launches),
+   the cells one launch updates (*cells) and the time steps it advances them
+   (*steps).  No counterpart in the reference. */
+int fdtd2d_time_step_kernel(fdtd2d_ctx *ctx, int on);
+int fdtd2d_step_kernel_time(fdtd2d_ctx *ctx, double *ms, int64_t *launches, int64_t *cells, int32_t *steps);
+
 /* Stability number of the explicit update with the Drude current:
    (c dt)^2 (1/dx^2 + 1/dy^2) + (w_p,max dt / 2)^2, w_p,max from the largest
    plasma drive of the setup.  Above 1 the scheme grows without bound. */
