@@ -247,14 +247,23 @@ def run_batched(args, local: int) -> tuple[dict, float]:
              for k in range(args.batch_shots)]
     probs = [F.Problem.from_spec(**sp) for sp in specs]
     cells = sum(p.nx * p.ny * p.n_steps for p in probs)
-    t = time.perf_counter()
-    plain_dft = []
-    for p in probs:
-        with F.Shot(p, local) as s:
-            s.run(1, p.n_steps)
-            s.traces()
-            plain_dft.append(s.dft())
-    tp = time.perf_counter() - t
+
+    def plain_pass():
+        t = time.perf_counter()
+        out = []
+        for p in probs:
+            with F.Shot(p, local) as s:
+                s.run(1, p.n_steps)
+                s.traces()
+                out.append(s.dft())
+        return time.perf_counter() - t, out
+
+    # cold: every grid size new to the process (kernel choices timed at
+    # create); warm: the same shots again with the choices kept
+    F.clear_kernel_choices()
+    tp, plain_dft = plain_pass()
+    tw, _ = plain_pass()
+    F.clear_kernel_choices()
     t = time.perf_counter()
     with F.Batch(local) as b:
         ids = [b.add(p) for p in probs]
@@ -270,6 +279,7 @@ def run_batched(args, local: int) -> tuple[dict, float]:
             batch_dft.append(sh.dft())
         name = b.kernel_name()
         launches = b.launches()
+        solo = sum(1 for i in ids if b.shot(i).kernel_name().startswith("step_tmat"))
     tb = time.perf_counter() - t
     same = all(np.array_equal(x, y) for x, y in zip(plain_dft, batch_dft))
     n = len(probs)
@@ -278,10 +288,14 @@ def run_batched(args, local: int) -> tuple[dict, float]:
                                  f"{args.batch_step_scale} ({sum(p.n_steps for p in probs)} steps in all)",
            "cell_updates": cells, "plain_shots_per_s": n / tp, "batched_shots_per_s": n / tb,
            "speedup": tp / tb, "plain_gcells": cells / tp / 1e9, "batched_gcells": cells / tb / 1e9,
-           "kernel": name, "gpu_launches": int(launches),
+           "plain_warm_shots_per_s": n / tw, "speedup_vs_warm": tw / tb, "plain_warm_gcells": cells / tw / 1e9,
+           "kernel": name, "tensor_path_members": solo, "gpu_launches": int(launches),
            "dft_equal_to_plain": bool(same),
-           "note": "end to end from host setups: create/upload, all steps, traces + DFT read back; the batch "
-                   "is one persistent launch per step in CUDA-graph blocks of 16"}
+           "note": "end to end from host setups: create/upload, all steps, traces + DFT read back. plain: one "
+                   "shot at a time through the single-shot ABI, cold (every grid size new, kernel choice "
+                   "timed at create) and warm (the same shots again, choices kept); batch (cold): grids of "
+                   ">= 2^21 cells as solo members (own streams, two-step tensor path), the rest in one "
+                   "persistent launch per step in CUDA-graph blocks of 16"}
     return out, cells / tb
 
 

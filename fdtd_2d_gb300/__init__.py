@@ -174,6 +174,7 @@ def _lib():
         "fdtd2d_write_tof": (C.c_int, [vp, _fp, C.c_int32, C.c_char_p]),
         "fdtd2d_run_timed": (C.c_int, [vp, C.c_int32, C.c_int32, _fp]),
         "fdtd2d_time_step_kernel": (C.c_int, [vp, C.c_int]),
+        "fdtd2d_clear_kernel_choices": (None, []),
         "fdtd2d_step_kernel_time": (C.c_int, [vp, _dp, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                               C.POINTER(C.c_int32)]),
         "fdtd2d_stability": (C.c_double, [C.POINTER(Setup)]),
@@ -431,6 +432,11 @@ class Shot:
             self.close()
         except Exception:
             pass
+
+
+def clear_kernel_choices() -> None:
+    """Forget the kernel choices shot creation keeps per shot class."""
+    _lib().fdtd2d_clear_kernel_choices()
 
 
 class Batch:

@@ -437,10 +437,13 @@ cudaError_t issue_pair(fdtd2d_ctx* c, const PairPlan& p, DevShot& h, TensorMaps&
 }
 
 // Kernel choices found by the create-time timing, per shot class (device,
-// grid, CPML depth, storage, drive map, the FDTD2D_* overrides): later shots
-// of the same class take the stored choice without timing.  `k` is the
-// tensor shape (-1: the one-row kernel alone), `q` the one-row shape, `lv`
-// the tensor path's steps per pass.
+// grid size class, CPML depth in steps of 16, storage, drive map, the
+// FDTD2D_* overrides):
+// later shots of the same class take the stored choice without timing.  The
+// size class of a side n is ceil(log2 n) and, within it, the half it falls
+// in, so that shots of similar grids share one timing.  `k` is the tensor
+// shape (-1: the one-row kernel alone), `q` the one-row shape, `lv` the
+// tensor path's steps per pass.
 struct KernelChoice {
   int k = -1, q = 0, lv = 1;
 };
@@ -455,7 +458,12 @@ ChoiceKey choice_key(const fdtd2d_ctx* c, int device, const char* what) {
     env += '|';
     env += x ? x : "-";
   }
-  return ChoiceKey{device, c->nx, c->ny, c->npml, c->h.store, c->h.kp != nullptr, env};
+  auto cls = [](int n) {
+    int b = 0;
+    while ((1 << b) < n) ++b;                      // n in (2^(b-1), 2^b]
+    return 2 * b + (n > 3 * (1 << b) / 4 ? 1 : 0);   // upper or lower half of that range
+  };
+  return ChoiceKey{device, cls(c->nx), cls(c->ny), (c->npml + 15) / 16, c->h.store, c->h.kp != nullptr, env};
 }
 
 bool find_choice(const ChoiceKey& key, KernelChoice* out) {
@@ -1225,6 +1233,11 @@ int fdtd2d_run_timed(fdtd2d_ctx* c, int32_t n_first, int32_t n_last, float* elap
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   return rc;
+}
+
+void fdtd2d_clear_kernel_choices(void) {
+  std::lock_guard<std::mutex> lock(g_choice_mu);
+  g_choice.clear();
 }
 
 int fdtd2d_time_step_kernel(fdtd2d_ctx* c, int on) {

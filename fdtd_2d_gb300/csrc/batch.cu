@@ -43,7 +43,22 @@ struct Member {
   int32_t base = 0;     // global steps issued before its first step
   bool live = false;
   bool done = false;    // all its steps issued
+  // A solo member is a full single shot on its own streams (the tensor path:
+  // two steps per pass where it wins), stepped by fdtd2d_run from the batch's
+  // run calls; `ev` holds the events recorded after its recent run calls on
+  // its stream, oldest first.
+  bool solo = false;
+  std::vector<cudaEvent_t> ev;
 };
+
+// Grids of at least this many cells (2^21, about 1448^2) join a batch as
+// solo members (their own tensor-path launches fill the GPU); smaller ones
+// share the batch kernel.  FDTD2D_BATCH_SOLO_CELLS overrides it (0: none
+// solo).
+int64_t solo_cells() {
+  const char* v = std::getenv("FDTD2D_BATCH_SOLO_CELLS");
+  return v ? std::atoll(v) : (int64_t)1 << 21;
+}
 
 }  // namespace
 
@@ -100,12 +115,12 @@ std::vector<int4> build_units(const fdtd2d_batch* b, int shape, int ctas) {
   const int band = tma_band_cols(shape);
   int64_t band_rows = 0;
   for (const Member& x : b->m)
-    if (x.live && !x.done) band_rows += (int64_t)((x.ctx->nx + band - 1) / band) * (x.ctx->ny - 1);
+    if (x.live && !x.done && !x.solo) band_rows += (int64_t)((x.ctx->nx + band - 1) / band) * (x.ctx->ny - 1);
   int rows = (int)std::min<int64_t>(512, std::max<int64_t>(16, (band_rows + 6LL * ctas - 1) / (6LL * ctas)));
   std::vector<int4> u;
   for (int k = 0; k < (int)b->m.size(); ++k) {
     const Member& x = b->m[k];
-    if (x.live && !x.done) shot_units(u, k, x.ctx->nx, x.ctx->ny, band, rows);
+    if (x.live && !x.done && !x.solo) shot_units(u, k, x.ctx->nx, x.ctx->ny, band, rows);
   }
   return u;
 }
@@ -207,6 +222,72 @@ cudaError_t capture_block(fdtd2d_batch* b, int K, cudaGraphExec_t* out) {
   return e;
 }
 
+int add_solo(fdtd2d_batch* b, const fdtd2d_setup* s, int64_t bytes, int32_t* shot) {
+  int slot = -1;
+  for (int k = 0; k < (int)b->m.size(); ++k)
+    if (!b->m[k].live) { slot = k; break; }
+  if (slot < 0) {
+    if ((int)b->m.size() >= kMaxShots) return FDTD2D_ERR_BUDGET;
+    b->m.emplace_back();
+    slot = (int)b->m.size() - 1;
+  }
+  fdtd2d_ctx* c = nullptr;
+  const int rc = create_ctx(s, b->device, false, &c);   // its own streams, kernel choice timed
+  if (rc) return rc;
+  // the bytes it holds: two more field buffers on the two-step path
+  if (c->tb) bytes += 2 * c->h.cells * 4 * store_bytes(c->h.store);
+  Member& x = b->m[slot];
+  x.ctx = c;
+  x.bytes = bytes;
+  x.base = b->g;
+  x.live = true;
+  x.done = c->n_steps <= 0;
+  x.solo = true;
+  b->used += bytes;
+  *shot = slot;
+  return FDTD2D_OK;
+}
+
+// Issue up to n more steps of every solo member on its own streams (the
+// host does not wait), keeping at most two run calls of each in flight.
+int run_solo(fdtd2d_batch* b, int32_t n) {
+  for (Member& x : b->m) {
+    if (!x.live || !x.solo || x.done) continue;
+    fdtd2d_ctx* c = x.ctx;
+    while (x.ev.size() >= 2) {
+      const cudaError_t e = cudaEventSynchronize(x.ev.front());
+      if (e != cudaSuccess) return fail(b, e);
+      cudaEventDestroy(x.ev.front());
+      x.ev.erase(x.ev.begin());
+    }
+    const int32_t last = std::min(c->n_steps, c->step + n);
+    const int64_t l0 = c->launches;
+    const int rc = fdtd2d_run(c, c->step + 1, last);
+    if (rc) {
+      b->last_cuda = c->last_cuda;
+      return rc;
+    }
+    b->launches += c->launches - l0;
+    cudaEvent_t e = nullptr;
+    cudaError_t ce = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventRecord(e, c->stream);
+    if (ce != cudaSuccess) return fail(b, ce);
+    x.ev.push_back(e);
+    if (c->step >= c->n_steps) x.done = true;
+  }
+  return FDTD2D_OK;
+}
+
+// A solo member whose steps have all been issued and have completed.
+bool solo_complete(const Member& x) {
+  return x.solo && x.done && (x.ev.empty() || cudaEventQuery(x.ev.back()) == cudaSuccess);
+}
+
+void release_events(Member& x) {
+  for (cudaEvent_t e : x.ev) cudaEventDestroy(e);
+  x.ev.clear();
+}
+
 }  // namespace
 
 extern "C" {
@@ -252,6 +333,12 @@ int fdtd2d_batch_add(fdtd2d_batch* b, const fdtd2d_setup* s, int32_t* shot) {
   const int64_t bytes = fdtd2d_device_bytes(s);
   if (bytes < 0) return FDTD2D_ERR_INVALID;
   if (b->used + bytes > b->budget) return FDTD2D_ERR_BUDGET;
+  // A large grid goes solo when it fits with the two extra field buffers of
+  // the two-step path.
+  const int64_t field_buf = (int64_t)buffer_floats(s->nx, s->ny) * 4 * 4;
+  const int64_t cells = (int64_t)s->nx * s->ny;
+  const int64_t sc = solo_cells();
+  if (sc > 0 && cells >= sc && b->used + bytes + 2 * field_buf <= b->budget) return add_solo(b, s, bytes, shot);
   int slot = -1;
   for (int k = 0; k < (int)b->m.size(); ++k)
     if (!b->m[k].live) { slot = k; break; }
@@ -289,9 +376,13 @@ int fdtd2d_batch_add(fdtd2d_batch* b, const fdtd2d_setup* s, int32_t* shot) {
 int fdtd2d_batch_run(fdtd2d_batch* b, int32_t n_steps) {
   if (!b || n_steps < 0) return FDTD2D_ERR_INVALID;
   cudaSetDevice(b->device);
+  if (n_steps > 0) {
+    const int rc = run_solo(b, n_steps);
+    if (rc) return rc;
+  }
   while (n_steps > 0) {
     bool any = false;
-    for (const Member& x : b->m) any = any || (x.live && !x.done);
+    for (const Member& x : b->m) any = any || (x.live && !x.done && !x.solo);
     if (!any) return FDTD2D_OK;
     if (!b->tuned) {
       const int forced = tma_shape_parse(std::getenv("FDTD2D_TMA"));
@@ -334,7 +425,7 @@ int fdtd2d_batch_run(fdtd2d_batch* b, int32_t n_steps) {
     b->launches += K;
     n_steps -= K;
     for (Member& x : b->m) {
-      if (!x.live) continue;
+      if (!x.live || x.solo) continue;
       x.ctx->step = std::min(x.ctx->n_steps, std::max(0, b->g - x.base));
       if (!x.done && x.ctx->step >= x.ctx->n_steps) {
         x.done = true;
@@ -348,6 +439,11 @@ int fdtd2d_batch_run(fdtd2d_batch* b, int32_t n_steps) {
 int fdtd2d_batch_synchronize(fdtd2d_batch* b) {
   if (!b) return FDTD2D_ERR_INVALID;
   cudaSetDevice(b->device);
+  for (Member& x : b->m)
+    if (x.live && x.solo) {
+      const int rc = fdtd2d_synchronize(x.ctx);
+      if (rc) return rc;
+    }
   cudaError_t e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) return fail(b, e);
   int err = 0;
@@ -370,7 +466,8 @@ int fdtd2d_batch_remove(fdtd2d_batch* b, int32_t shot) {
   if (!b || shot < 0 || shot >= (int)b->m.size() || !b->m[shot].live) return FDTD2D_ERR_INVALID;
   cudaSetDevice(b->device);
   Member& x = b->m[shot];
-  fdtd2d_destroy(x.ctx);   // memory released behind the queued kernels
+  fdtd2d_destroy(x.ctx);   // memory released behind the queued kernels (a solo shot waits for its own)
+  release_events(x);
   b->used -= x.bytes;
   x = Member();
   b->dirty = true;
@@ -394,7 +491,10 @@ int fdtd2d_batch_destroy(fdtd2d_batch* b) {
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
   for (Member& x : b->m)
-    if (x.live) fdtd2d_destroy(x.ctx);
+    if (x.live) {
+      fdtd2d_destroy(x.ctx);
+      release_events(x);
+    }
   drop_graphs(b);
   if (b->d_units) cudaFree(b->d_units);
   if (b->d_shots) cudaFree(b->d_shots);
@@ -473,7 +573,8 @@ int retire(fdtd2d_server* s, int* n_done) {
   s->blocks.erase(s->blocks.begin(), s->blocks.begin() + k);
   for (size_t r = 0; r < s->running.size();) {
     const Running x = s->running[r];
-    if (x.last_g > s->g_complete) {
+    const Member& mem = b->m[x.slot];
+    if (mem.solo ? !solo_complete(mem) : x.last_g > s->g_complete) {
       ++r;
       continue;
     }
@@ -551,9 +652,30 @@ int fdtd2d_server_step(fdtd2d_server* s) {
   int rc = retire(s, &n_done);
   if (rc) return rc;
   // 3. issue one block while any shot has steps left
-  bool steps_left = false;
-  for (const Running& x : s->running) steps_left = steps_left || x.last_g > b->g;
-  if (steps_left) {
+  bool steps_left = false, solo_left = false;
+  for (const Running& x : s->running) {
+    const Member& mem = b->m[x.slot];
+    if (mem.solo)
+      solo_left = solo_left || !mem.done;
+    else
+      steps_left = steps_left || x.last_g > b->g;
+  }
+  if (solo_left && !steps_left) {
+    // only solo members have steps left: issue theirs, then wait for the
+    // oldest run call of one of them instead of spinning
+    rc = run_solo(b, s->block);
+    if (rc) return rc;
+    for (const Running& x : s->running) {
+      Member& mem = b->m[x.slot];
+      if (mem.solo && !mem.ev.empty()) {
+        const cudaError_t we = cudaEventSynchronize(mem.ev.front());
+        if (we != cudaSuccess) return fail(b, we);
+        break;
+      }
+    }
+    rc = retire(s, &n_done);
+    if (rc) return rc;
+  } else if (steps_left) {
     rc = fdtd2d_batch_run(b, s->block);
     if (rc) return rc;
     cudaEvent_t e = take_event(s);
@@ -571,6 +693,18 @@ int fdtd2d_server_step(fdtd2d_server* s) {
     // nothing more to issue: wait for the oldest block instead of spinning
     const cudaError_t we = cudaEventSynchronize(s->blocks.front().second);
     if (we != cudaSuccess) return fail(b, we);
+    rc = retire(s, &n_done);
+    if (rc) return rc;
+  } else {
+    // only solo members still running, all issued: wait for one of them
+    for (const Running& x : s->running) {
+      const Member& mem = b->m[x.slot];
+      if (mem.solo && !mem.ev.empty()) {
+        const cudaError_t we = cudaEventSynchronize(mem.ev.back());
+        if (we != cudaSuccess) return fail(b, we);
+        break;
+      }
+    }
     rc = retire(s, &n_done);
     if (rc) return rc;
   }

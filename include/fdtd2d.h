@@ -295,6 +295,10 @@ int fdtd2d_run_timed(fdtd2d_ctx *ctx, int32_t n_first, int32_t n_last, float *el
    the cells one launch updates (*cells) and the time steps it advances them
    (*steps).  No counterpart in the reference. */
 int fdtd2d_time_step_kernel(fdtd2d_ctx *ctx, int on);
+
+/* Forget the kernel choices fdtd2d_create keeps per shot class (the next
+   shot of every class is timed again).  No counterpart in the reference. */
+void fdtd2d_clear_kernel_choices(void);
 int fdtd2d_step_kernel_time(fdtd2d_ctx *ctx, double *ms, int64_t *launches, int64_t *cells, int32_t *steps);
 
 /* Stability number of the explicit update with the Drude current:

@@ -168,3 +168,59 @@ def test_serving_results_equal_alone(gpu):
     for k, (dft, tr) in enumerate(solo):
         assert np.array_equal(got[k]["dft"], dft), k
         assert np.array_equal(got[k]["det_ez"], tr), k
+
+
+def big_problem(k: int):
+    """A wide shot whose interior takes the tensor path when run alone."""
+    sp = shot_spec(k)
+    sp.update(nx=1400 + 64 * k, ny=260 + 16 * k, x_center=900.0, width=120.0)
+    sp["dft_freq"] = sp["freq"]
+    return F.Problem.from_spec(**sp)
+
+
+def test_solo_members_equal_alone(gpu, monkeypatch):
+    """Members of at least FDTD2D_BATCH_SOLO_CELLS cells are solo members:
+    full shots on their own streams (the tensor path, two steps per pass
+    where it wins) stepped from the batch's run calls beside the batch
+    kernel's members.  Every result equals its solo run bitwise."""
+    monkeypatch.setenv("FDTD2D_BATCH_SOLO_CELLS", "300000")
+    probs = problems(4) + [big_problem(0), big_problem(1)]
+    ref = [alone(p, gpu) for p in probs]
+    with F.Batch(gpu) as b:
+        ids = [b.add(p) for p in probs]
+        assert all(i is not None for i in ids)
+        names = [b.shot(i).kernel_name() for i in ids]
+        assert any(n.startswith("step_tmat") for n in names), names
+        while not all(b.finished(i) for i in ids):
+            b.run(37)
+        b.synchronize()
+        for i, r, p in zip(ids, ref, probs):
+            assert b.step(i) == p.n_steps
+            assert_same(snapshot(b.shot(i)), r, f"shot {i}")
+
+
+def test_serving_with_solo_members(gpu, monkeypatch):
+    """The serving loop with solo members among the shots (retired on their
+    own events): DFT and Ez traces equal each solo run bitwise."""
+    monkeypatch.setenv("FDTD2D_BATCH_SOLO_CELLS", "300000")
+    probs = problems(3) + [big_problem(0), big_problem(2)]
+    solo = []
+    for p in probs:
+        with F.Shot(p, gpu) as s:
+            s.run(1, p.n_steps)
+            solo.append((s.dft(), s.traces()["det_ez"]))
+    got = {}
+    with F.Server(gpu, block_steps=24) as srv:
+        arrivals = {0: [0, 3], 2: [1], 4: [4, 2]}
+        rnd = 0
+        while len(got) < len(probs):
+            for k in arrivals.get(rnd, []):
+                srv.submit(probs[k], k)
+            srv.step()
+            while (r := srv.pop()) is not None:
+                got[r["tag"]] = r
+            rnd += 1
+            assert rnd < 10000
+    for k, (dft, tr) in enumerate(solo):
+        assert np.array_equal(got[k]["dft"], dft), k
+        assert np.array_equal(got[k]["det_ez"], tr), k
