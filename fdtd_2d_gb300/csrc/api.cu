@@ -532,18 +532,38 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   // no kernel writes keep their values in every buffer), its unit counter,
   // and a scratch psi slab for the trials (a trial pair's second step writes
   // psi buffer 0).
-  const bool try2 = tb_mode != 0 && c->n_steps >= 2 && ny - 2 * P - 4 >= 8;
+  bool try2 = tb_mode != 0 && c->n_steps >= 2 && ny - 2 * P - 4 >= 8;
   float* psi_trial = nullptr;
   const size_t psi_floats = (size_t)h.psi_buf * 2 + 1024;
+  auto give_back = [&](float*& p) {
+    if (!p) return;
+    cudaFreeAsync(p, c->stream);
+    auto it = std::find(c->allocs.begin(), c->allocs.end(), (void*)p);
+    if (it != c->allocs.end()) c->allocs.erase(it);
+    p = nullptr;
+  };
   if (try2) {
     const size_t fbytes = (size_t)h.cells * 4 * store_bytes(h.store);
     cudaError_t e = dalloc(c, &h.fb[2], fbytes / 4);
     if (e == cudaSuccess) e = dalloc(c, &h.fb[3], fbytes / 4);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h.fb[2], h.fb[0], fbytes, cudaMemcpyDeviceToDevice, c->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h.fb[3], h.fb[0], fbytes, cudaMemcpyDeviceToDevice, c->stream);
     if (e == cudaSuccess && !c->d_ctr) e = dalloc(c, &c->d_ctr, 1);
     if (e == cudaSuccess) e = cudaMallocAsync(&psi_trial, psi_floats * 4, c->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(psi_trial, h.psi, psi_floats * 4, cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaErrorMemoryAllocation) {
+      // no room for the two-step form's buffers: the one-step forms only
+      cudaGetLastError();
+      give_back(h.fb[2]);
+      give_back(h.fb[3]);
+      if (psi_trial) cudaFreeAsync(psi_trial, c->stream);
+      psi_trial = nullptr;
+      try2 = false;
+      if (tb_mode == 1) return FDTD2D_OK;   // only the two-step form was asked for: the one-row kernel
+      e = cudaSuccess;
+    } else {
+      if (e == cudaSuccess) e = cudaMemcpyAsync(h.fb[2], h.fb[0], fbytes, cudaMemcpyDeviceToDevice, c->stream);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(h.fb[3], h.fb[0], fbytes, cudaMemcpyDeviceToDevice, c->stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(psi_trial, h.psi, psi_floats * 4, cudaMemcpyDeviceToDevice, c->stream);
+    }
     if (e != cudaSuccess) return fail_cuda(c, e);
   }
   DevShot t = h;
@@ -689,9 +709,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   if (h.fb[2] && !(best_k >= 0 && best_l == 2)) {
     // the two-step form lost: give its buffers back
     for (int b = 2; b < 4; ++b) {
-      cudaFreeAsync(h.fb[b], c->stream);
-      c->allocs.erase(std::find(c->allocs.begin(), c->allocs.end(), (void*)h.fb[b]));
-      h.fb[b] = nullptr;
+      give_back(h.fb[b]);
       std::memset(&best_m.hj[b], 0, sizeof best_m.hj[b]);
       std::memset(&best_m.e[b], 0, sizeof best_m.e[b]);
     }
