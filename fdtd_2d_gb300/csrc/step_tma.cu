@@ -53,7 +53,9 @@ struct Cfg {
   static constexpr uint32_t kXOffB = kPsiOffB + 2 * kPsiBytes;
   static constexpr uint32_t kStageBytes = kXOffB + 4 * kXSlot * 4;
   static constexpr size_t kSmem = (size_t)ST * kStageBytes;
-  static constexpr int kMinBlocks = W <= 4 ? 4 : 2;   // W = 8: caps registers at 128 per thread
+  // CTAs per SM the launch bounds ask for: W = 1 and 2 cap registers near
+  // 128 per thread (16 and 8 CTAs; no spills), W = 8 at 128 (2 CTAs)
+  static constexpr int kMinBlocks = W == 1 ? 16 : (W == 2 ? 8 : (W <= 4 ? 4 : 2));
   static_assert(kSegBytes % 16 == 0 && kPsiOffB % 16 == 0 && kXOffB % 16 == 0 && kStageBytes % 16 == 0,
                 "16-byte aligned stage slots");
 };
