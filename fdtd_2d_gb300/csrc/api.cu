@@ -486,7 +486,7 @@ void keep_choice(const ChoiceKey& key, const KernelChoice& ch) {
 // idempotently) against the staged kernel alone, and keeps the fastest per
 // step.  Each tensor shape is tried in its one-step form and in its two-step
 // form (two time steps per pass over the fields; two more field buffers).
-// The trials cover the shapes that win on GB300 (two tensor shapes, three
+// The trials cover the shapes that win on GB300 (three tensor shapes, three
 // one-row shapes for the CPML bands) unless FDTD2D_TMAT_AUTOTUNE=full asks
 // for every compiled pair; a shot of a class timed before takes the stored
 // choice.  FDTD2D_TMAT=0 leaves the tensor path off, FDTD2D_TMAT=W,R,ST
@@ -608,7 +608,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   const int quick_q[3] = {tma_shape_find(2, 2), tma_shape_find(4, 2), tma_shape_find(4, 3)};
   for (int k = 0; k < tmat_shape_count(); ++k) {
     if (forced >= 0 && k != forced) continue;
-    if (forced < 0 && !full && k >= 2) continue;   // shapes 0 and 1: the ones that win
+    if (forced < 0 && !full && k >= 2 && k != tmat_shape_find(4, 2, 2)) continue;   // the shapes that win
     const int bt = tmat_band_cols(k), R = tmat_rows(k);
     TensorMaps maps{};
     if (ny - 2 * P < 4 * R + 2 || !encode_maps(h, nx, ny, tmat_box_cols(k), R, &maps)) continue;

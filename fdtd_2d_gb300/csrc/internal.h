@@ -162,6 +162,7 @@ struct TensorMaps {
 // whose band and halo column lie outside the x strips and whose rows lie in
 // [npml, ny - npml).  Shapes: (warps, rows per stage, stages).
 int tmat_shape_count();
+int tmat_shape_find(int warps, int rows, int stages);   // -1 if not compiled
 void tmat_shape_dims(int shape, int* warps, int* rows, int* stages);
 int tmat_band_cols(int shape);
 int tmat_box_cols(int shape);   // columns per tensor box (band + 16 halo = boxes x box_cols)

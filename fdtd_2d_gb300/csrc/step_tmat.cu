@@ -48,7 +48,11 @@ struct TCfg {
   static constexpr uint32_t kStageBytes = kKOff + kBoxes * kEBytes;
   static constexpr size_t kSmem = (size_t)ST * kStageBytes;
   static constexpr int kMinBlocks = W <= 2 ? 6 : (W <= 4 ? 4 : 2);
-  static constexpr int kMinBlocks2 = W <= 2 ? 5 : (W <= 4 ? 3 : 1);   // two-step form: more registers
+  // two-step form: more registers; 4 CTAs (128 registers, no spills in
+  // F32) where shared memory lets four fit, 3 otherwise (16-bit storage:
+  // its conversions spill at 128)
+  static constexpr int kMinBlocks2 =
+      W <= 2 ? 5 : (W <= 4 ? ((sizeof(T) == 4 && kSmem <= 56 * 1024) ? 4 : 3) : 1);
   static_assert(kSpan % kBoxes == 0 && kBX % 8 == 0 && kBX <= 256, "box tiling of the staged span");
 };
 
@@ -717,12 +721,18 @@ constexpr TShape tentry() {
 
 // Compiled shapes (warps, rows per stage, stages); the first is the default.
 const TShape kTShapes[] = {tentry<4, 4, 2>(), tentry<4, 2, 3>(), tentry<4, 4, 3>(), tentry<2, 8, 2>(),
-                           tentry<4, 8, 2>(), tentry<8, 2, 2>()};
+                           tentry<4, 8, 2>(), tentry<8, 2, 2>(), tentry<4, 2, 2>()};
 constexpr int kNumTShapes = sizeof(kTShapes) / sizeof(kTShapes[0]);
 
 }  // namespace
 
 int tmat_shape_count() { return kNumTShapes; }
+
+int tmat_shape_find(int warps, int rows, int stages) {
+  for (int k = 0; k < kNumTShapes; ++k)
+    if (kTShapes[k].warps == warps && kTShapes[k].rows == rows && kTShapes[k].stages == stages) return k;
+  return -1;
+}
 
 void tmat_shape_dims(int shape, int* warps, int* rows, int* stages) {
   *warps = kTShapes[shape].warps;

@@ -130,7 +130,7 @@ def test_every_launch_shape(gpu, monkeypatch, shape):
 
 
 # Multi-row tensor shapes (warps, rows per stage, stages) of step_tmat.cu.
-TMAT_SHAPES = ["4,4,2", "4,2,3", "4,4,3", "2,8,2", "4,8,2", "8,2,2"]
+TMAT_SHAPES = ["4,4,2", "4,2,3", "4,4,3", "2,8,2", "4,8,2", "8,2,2", "4,2,2"]
 
 
 def _stepped_state(gpu, prob, st, steps):
