@@ -208,7 +208,7 @@ def _stepped_all(gpu, prob, st, steps, chunks):
 
 
 @pytest.mark.parametrize("shape", TMAT_SHAPES)
-@pytest.mark.parametrize("storage", [F.STORE_F32, F.STORE_F16])
+@pytest.mark.parametrize("storage", [F.STORE_F32, F.STORE_F16, F.STORE_BF16])
 def test_two_step_equals_one_step(gpu, monkeypatch, shape, storage):
     """The two-step form (FDTD2D_TB=1: two time steps per pass over the
     interior, the CPML-band kernel stepping the rest once per step between)
