@@ -14,6 +14,12 @@
 // same time step.  The arithmetic is the same, operation for operation, as
 // that kernel's, so either kernel gives a cell the same bits.
 //
+// step_tmat2_kernel is the two-step form: one pass over state n-1 gives
+// state n+1 of the interior (each warp recomputes step n one column beyond
+// its sides, each unit one row beyond its ends), so the fields are read and
+// written once for two time steps; frame_kernel steps the 2-cell frame the
+// next pass reads beyond the interior.
+//
 // Every wait is bounded as in step_tma.cu (1 s without progress: the error
 // word is set, the copies in flight are waited for, the kernel returns).
 #include <algorithm>
