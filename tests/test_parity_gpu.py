@@ -240,6 +240,56 @@ def test_two_step_equals_one_step(gpu, monkeypatch, shape, storage):
         assert np.array_equal(ref[k], got[k]), (shape, k)
 
 
+def test_two_step_fields_written_between_runs(gpu, monkeypatch):
+    """Fields and psi written between run calls reach every buffer the
+    two-step path rotates through: runs of 9, then a write, then 6 and 2
+    steps, give the one-row kernel's bits; a two-step shot's shortest runs
+    (2 steps, then 1) too."""
+    monkeypatch.delenv("FDTD2D_KERNEL", raising=False)
+    monkeypatch.delenv("FDTD2D_TMA", raising=False)
+    nx, ny, P = 2600, 301, 11
+    prob = F.Problem.from_spec(nx=nx, ny=ny, npml=P, n_steps=17, profile=1, x_lo=nx // 3, x_hi=nx - 3,
+                               ne_peak=2e19, nu=3e9, src_i=1300, src_j=150, det_i=1303, det_j=151, n_det=1)
+    st = _random_fields(nx, ny, P, 21)
+    mid = _random_fields(nx, ny, P, 22)
+
+    def stepped():
+        with F.Shot(prob, gpu) as shot:
+            name = shot.kernel_name()
+            load_state([shot], st)
+            shot.run(1, 9)
+            shot.write_field(F.FIELD_EZ, mid[F.FIELD_EZ])
+            shot.write_field(F.FIELD_HY, mid[F.FIELD_HY])
+            shot.write_field(PSI_FIELDS[0], mid[PSI_FIELDS[0]])
+            shot.run(10, 15)
+            shot.run(16, 17)
+            out = {w: shot.read_field(w) for w in FIELDS + PSI_FIELDS}
+            out["det"] = shot.traces()["det_ez"]
+        return name, out
+
+    monkeypatch.setenv("FDTD2D_TMAT", "0")
+    _, ref = stepped()
+    monkeypatch.setenv("FDTD2D_TMAT", "4,2,2")
+    monkeypatch.setenv("FDTD2D_TB", "1")
+    name, got = stepped()
+    assert name.startswith("step_tmat2_kernel<4,2,2>"), name
+    for k in ref:
+        assert np.array_equal(ref[k], got[k]), k
+
+    short = F.Problem.from_spec(nx=nx, ny=ny, npml=P, n_steps=3, profile=1, x_lo=nx // 3, x_hi=nx - 3,
+                                ne_peak=2e19, nu=3e9, src_i=1300, src_j=150, det_i=1303, det_j=151, n_det=1)
+    outs = []
+    for tmat in ("0", "4,2,2"):
+        monkeypatch.setenv("FDTD2D_TMAT", tmat)
+        with F.Shot(short, gpu) as shot:
+            load_state([shot], st)
+            shot.run(1, 2)
+            shot.run(3, 3)
+            outs.append({w: shot.read_field(w) for w in FIELDS})
+    for w in FIELDS:
+        assert np.array_equal(outs[0][w], outs[1][w]), w
+
+
 def test_two_step_against_oracle(gpu, monkeypatch):
     """The two-step form against the FP64 oracle on a CPML-absorbed pulse
     from a steered array (fields, traces, DFT phase)."""
