@@ -564,13 +564,20 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(psi_trial, h.psi, psi_floats * 4, cudaMemcpyDeviceToDevice, c->stream);
     }
-    if (e != cudaSuccess) return fail_cuda(c, e);
+    if (e != cudaSuccess) {
+      if (psi_trial) cudaFreeAsync(psi_trial, c->stream);
+      return fail_cuda(c, e);
+    }
   }
   DevShot t = h;
   t.record = 0;
   t.dft = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return FDTD2D_ERR_CUDA;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    if (psi_trial) cudaFreeAsync(psi_trial, c->stream);
+    return FDTD2D_ERR_CUDA;
+  }
   auto timed = [&](auto&& step) -> float {
     cudaError_t e = step();
     if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
