@@ -96,7 +96,11 @@ float vmax(const Vec& v) {
   return r;
 }
 
+// The second difference, 0 at both ends.  A TOF window that opens after the
+// run's last step leaves no samples: then there is nothing to write (the
+// reference indexes the empty vector there).
 void sec_diff(const Vec& src, Vec& dst) {
+  if (dst.empty()) return;
   dst[0] = dst[dst.size() - 1] = 0;
   for (size_t i = 1; i + 1 < src.size(); i++) dst[i] = src[i - 1] - 2 * src[i] + src[i + 1];
 }

@@ -239,3 +239,20 @@ def test_source_to_detect_files_match_reference():
     s3, s4, s5 = sums
     eh = np.hypot(s3 * s5, s3 * s4)
     assert O.rel_l2(dif[:, 7] / 1000, eh) <= 1e-5
+
+
+def test_tof_window_after_the_run(tmp_path):
+    """A TOF window that opens after the run's last step (BeginAfter past
+    the shot's length, as the default Settings.ini's 6..18 ns window on a
+    run shortened below 6 ns) leaves no saved samples: processing writes its
+    files with the not-found taus instead of indexing an empty line."""
+    p, _, _ = load("tof_line")
+    ini = (GOLDEN / "tof_line" / "Settings.ini").read_text()
+    key = {ln.split("=")[0].strip(): ln.split("=")[1].split(";")[0].strip()
+           for ln in ini.splitlines() if "=" in ln and not ln.startswith(";")}
+    size = int(int(key["SizeI"]) / float(key["ds"]))
+    p.write_tof(np.zeros((0, size), np.float32), tmp_path)
+    for f in ("SD.txt", "CF.txt", "ARC.txt"):
+        rows = np.atleast_2d(np.loadtxt(tmp_path / f))
+        assert rows.shape[0] > 0, f
+        assert np.all(rows[:, 1] == int(key["BeginAfter"]) - 1), f
