@@ -266,11 +266,11 @@ int validate(const fdtd2d_setup* s) {
 }
 
 // Split rows [0, ny-1) x column blocks of `cols` into at most `warps` units.
-std::vector<int4> make_units(int shot, int nx, int ny, int warps, int cols = kCols) {
+std::vector<int4> make_units(int shot, int nx, int ny, int warps, int cols = kCols, int min_rows = 8) {
   const int cb = (nx + cols - 1) / cols;
   const int rows = ny - 1;
   int strips = std::max(1, warps / cb);
-  strips = std::min(strips, std::max(1, rows / 8));
+  strips = std::min(strips, std::max(1, rows / min_rows));
   std::vector<int4> u;
   u.reserve((size_t)cb * strips);
   for (int s = 0; s < strips; ++s) {
@@ -1130,7 +1130,9 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
     tma_shape_name(c->tma_shape, "step_tma_kernel", c->kernel_name, sizeof c->kernel_name);
   } else {
     c->grid_warps = resident_warps(c->medium, device);
-    units = make_units(0, nx, ny, c->grid_warps);
+    // one warp per unit, units of at least 2 rows: a narrow grid (a few
+    // 128-column blocks) still fills the resident warps in one wave
+    units = make_units(0, nx, ny, c->grid_warps, kCols, 2);
     std::snprintf(c->kernel_name, sizeof c->kernel_name, "step_stream_kernel<%d>", c->medium == FDTD2D_MEDIUM_UNIFORM ? 0 : 1);
   }
   c->n_units = (int)units.size();

@@ -33,6 +33,7 @@
 #include <cstring>
 #include <ctime>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/fdtd2d.h"
@@ -58,6 +59,34 @@ struct File {
   }
   explicit operator bool() const { return f != nullptr; }
 };
+
+// One Ez slice as the reference prints it (kernel.cu:2173-2303): a line per
+// column i of "%12f " values over j, and a newline in each of the other
+// slice files per line.  The lines are formatted in parallel into strings,
+// then written in order, so the files hold the bytes a serial loop writes.
+void write_slice(FILE* fez, FILE* fex, FILE* fhx, FILE* fhy, FILE* fhz, const std::vector<float>& ez, int nx,
+                 int ny, int sieve) {
+  std::vector<int> cols;
+  for (int i = 1; i < nx - 1; i += sieve) cols.push_back(i);
+  std::vector<std::string> lines(cols.size());
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int k = 0; k < (int)cols.size(); ++k) {
+    std::string& line = lines[k];
+    char buf[64];
+    for (int j = 1; j < ny - 1; j += sieve) {
+      const int len = std::snprintf(buf, sizeof buf, "%12f ", ez[(size_t)j * nx + cols[k]]);
+      line.append(buf, (size_t)len);
+    }
+  }
+  for (const std::string& line : lines) {
+    std::fwrite(line.data(), 1, line.size(), fez);
+    std::fputc('\n', fex);
+    std::fputc('\n', fez);
+    std::fputc('\n', fhx);
+    std::fputc('\n', fhy);
+    std::fputc('\n', fhz);
+  }
+}
 
 std::string join(const std::string& dir, const char* name) {
   if (dir.empty()) return name;
@@ -276,7 +305,11 @@ extern "C" int fdtd2d_run_settings(const char* ini_path, const char* out_dir, in
   // Step loop with the reference's slice-save cadence (kernel.cu:2173-2303):
   // inside [From, To] a counter runs 1..TimeSieve and a slice is written when
   // it reaches TimeSieve.
-  std::vector<float> ez((size_t)nx * ny);
+  // Two slice buffers: a slice is written on a writer thread while the GPU
+  // steps on towards the next one (at most one write in flight, so the
+  // slices reach the files in order).
+  std::vector<float> ez_buf[2] = {std::vector<float>((size_t)nx * ny), std::vector<float>((size_t)nx * ny)};
+  std::thread writer;
   int save_counter = 0, save_app = 1;
   int32_t done = 0;
   const int sieve = ip.save_grid_sieve > 0 ? ip.save_grid_sieve : 1;
@@ -294,18 +327,14 @@ extern "C" int fdtd2d_run_settings(const char* ini_path, const char* out_dir, in
     rc = advance(done + 1, n);
     done = n;
     if (rc || !save) continue;
+    std::vector<float>& ez = ez_buf[save_counter & 1];
+    if (writer.joinable()) writer.join();   // the other buffer's write is done before this one is read into
     rc = fdtd2d_read_field(ctx, FDTD2D_FIELD_EZ, ez.data());
     if (rc) break;
     save_counter++;
-    for (int i = 1; i < nx - 1; i += sieve) {
-      for (int j = 1; j < ny - 1; j += sieve) std::fprintf(pEz.f, "%12f ", ez[(size_t)j * nx + i]);
-      std::fputc('\n', pEx.f);
-      std::fputc('\n', pEz.f);
-      std::fputc('\n', pHx.f);
-      std::fputc('\n', pHy.f);
-      std::fputc('\n', pHz.f);
-    }
+    writer = std::thread(write_slice, pEz.f, pEx.f, pHx.f, pHy.f, pHz.f, std::cref(ez), nx, ny, sieve);
   }
+  if (writer.joinable()) writer.join();
   if (rc == FDTD2D_OK) rc = fdtd2d_synchronize(ctx);
 
   if (rc == FDTD2D_OK) {

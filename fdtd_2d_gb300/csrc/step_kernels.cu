@@ -345,21 +345,33 @@ cudaError_t build_source_tables(float* src_val, double2* twiddle, const float* e
 // loads); here the column max and the downward scan are block reductions.
 // The scan result is the largest j in [1, ny-3] where |Ez| is not below the
 // edge level, which is where the reference's do-while from j = ny-2 stops.
-__global__ void rc_kernel(const float* __restrict__ ez, int64_t pitch, int ny,
-                          const int* __restrict__ scan_i, const int* __restrict__ max_i, int j_cut,
-                          float level, float* __restrict__ edge, int* __restrict__ spd_row) {
+__global__ void __launch_bounds__(1024) rc_kernel(const float* __restrict__ ez, int64_t pitch, int ny,
+                                                  const int* __restrict__ scan_i, const int* __restrict__ max_i,
+                                                  int j_cut, float level, float* __restrict__ edge,
+                                                  int* __restrict__ spd_row) {
+  constexpr int kPer = 8;   // scan-column rows a thread holds while the column max is formed
   __shared__ float s_max[32];
   __shared__ int s_best[32];
   __shared__ float s_edge;
   const int l = blockIdx.x;
   const int im = max_i[l], is = scan_i[l];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int tid = threadIdx.x, T = blockDim.x;
+  const int lane = tid & 31, w = tid >> 5, nw = T >> 5;
+  // The scan column's first kPer*T rows are loaded beside the max column, so
+  // both columns' loads are in flight together.
+  float sv[kPer];
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    const int j = 1 + tid + k * T;
+    sv[k] = j <= ny - 3 ? fabsf(ez[(int64_t)j * pitch + is]) : 0.f;
+  }
   float m = -INFINITY;
-  for (int j = j_cut + (int)threadIdx.x; j < ny - 2; j += blockDim.x) m = fmaxf(m, ez[(int64_t)j * pitch + im]);
+#pragma unroll 4
+  for (int j = j_cut + tid; j < ny - 2; j += T) m = fmaxf(m, ez[(int64_t)j * pitch + im]);
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if (lane == 0) s_max[w] = m;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     float temp = ez[im];  // Dev_FindMax starts from row 0
     for (int k = 0; k < nw; ++k)
       if (s_max[k] > temp) temp = s_max[k];
@@ -372,12 +384,17 @@ __global__ void rc_kernel(const float* __restrict__ ez, int64_t pitch, int ny,
   __syncthreads();
   const float e = s_edge;
   int best = 0;
-  for (int j = 1 + (int)threadIdx.x; j <= ny - 3; j += blockDim.x)
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    const int j = 1 + tid + k * T;
+    if (j <= ny - 3 && !(sv[k] < e)) best = max(best, j);
+  }
+  for (int j = 1 + tid + kPer * T; j <= ny - 3; j += T)
     if (!(fabsf(ez[(int64_t)j * pitch + is]) < e)) best = max(best, j);
   for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
   if (lane == 0) s_best[w] = best;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     int b = 0;
     for (int k = 0; k < nw; ++k) b = max(b, s_best[k]);
     spd_row[l] = b;
@@ -387,7 +404,7 @@ __global__ void rc_kernel(const float* __restrict__ ez, int64_t pitch, int ny,
 cudaError_t launch_rc(const float* ez, int64_t pitch, int ny, int n_rc, const int* scan_i,
                       const int* max_i, int j_cut, float level, float* edge, int* spd_row,
                       cudaStream_t stream) {
-  rc_kernel<<<n_rc, 256, 0, stream>>>(ez, pitch, ny, scan_i, max_i, j_cut, level, edge, spd_row);
+  rc_kernel<<<n_rc, 1024, 0, stream>>>(ez, pitch, ny, scan_i, max_i, j_cut, level, edge, spd_row);
   return cudaGetLastError();
 }
 
