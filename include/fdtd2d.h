@@ -228,7 +228,11 @@ const char *fdtd2d_kernel_name(const fdtd2d_ctx *ctx);
    A batch advances many uniform-medium shots (CPML <= 120 cells, no wave-front
    tracker or line probe) together: one persistent launch per time step, issued
    in blocks captured as CUDA graphs, each shot at its own step.  Shots can be
-   admitted between fdtd2d_batch_run calls while others are in flight. ---- */
+   admitted between fdtd2d_batch_run calls while others are in flight.  A shot
+   of at least 2^21 cells (FDTD2D_BATCH_SOLO_CELLS overrides; 0 for none) is
+   a solo member instead: a full single shot on its own streams with its own
+   kernel choice (two steps per pass where that wins), stepped from the same
+   run calls; its budget share counts that path's two extra field buffers. ---- */
 typedef struct fdtd2d_batch fdtd2d_batch;
 
 /* hbm_budget_bytes <= 0: 90 % of the device memory free now. */
