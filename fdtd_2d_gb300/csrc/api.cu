@@ -479,6 +479,66 @@ void keep_choice(const ChoiceKey& key, const KernelChoice& ch) {
   g_choice[key] = ch;
 }
 
+// A material-ID medium that the uniform medium represents exactly: every
+// cell inside the reference's launch coverage, no PEC cell (Ez material 1),
+// one (CA, CB) over the materials of the Ez map and one (DA, DB) over those
+// of the Hx and Hy maps (bit for bit: the reference's vacuum and plasma
+// levels all share them).  Then the shot is stepped as the uniform medium
+// with a drive map holding each Ez cell's material drive, the float the
+// material kernel reads, so the staged and tensor kernels give it the
+// material kernel's bits.  kp stays empty when no cell has plasma.
+bool material_as_uniform(const fdtd2d_setup* s, double beta, float* ca, float* cb, float* da, float* db,
+                         std::vector<float>* kp) {
+  const int64_t n = (int64_t)s->nx * s->ny;
+  // reference thread indices each update kernel needs for every cell (its
+  // largest index + 1): Hx, Hx y strips, Hy, Hy x strips, Jz, Ez, Ez x
+  // strips, Ez y strips
+  const int64_t X = s->nx, Y = s->ny, Q = s->npml - 1;
+  const int64_t need[8] = {(Y - 1) * (X - 1), Q * (X - 1), Y * (X - 1), Y * Q,
+                           (Y - 2) * (X - 2), (Y - 2) * (X - 2), (Y - 2) * Q, Q * (X - 2)};
+  for (int k = 0; k < 8; ++k)
+    if (s->cover[k] != 0 && s->cover[k] < need[k]) return false;
+  const int nm = s->n_materials;
+  std::vector<char> used_e(nm, 0), used_h(nm, 0);
+  for (int64_t t = 0; t < n; ++t) {
+    const int32_t a = s->id1[t], b = s->id2[t], e = s->id3[t];
+    if (a < 0 || a >= nm || b < 0 || b >= nm || e < 0 || e >= nm) return false;
+    used_h[a] = used_h[b] = 1;
+    used_e[e] = 1;
+  }
+  if (nm > 1 && used_e[1]) return false;
+  auto same = [](float x, float y) { return std::memcmp(&x, &y, sizeof(float)) == 0; };
+  int fe = -1, fh = -1;
+  for (int m = 0; m < nm; ++m) {
+    if (used_e[m]) {
+      if (fe < 0) fe = m;
+      else if (!same(s->mat_ca[m], s->mat_ca[fe]) || !same(s->mat_cb[m], s->mat_cb[fe])) return false;
+    }
+    if (used_h[m]) {
+      if (fh < 0) fh = m;
+      else if (!same(s->mat_da[m], s->mat_da[fh]) || !same(s->mat_db[m], s->mat_db[fh])) return false;
+    }
+  }
+  if (fe < 0 || fh < 0) return false;
+  *ca = s->mat_ca[fe];
+  *cb = s->mat_cb[fe];
+  *da = s->mat_da[fh];
+  *db = s->mat_db[fh];
+  std::vector<float> drive(nm, 0.f);
+  bool any = false;
+  for (int m = 0; m < nm; ++m) {
+    const double ne = s->mat_ne[m];
+    drive[m] = ne > 0 ? (float)(beta * ne) : 0.f;   // the material table's value
+    any = any || (used_e[m] && drive[m] != 0.f);
+  }
+  kp->clear();
+  if (any) {
+    kp->resize((size_t)n);
+    for (int64_t t = 0; t < n; ++t) (*kp)[(size_t)t] = drive[s->id3[t]];
+  }
+  return true;
+}
+
 // Multi-row tensor path (step_tmat.cu) for the interior of the shot, beside
 // the staged kernel on the CPML bands and rows.  Times every tensor shape that
 // fits the grid (tensor kernel on the interior units + staged kernel on the
@@ -809,6 +869,16 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
   h.ja = (float)((1.0 - nudt) / (1.0 + nudt));
   const double beta = s->jz_coef * s->dt / (1.0 + nudt);
   h.dx = (float)s->dx; h.dy = (float)s->dy;
+  // a material medium the uniform one represents exactly runs as uniform
+  // (FDTD2D_MATERIAL_AS_UNIFORM=0 keeps the material kernel)
+  bool as_uniform = false;
+  float u_ca = 0.f, u_cb = 0.f, u_da = 0.f, u_db = 0.f;
+  std::vector<float> u_kp;
+  if (s->medium == FDTD2D_MEDIUM_MATERIAL_ID && s->storage == FDTD2D_STORE_F32) {
+    const char* v = std::getenv("FDTD2D_MATERIAL_AS_UNIFORM");
+    if (!(v && std::strcmp(v, "0") == 0)) as_uniform = material_as_uniform(s, beta, &u_ca, &u_cb, &u_da, &u_db, &u_kp);
+  }
+  if (as_uniform) c->medium = FDTD2D_MEDIUM_UNIFORM;
 
 #define CK(expr)                     \
   do {                               \
@@ -847,7 +917,17 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
   CK(dalloc(c, &h.psi, (size_t)h.psi_buf * 2 + 1024));
 
   // medium
-  if (s->medium == FDTD2D_MEDIUM_UNIFORM) {
+  if (as_uniform) {
+    h.ca = u_ca; h.cb = u_cb; h.da = u_da; h.db = u_db;
+    if (!u_kp.empty()) {
+      float* kp_buf = nullptr;
+      CK(dalloc(c, &kp_buf, cells));
+      CK(cudaMemcpy2DAsync(kp_buf + kMargin, pitch * sizeof(float), u_kp.data(), nx * sizeof(float),
+                           nx * sizeof(float), ny, cudaMemcpyHostToDevice, c->stream));
+      CK(cudaStreamSynchronize(c->stream));   // u_kp is released when create returns
+      h.kp = kp_buf + kMargin;
+    }
+  } else if (s->medium == FDTD2D_MEDIUM_UNIFORM) {
     h.ca = s->ca; h.cb = s->cb; h.da = s->da; h.db = s->db;
     if (h.store != FDTD2D_STORE_F32) set_storage_scales(s, beta, &h);
     if (s->ne) {
@@ -1023,7 +1103,7 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
 
   for (int k = 0; k < 8; ++k) {
     const int64_t v = s->cover[k];
-    h.cov[k] = (s->medium != FDTD2D_MEDIUM_MATERIAL_ID || v == 0) ? INT64_MAX : (v < 0 ? 0 : v);
+    h.cov[k] = (s->medium != FDTD2D_MEDIUM_MATERIAL_ID || as_uniform || v == 0) ? INT64_MAX : (v < 0 ? 0 : v);
   }
 
   // wave-front tracker and line probe

@@ -13,6 +13,7 @@ import numpy as np
 import pytest
 
 import fdtd_2d_gb300 as F
+from helpers import FIELDS, PSI_FIELDS
 
 pytestmark = pytest.mark.gpu
 
@@ -138,3 +139,37 @@ def test_source_to_detect_files(run):
         mag = (np.abs(main[k]) + np.abs(per[k])).sum(1)
         assert np.linalg.norm(m[:, c] - r[:, c]) <= 1e-5 * np.linalg.norm(mag), c
     assert np.linalg.norm(m[:, 7] - r[:, 7]) <= 1e-5 * np.linalg.norm(r[:, 7])
+
+
+def test_material_medium_as_uniform(gpu, monkeypatch, tmp_path):
+    """A Settings.ini medium whose materials share CA/CB/DA/DB, with no PEC
+    cell and the reference's launch coverage reaching every cell (the golden
+    sphere-and-fluctuation case enlarged to 500 x 1200 cells) runs as the
+    uniform medium on the staged kernels, with the material kernel's bits:
+    fields, psi, detector traces and the wave-front tracker rows."""
+    ini = (GOLDEN / "sphere_fluc_chirp" / "Settings.ini").read_text()
+    for key, val in (("Imax", "250"), ("Jmax", "600"), ("Use_Exp_time", "0"), ("Max_time", "300")):
+        ini = re.sub(rf"(?m)^{key}\s*=.*$", f"{key} = {val}", ini)
+    path = tmp_path / "Settings.ini"
+    path.write_text(ini)
+    prob = F.Problem.from_ini(path)
+    s = prob.setup
+    assert (s.nx, s.ny) == (500, 1200) and s.n_rc > 0
+
+    def stepped():
+        with F.Shot(prob, gpu) as shot:
+            name = shot.kernel_name()
+            shot.run(1, prob.n_steps)
+            out = {w: shot.read_field(w) for w in FIELDS + PSI_FIELDS}
+            out["det"] = shot.traces()["det_ez"]
+            out["rc"] = shot.rc()
+        return name, out
+
+    monkeypatch.setenv("FDTD2D_MATERIAL_AS_UNIFORM", "0")
+    name0, ref = stepped()
+    assert name0 == "step_stream_kernel<1>", name0
+    monkeypatch.delenv("FDTD2D_MATERIAL_AS_UNIFORM")
+    name1, got = stepped()
+    assert name1.startswith("step_tma"), name1
+    for k in ref:
+        assert np.array_equal(ref[k], got[k]), k
