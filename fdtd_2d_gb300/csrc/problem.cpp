@@ -126,26 +126,47 @@ void gaussian_random_field(std::vector<float>& g, int nx, int ny, double corr, u
   const double norm = 1.0 / e2;  // two passes: variance scales by e2 each
   const int wx = nx + 2 * R, wy = ny + 2 * R;
   std::vector<float> w((size_t)wx * wy);
-  Rng rng(seed);
-  for (size_t t = 0; t < w.size(); ++t) w[t] = (float)rng.normalish();
-  std::vector<float> tmp((size_t)wx * ny);
-  // pass 1: along y
+  // The generator is a counter (each output mixes seed + k * golden), and a
+  // value takes four outputs: value t starts from seed + 4t * golden, so the
+  // values are formed in parallel and equal the sequential stream's.
 #pragma omp parallel for schedule(static)
-  for (int j = 0; j < ny; ++j) {
-    for (int i = 0; i < wx; ++i) {
-      double acc = 0;
-      for (int d = 0; d <= 2 * R; ++d) acc += k[d] * w[(size_t)(j + d) * wx + i];
-      tmp[(size_t)j * wx + i] = (float)acc;
+  for (int64_t t = 0; t < (int64_t)w.size(); ++t) {
+    Rng rng(seed + (uint64_t)t * 4u * 0x9E3779B97F4A7C15ull);
+    w[(size_t)t] = (float)rng.normalish();
+  }
+  std::vector<float> tmp((size_t)wx * ny);
+  // Each output sums k[d] * input over d = 0 .. 2R in that order; the loops
+  // run d outside and the columns inside (contiguous, vectorisable), one
+  // accumulator per column, which keeps every output's order of additions.
+  // pass 1: along y
+#pragma omp parallel
+  {
+    std::vector<double> acc((size_t)wx);
+#pragma omp for schedule(static)
+    for (int j = 0; j < ny; ++j) {
+      std::fill(acc.begin(), acc.end(), 0.0);
+      for (int d = 0; d <= 2 * R; ++d) {
+        const double kd = k[(size_t)d];
+        const float* src = &w[(size_t)(j + d) * wx];
+        for (int i = 0; i < wx; ++i) acc[(size_t)i] += kd * src[i];
+      }
+      for (int i = 0; i < wx; ++i) tmp[(size_t)j * wx + i] = (float)acc[(size_t)i];
     }
   }
   g.assign((size_t)nx * ny, 0.f);
-#pragma omp parallel for schedule(static)
-  for (int j = 0; j < ny; ++j) {
-    for (int i = 0; i < nx; ++i) {
-      double acc = 0;
-      const float* row = &tmp[(size_t)j * wx + i];
-      for (int d = 0; d <= 2 * R; ++d) acc += k[d] * row[d];
-      g[(size_t)j * nx + i] = (float)(acc * norm);
+  // pass 2: along x
+#pragma omp parallel
+  {
+    std::vector<double> acc((size_t)nx);
+#pragma omp for schedule(static)
+    for (int j = 0; j < ny; ++j) {
+      std::fill(acc.begin(), acc.end(), 0.0);
+      const float* row = &tmp[(size_t)j * wx];
+      for (int d = 0; d <= 2 * R; ++d) {
+        const double kd = k[(size_t)d];
+        for (int i = 0; i < nx; ++i) acc[(size_t)i] += kd * row[i + d];
+      }
+      for (int i = 0; i < nx; ++i) g[(size_t)j * nx + i] = (float)(acc[(size_t)i] * norm);
     }
   }
 }
@@ -267,16 +288,22 @@ int fdtd2d_problem_from_spec(const fdtd2d_spec* sp, fdtd2d_problem** out) {
     p.ne.assign((size_t)nx * ny, 0.f);
     std::vector<float> g;
     if (sp->profile == 3 && sp->grf_rms != 0) gaussian_random_field(g, nx, ny, sp->grf_corr, sp->seed);
+    // the profile depends on the column only
+    std::vector<double> col((size_t)nx, 0.0);
+    for (int i = 0; i < nx; ++i) {
+      if (sp->profile == 1) {
+        if (i >= sp->x_lo && i <= sp->x_hi && sp->x_hi > sp->x_lo)
+          col[(size_t)i] = sp->ne_peak * (i - sp->x_lo) / (sp->x_hi - sp->x_lo);
+      } else {
+        col[(size_t)i] = 0.5 * sp->ne_peak * (1.0 + std::tanh((i - sp->x_center) / sp->width));
+      }
+    }
+    const bool grf = sp->profile == 3 && !g.empty();
+#pragma omp parallel for schedule(static)
     for (int j = 0; j < ny; ++j) {
       for (int i = 0; i < nx; ++i) {
-        double n = 0;
-        if (sp->profile == 1) {
-          if (i >= sp->x_lo && i <= sp->x_hi && sp->x_hi > sp->x_lo)
-            n = sp->ne_peak * (i - sp->x_lo) / (sp->x_hi - sp->x_lo);
-        } else {
-          n = 0.5 * sp->ne_peak * (1.0 + std::tanh((i - sp->x_center) / sp->width));
-          if (sp->profile == 3 && !g.empty()) n *= 1.0 + sp->grf_rms * g[(size_t)j * nx + i];
-        }
+        double n = col[(size_t)i];
+        if (grf) n *= 1.0 + sp->grf_rms * g[(size_t)j * nx + i];
         p.ne[(size_t)j * nx + i] = (float)std::max(0.0, n);
       }
     }

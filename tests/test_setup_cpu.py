@@ -233,3 +233,25 @@ def test_oracle_overdense_plasma_reflects():
     hi, direct = echo(2 * 4 * nc)       # tanh plateau 4 nc
     lo, _ = echo(2 * 0.05 * nc)         # 5 % of nc
     assert hi > 0.2 * direct and hi > 5 * lo
+
+
+def test_plasma_map_pinned():
+    """The parameterised shots' plasma maps (tanh x Gaussian random field,
+    linear slab) are pinned by checksum: their parallel construction must
+    give the sequential construction's floats.  The checksums were taken with
+    x86-64 glibc's exp and tanh; another libm may round them differently."""
+    import hashlib
+    import platform
+
+    if platform.machine() not in ("x86_64", "AMD64"):
+        pytest.skip("checksums taken with x86-64 glibc")
+
+    want = {(700, 500, 3): "fb5050f814227453ca39aee54c4e3d39",
+            (640, 480, 1): "f256d0d42a3efac6e79e3ee0cb72bd85"}
+    for (nx, ny, prof), digest in want.items():
+        kw = dict(nx=nx, ny=ny)
+        if prof == 1:
+            kw.update(profile=1, x_lo=100, x_hi=600, grf_rms=0.0)
+        p = F.Problem.from_spec(F.production_spec(n_steps=10, **kw))
+        ne = p.array("ne", p.nx * p.ny, np.float32)
+        assert hashlib.sha256(ne.tobytes()).hexdigest()[:32] == digest, (nx, ny, prof)
