@@ -31,6 +31,17 @@ __device__ __forceinline__ float upd_e(float ca, float e, float cb, float dhy, f
   return __fmaf_rn(cb, curl, __fmul_rn(ca, e));
 }
 
+// upd_e on values in stored units: Ez/sE, H/sH, Jz/sJ, with cb_s = cb*sH/sE
+// and rj = sJ/sH.  The scales are powers of two, so in the normal range each
+// rounding here is the FP32 rounding above times an exact power of two; rj*Jz
+// is exact, so the fma gives the subtraction's bits.  The result is upd_e's
+// value divided by sE, bit for bit (with unit scales the two are identical).
+__device__ __forceinline__ float upd_es(float ca, float e, float cb_s, float dhy, float dex, float dhx, float dey,
+                                        float jz, float rj) {
+  const float curl = __fmaf_rn(-rj, jz, __fmaf_rn(dhy, dex, __fmul_rn(dhx, dey)));
+  return __fmaf_rn(cb_s, curl, __fmul_rn(ca, e));
+}
+
 // Jz = ja*Jz + kp*Ez where the cell carries plasma (kp != 0), else unchanged.
 // At nu = 0, ja = 1 and kp = (e^2/m_e)*ne*dt: the reference's
 // Jz + D_CJ*Ez*NE*dt (FDTD_2D_Full/kernel.cu:156-157).

@@ -300,24 +300,43 @@ __device__ void tband(const DevShot& S, const TensorMaps& M, TRing& R, int c0, i
 
 // Sources of step n, then its detectors when `rec`, on the cells i..i+3 of
 // one row (the point loop of tband), plus the sources at column xc, which
-// are applied to ezx: the edge column a two-step unit recomputes.
+// are applied to ezx: the edge column a two-step unit recomputes.  The
+// fields are in stored units (Ez/sE, H/sH): a source sample enters as
+// sample/sE, a detector records the field times its scale, both exact
+// (kScaled false: FP32 storage, unit scales).
+template <bool kScaled>
+__device__ __forceinline__ float upd_e2(float ca, float e, float cb, float dhy, float dex, float dhx, float dey,
+                                        float jz, float rj) {
+  if constexpr (kScaled) return upd_es(ca, e, cb, dhy, dex, dhx, dey, jz, rj);
+  else return upd_e(ca, e, cb, dhy, dex, dhx, dey, jz);
+}
+
+template <bool kScaled>
 __device__ __forceinline__ void pts2(const DevShot& S, int p0, int p1, int i, int n, bool rec, float (&ez)[4],
                                      const float (&hx)[4], const float (&hy)[4], int xc, float& ezx) {
+  // value of a source sample in stored units, of a stored field in FP32 units
+  auto src = [&](int z, int m) {
+    const float v = __ldg(S.src_val + (int64_t)m * S.n_src + z);
+    return kScaled ? __fmul_rn(v, S.isc[0]) : v;
+  };
+  auto unit = [&](float v, int f) { return kScaled ? __fmul_rn(v, S.sc[f]) : v; };
   for (int p = p0; p < p1; ++p) {
     const int4 pt = __ldg(S.pts + p);
-    if (pt.y == kPointSource && pt.x == xc) ezx = __fsub_rn(ezx, __ldg(S.src_val + (int64_t)n * S.n_src + pt.z));
+    if (pt.y == kPointSource && pt.x == xc)
+      ezx = __fsub_rn(ezx, src(pt.z, n));
     const int kk = pt.x - i;
     if (kk < 0 || kk > 3) continue;
     float e = 0.f;
 #pragma unroll
     for (int q = 0; q < 4; ++q) if (q == kk) e = ez[q];
     if (pt.y == kPointSource) {
-      e = __fsub_rn(e, __ldg(S.src_val + (int64_t)n * S.n_src + pt.z));
+      e = __fsub_rn(e, src(pt.z, n));
 #pragma unroll
       for (int q = 0; q < 4; ++q) if (q == kk) ez[q] = e;
     } else if (!rec) {
       continue;
     } else if (pt.y == kPointDetEz) {
+      e = unit(e, 0);
       if (S.record) S.trace[(int64_t)(n - 1) * S.n_det + pt.z] = e;
       if (S.dft) {
         const double2 tw = __ldg(S.twiddle + n);
@@ -332,7 +351,7 @@ __device__ __forceinline__ void pts2(const DevShot& S, int p0, int p1, int i, in
       for (int q = 0; q < 4; ++q) if (q == kk) { hxv = hx[q]; hyv = hy[q]; }
       if (S.record) {
         float* dst = S.ctrace + ((int64_t)(n - 1) * S.n_comp + pt.z) * 3;
-        dst[0] = e; dst[1] = hxv; dst[2] = hyv;
+        dst[0] = unit(e, 0); dst[1] = unit(hxv, 1); dst[2] = unit(hyv, 2);
       }
     }
   }
@@ -367,9 +386,18 @@ __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const in
   T* __restrict__ hxw = field_ptr_t<T>(S, kHx, 2);
   T* __restrict__ hyw = field_ptr_t<T>(S, kHy, 2);
   T* __restrict__ jzw = field_ptr_t<T>(S, kJz, 2);
-  const float sE = S.sc[0], sHx = S.sc[1], sHy = S.sc[2], sJ = S.sc[3], sK = S.sc[4];
-  const float iE = S.isc[0], iHx = S.isc[1], iHy = S.isc[2], iJ = S.isc[3];
-  const float da = S.da, db = S.db, ca = S.ca, cb = S.cb, ja = S.ja;
+  // Arithmetic in stored units (Ez/sE, Hx/sH, Hy/sH, Jz/sJ): loads and
+  // stores convert without a scale, and the power-of-two scales are folded
+  // into db, cb, the drive map and the Jz term of the curl (upd_es), so
+  // every stored value keeps the bits of the FP32-unit update.  Hx and Hy
+  // share one scale (checked at launch).  FP32 storage has unit scales.
+  constexpr bool kScaled = sizeof(T) == 2;
+  const float sE = kScaled ? S.sc[0] : 1.f, sH = kScaled ? S.sc[1] : 1.f, iH = kScaled ? S.isc[1] : 1.f;
+  const float da = S.da, ca = S.ca, ja = S.ja;
+  const float db = kScaled ? __fmul_rn(__fmul_rn(S.db, sE), iH) : S.db;           // db sE/sH
+  const float cb = kScaled ? __fmul_rn(__fmul_rn(S.cb, sH), S.isc[0]) : S.cb;      // cb sH/sE
+  const float rj = kScaled ? __fmul_rn(S.sc[3], iH) : 1.f;                         // sJ/sH
+  const float rk = kScaled ? __fmul_rn(__fmul_rn(S.sc[4], sE), S.isc[3]) : 1.f;    // sK sE/sJ
 
   const int i0 = c0 + warp * kCols;            // this warp's first column
   const int i = i0 + 4 * lane;                 // this lane's first column
@@ -401,20 +429,20 @@ __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const in
   // Row jb state: Ez_{n-1}(jb) here and at the edge column and its
   // neighbours, Hx_n(jb - 1) recomputed (row jb - 1 >= npml - 1: no CPML).
   float ezc[4], hxp[4];
-  St::ldg4(ezc, ezo + (int64_t)jb * pitch + i, sE);
-  float e_m = St::ldg1(ezo + (int64_t)jb * pitch + xc - 1, sE);
-  float e_0 = St::ldg1(ezo + (int64_t)jb * pitch + xc, sE);
-  float e_p = St::ldg1(ezo + (int64_t)jb * pitch + xc + 1, sE);
+  St::ldg4(ezc, ezo + (int64_t)jb * pitch + i);
+  float e_m = St::ldg1(ezo + (int64_t)jb * pitch + xc - 1);
+  float e_0 = St::ldg1(ezo + (int64_t)jb * pitch + xc);
+  float e_p = St::ldg1(ezo + (int64_t)jb * pitch + xc + 1);
   float hxe_p;                                 // Hx_n(xc, j - 1)
   {
     float ezp[4], hxo[4];
     const int64_t o = (int64_t)(jb - 1) * pitch;
-    St::ldg4(ezp, ezo + o + i, sE);
-    St::ldg4(hxo, hxo_p + o + i, sHx);
+    St::ldg4(ezp, ezo + o + i);
+    St::ldg4(hxo, hxo_p + o + i);
     const float dhy0 = __ldg(S.den_hy + jb - 1);
 #pragma unroll
     for (int q = 0; q < 4; ++q) hxp[q] = upd_h(da, hxo[q], db, ezp[q], ezc[q], dhy0);
-    hxe_p = upd_h(da, St::ldg1(hxo_p + o + xc, sHx), db, St::ldg1(ezo + o + xc, sE), e_0, dhy0);
+    hxe_p = upd_h(da, St::ldg1(hxo_p + o + xc), db, St::ldg1(ezo + o + xc), e_0, dhy0);
   }
 
   // state n of the previous row as stored, for step n+1
@@ -446,23 +474,23 @@ __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const in
 
       // ---- staged state n-1: row j (Ez row j+1)
       float ezn[4], hxo[4], hyo[4], jzo[4], kp[4];
-      St::lds4(ezn, at<C>(st, 3, r, xr), sE);
-      St::lds4(hxo, at<C>(st, 0, r, xr), sHx);
-      St::lds4(hyo, at<C>(st, 1, r, xr), sHy);
-      St::lds4(jzo, at<C>(st, 2, r, xr), sJ);
+      St::lds4(ezn, at<C>(st, 3, r, xr));
+      St::lds4(hxo, at<C>(st, 0, r, xr));
+      St::lds4(hyo, at<C>(st, 1, r, xr));
+      St::lds4(jzo, at<C>(st, 2, r, xr));
       if (has_kp) {
-        St::lds4(kp, at<C>(st, 4, r, xr), sK);
+        St::lds4(kp, at<C>(st, 4, r, xr), rk);
       } else {
         zero4(kp);
       }
-      const float f_m = St::ld1(at<C>(st, 3, r, sx - 1), sE);
-      const float f_0 = St::ld1(at<C>(st, 3, r, sx), sE);
-      const float f_p = St::ld1(at<C>(st, 3, r, sx + 1), sE);
-      const float hyoA = St::ld1(at<C>(st, 1, r, sx - 1), sHy);
-      const float hyoB = St::ld1(at<C>(st, 1, r, sx), sHy);
-      const float hxoE = St::ld1(at<C>(st, 0, r, sx), sHx);
-      const float jzoE = St::ld1(at<C>(st, 2, r, sx), sJ);
-      const float kpE = has_kp ? St::ld1(at<C>(st, 4, r, sx), sK) : 0.f;
+      const float f_m = St::ld1(at<C>(st, 3, r, sx - 1));
+      const float f_0 = St::ld1(at<C>(st, 3, r, sx));
+      const float f_p = St::ld1(at<C>(st, 3, r, sx + 1));
+      const float hyoA = St::ld1(at<C>(st, 1, r, sx - 1));
+      const float hyoB = St::ld1(at<C>(st, 1, r, sx));
+      const float hxoE = St::ld1(at<C>(st, 0, r, sx));
+      const float jzoE = St::ld1(at<C>(st, 2, r, sx));
+      const float kpE = !has_kp ? 0.f : kScaled ? __fmul_rn(St::ld1(at<C>(st, 4, r, sx)), rk) : St::ld1(at<C>(st, 4, r, sx));
 
       // ---- step n, row j
       float hxn[4], hyn[4], jzn[4], ezs_n[4];
@@ -480,41 +508,41 @@ __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const in
       if (lane == 0) hyl = hyB;
       const float hxE = upd_h(da, hxoE, db, e_0, f_0, dhy);
       const float jzE = upd_j(ja, jzoE, kpE, e_0);
-      float ezE = upd_e(ca, e_0, cb, __fsub_rn(hyB, hyA), dexE, __fsub_rn(hxe_p, hxE), dey, jzE);
+      float ezE = upd_e2<kScaled>(ca, e_0, cb, __fsub_rn(hyB, hyA), dexE, __fsub_rn(hxe_p, hxE), dey, jzE, rj);
       const float hyl4[4] = {hyl, hyn[0], hyn[1], hyn[2]};
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         jzn[q] = upd_j(ja, jzo[q], kp[q], ezc[q]);
-        ezs_n[q] = upd_e(ca, ezc[q], cb, __fsub_rn(hyn[q], hyl4[q]), dex[q], __fsub_rn(hxp[q], hxn[q]), dey, jzn[q]);
+        ezs_n[q] = upd_e2<kScaled>(ca, ezc[q], cb, __fsub_rn(hyn[q], hyl4[q]), dex[q], __fsub_rn(hxp[q], hxn[q]), dey, jzn[q], rj);
       }
       const bool own = j >= j0 && j < j1;
-      pts2(S, p0, p1, i, n, own, ezs_n, hxn, hyn, xc, ezE);
+      pts2<kScaled>(S, p0, p1, i, n, own, ezs_n, hxn, hyn, xc, ezE);
       if (own) {
         const int64_t o = (int64_t)j * pitch + i;
         if (((ring & kRingTop) && j == j0) || ((ring & kRingBottom) && j == j1 - 1)) {
-          St::stcs4(ezm + o, ezs_n, iE);
-          St::stcs4(hxm + o, hxn, iHx);
-          St::stcs4(hym + o, hyn, iHy);
-          St::stcs4(jzm + o, jzn, iJ);
+          St::stcs4(ezm + o, ezs_n);
+          St::stcs4(hxm + o, hxn);
+          St::stcs4(hym + o, hyn);
+          St::stcs4(jzm + o, jzn);
         } else if ((ring & kRingLeft) && warp == 0 && lane == 0) {
-          St::st1(ezm + o, ezs_n[0], iE);
-          St::st1(hxm + o, hxn[0], iHx);
-          St::st1(hym + o, hyn[0], iHy);
-          St::st1(jzm + o, jzn[0], iJ);
+          St::st1(ezm + o, ezs_n[0]);
+          St::st1(hxm + o, hxn[0]);
+          St::st1(hym + o, hyn[0]);
+          St::st1(jzm + o, jzn[0]);
         } else if ((ring & kRingRight) && warp == C::kWarps - 1 && lane == 31) {
-          St::st1(ezm + o + 3, ezs_n[3], iE);
-          St::st1(hxm + o + 3, hxn[3], iHx);
-          St::st1(hym + o + 3, hyn[3], iHy);
-          St::st1(jzm + o + 3, jzn[3], iJ);
+          St::st1(ezm + o + 3, ezs_n[3]);
+          St::st1(hxm + o + 3, hxn[3]);
+          St::st1(hym + o + 3, hyn[3]);
+          St::st1(jzm + o + 3, jzn[3]);
         }
       }
 
       // ---- step n+1, row j-1 (row jb: its Hx only)
       float ezs[4], hxs[4], hys[4], jzs[4];       // state n of row j as stored
-      St::rt4(ezs, ezs_n, iE, sE);
-      St::rt4(hxs, hxn, iHx, sHx);
-      St::rt4(hys, hyn, iHy, sHy);
-      St::rt4(jzs, jzn, iJ, sJ);
+      St::rt4(ezs, ezs_n);
+      St::rt4(hxs, hxn);
+      St::rt4(hys, hyn);
+      St::rt4(jzs, jzn);
       if (j > jb) {
         float hx2[4];
 #pragma unroll
@@ -533,16 +561,16 @@ __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const in
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
             jz2[q] = upd_j(ja, jz1[q], kp1[q], ez1[q]);
-            ez2[q] = upd_e(ca, ez1[q], cb, __fsub_rn(hy2[q], hl4[q]), dex[q], __fsub_rn(hx2p[q], hx2[q]), dey1,
-                           jz2[q]);
+            ez2[q] = upd_e2<kScaled>(ca, ez1[q], cb, __fsub_rn(hy2[q], hl4[q]), dex[q], __fsub_rn(hx2p[q], hx2[q]), dey1,
+                            jz2[q], rj);
           }
           float unused = 0.f;
-          pts2(S, q0, q1, i, n + 1, true, ez2, hx2, hy2, -1, unused);
+          pts2<kScaled>(S, q0, q1, i, n + 1, true, ez2, hx2, hy2, -1, unused);
           const int64_t o = (int64_t)(j - 1) * pitch + i;
-          St::stcs4(hxw + o, hx2, iHx);
-          St::stcs4(hyw + o, hy2, iHy);
-          St::stcs4(ezw + o, ez2, iE);
-          St::stcs4(jzw + o, jz2, iJ);
+          St::stcs4(hxw + o, hx2);
+          St::stcs4(hyw + o, hy2);
+          St::stcs4(ezw + o, ez2);
+          St::stcs4(jzw + o, jz2);
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) hx2p[q] = hx2[q];
@@ -558,8 +586,8 @@ __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const in
         hxp[q] = hxn[q];
         ezc[q] = ezn[q];
       }
-      eze1 = St::rt1(ezE, iE, sE);
-      hye1 = St::rt1(hyB, iHy, sHy);
+      eze1 = St::rt1(ezE);
+      hye1 = St::rt1(hyB);
       hxe_p = hxE;
       e_m = f_m;
       e_0 = f_0;
@@ -767,6 +795,7 @@ cudaError_t launch_step_tmat2(int shape, const DevShot& shot, const TensorMaps& 
   const TShape& e = kTShapes[shape];
   const int ctas = max_ctas < n_units ? max_ctas : n_units;
   if (ctas <= 0) return cudaSuccess;
+  if (shot.sc[1] != shot.sc[2]) return cudaErrorInvalidValue;   // one H scale (stored-unit curl)
   const int st = shot.store;
   e.fn2[st]<<<ctas, e.warps * 32, e.smem[st], stream>>>(shot, maps, units, n_units, n_global, ctr, err);
   return cudaGetLastError();

@@ -40,6 +40,15 @@ struct Sto<float> {
     o[0] = d[0]; o[1] = d[1]; o[2] = d[2]; o[3] = d[3];
   }
   __device__ static __forceinline__ float rt1(float v, float, float) { return v; }
+  // The same in stored units (no scale).
+  __device__ static __forceinline__ void lds4(float (&d)[4], const float* p) { lds4(d, p, 1.f); }
+  __device__ static __forceinline__ void ldg4(float (&d)[4], const float* p) { ldg4(d, p, 1.f); }
+  __device__ static __forceinline__ float ld1(const float* p) { return *p; }
+  __device__ static __forceinline__ float ldg1(const float* p) { return __ldg(p); }
+  __device__ static __forceinline__ void stcs4(float* p, const float (&d)[4]) { stcs4(p, d, 1.f); }
+  __device__ static __forceinline__ void st1(float* p, float v) { *p = v; }
+  __device__ static __forceinline__ void rt4(float (&o)[4], const float (&d)[4]) { rt4(o, d, 1.f, 1.f); }
+  __device__ static __forceinline__ float rt1(float v) { return v; }
 };
 
 template <class T, class T2>
@@ -118,6 +127,43 @@ struct Sto16Ops {
   __device__ static __forceinline__ float rt1(float v, float isc, float sc) {
     return B::to_f2(B::from_f2(v * isc, 0.f) & 0xffffu).x * sc;
   }
+  // The same in stored units: the value the element holds, no scale.
+  __device__ static __forceinline__ void cvt(float (&d)[4], uint2 v) {
+    const float2 a = B::to_f2(v.x), b = B::to_f2(v.y);
+    d[0] = a.x; d[1] = a.y; d[2] = b.x; d[3] = b.y;
+  }
+  __device__ static __forceinline__ void lds4(float (&d)[4], const T* p) {
+    cvt(d, *reinterpret_cast<const uint2*>(p));
+  }
+  __device__ static __forceinline__ void ldg4(float (&d)[4], const T* p) {
+    cvt(d, __ldg(reinterpret_cast<const uint2*>(p)));
+  }
+  __device__ static __forceinline__ float ld1(const T* p) {
+    uint16_t u;
+    memcpy(&u, p, 2);
+    return B::to_f2((uint32_t)u).x;
+  }
+  __device__ static __forceinline__ float ldg1(const T* p) {
+    const uint16_t u = __ldg(reinterpret_cast<const unsigned short*>(p));
+    return B::to_f2((uint32_t)u).x;
+  }
+  __device__ static __forceinline__ void stcs4(T* p, const float (&d)[4]) {
+    uint2 v;
+    v.x = B::from_f2(d[0], d[1]);
+    v.y = B::from_f2(d[2], d[3]);
+    __stcs(reinterpret_cast<uint2*>(p), v);
+  }
+  __device__ static __forceinline__ void st1(T* p, float v) {
+    const uint16_t u = (uint16_t)(B::from_f2(v, 0.f) & 0xffffu);
+    memcpy(p, &u, 2);
+  }
+  __device__ static __forceinline__ void rt4(float (&o)[4], const float (&d)[4]) {
+    uint2 v;
+    v.x = B::from_f2(d[0], d[1]);
+    v.y = B::from_f2(d[2], d[3]);
+    cvt(o, v);
+  }
+  __device__ static __forceinline__ float rt1(float v) { return B::to_f2(B::from_f2(v, 0.f) & 0xffffu).x; }
 };
 
 template <>
