@@ -693,24 +693,29 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
       // first multiple of the one-row band at or past the CPML (two-step
       // form: two cells further in on every side, so that the frame kernel's
       // cells and their neighbours have no CPML), then whole tensor bands
+      // (two-step form: whole one-row bands; the first tensor unit of a row
+      // range then starts `lead` columns left of ci0, and its warps there
+      // idle)
       const int ri0 = lv == 1 ? P : P + 2, ri1 = ny - ri0;
       for (int q = 0; q < tma_shape_count(); ++q) {
         if (q_forced >= 0 && q != q_forced) continue;
         if (q_forced < 0 && !full && q != quick_q[0] && q != quick_q[1] && q != quick_q[2]) continue;
         const int b1 = tma_band_cols(q);
+        const int gran = lv == 1 ? bt : b1;
         const int ci0 = (ri0 + b1 - 1) / b1 * b1;
-        const int ci1 = ci0 + std::max(0, (nx - ri0 - ci0) / bt) * bt;
+        const int ci1 = ci0 + std::max(0, (nx - ri0 - ci0) / gran) * gran;
         if (ci1 - ci0 < bt) continue;
         const int ectas = tma_resident_ctas(q, P, h.store, device);
         std::vector<int4> tu, eu;
-        const int nbt = (ci1 - ci0) / bt;
+        const int nbt = (ci1 - ci0 + bt - 1) / bt;
+        const int lead = nbt * bt - (ci1 - ci0);   // a multiple of kCols below bt
         // (two-step form: about three units per CTA, taken in turn)
-        add_units(tu, ci0, ci1, bt, ri0, ri1,
+        add_units(tu, ci0 - lead, ci1, bt, ri0, ri1,
                   std::min((lv == 1 ? 1 : 3) * std::max(1, tctas / nbt), (ri1 - ri0) / (2 * R)));
         if (lv == 2)
           for (int4& u : tu)
-            u.x = (u.z == ri0 ? kRingTop : 0) | (u.w == ri1 ? kRingBottom : 0) | (u.y == ci0 ? kRingLeft : 0) |
-                  (u.y + bt == ci1 ? kRingRight : 0);
+            u.x = (u.z == ri0 ? kRingTop : 0) | (u.w == ri1 ? kRingBottom : 0) |
+                  (u.y == ci0 - lead ? kRingLeft | (lead / kCols) << 4 : 0) | (u.y + bt == ci1 ? kRingRight : 0);
         eu = edge_units(nx, ny, P, ci0, ci1, ri0, ri1, b1, ectas);
         int4 *dt = nullptr, *de = nullptr;
         cudaError_t e = cudaMallocAsync(&dt, tu.size() * sizeof(int4), c->stream);

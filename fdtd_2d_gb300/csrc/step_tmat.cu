@@ -125,7 +125,8 @@ __device__ __forceinline__ const typename C::Elem* at(const unsigned char* st, i
 }
 
 template <class C>
-__device__ void tband(const DevShot& S, const TensorMaps& M, TRing& R, int c0, int j0, int j1, int n, int* err) {
+__device__ void tband(const DevShot& S, const TensorMaps& M, TRing& R, int c0, int j0, int j1, int idle, int n,
+                      int* err) {
   using T = typename C::Elem;
   using St = Sto<T>;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -140,11 +141,16 @@ __device__ void tband(const DevShot& S, const TensorMaps& M, TRing& R, int c0, i
   T* __restrict__ jzw = field_ptr_t<T>(S, kJz, par ^ 1);
   const float sE = S.sc[0], sHx = S.sc[1], sHy = S.sc[2], sJ = S.sc[3], sK = S.sc[4];
 
-  const int i0 = c0 + warp * kCols;            // this warp's first column
+  // The first `idle` warps lie left of the region (a two-step unit list
+  // stepped once): they only follow the stages, and their few preamble
+  // loads address the first working warp's columns.
+  const bool act = warp >= idle;
+  const int wl = act ? warp : idle;
+  const int i0 = c0 + wl * kCols;              // this warp's first column
   const int i = i0 + 4 * lane;                 // this lane's first column (all interior)
-  const int xr = C::kHalo + warp * kCols + 4 * lane;   // its staged column
-  const int xl = C::kHalo + warp * kCols - 1;          // Ez/Hy (i0 - 1)
-  const int xe = C::kHalo + warp * kCols + kCols;      // Ez (i0 + 128)
+  const int xr = C::kHalo + wl * kCols + 4 * lane;     // its staged column
+  const int xl = C::kHalo + wl * kCols - 1;            // Ez/Hy (i0 - 1)
+  const int xe = C::kHalo + wl * kCols + kCols;        // Ez (i0 + 128)
   const int nst = (j1 - j0 + C::kRows - 1) / C::kRows;
   const bool producer = tid == 0;
   R.issued = R.used;
@@ -191,7 +197,7 @@ __device__ void tband(const DevShot& S, const TensorMaps& M, TRing& R, int c0, i
     }
     const unsigned char* st = R.stage + s * C::kStageBytes;
     const int jr = j0 + k * C::kRows;
-    const int rows_here = min(C::kRows, j1 - jr);
+    const int rows_here = act ? min(C::kRows, j1 - jr) : 0;
     for (int r = 0; r < rows_here; ++r) {
       const int j = jr + r;
       const int jn = j + 1 < j1 ? j + 1 : j;
@@ -399,9 +405,17 @@ __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const in
   const float rj = kScaled ? __fmul_rn(S.sc[3], iH) : 1.f;                         // sJ/sH
   const float rk = kScaled ? __fmul_rn(__fmul_rn(S.sc[4], sE), S.isc[3]) : 1.f;    // sK sE/sJ
 
-  const int i0 = c0 + warp * kCols;            // this warp's first column
+  // The first `idle` warps of a unit (bits 4-6 of its ring word) lie left of
+  // R: a region that is not a whole number of units wide starts with a unit
+  // whose leading columns belong to the CPML-band kernel.  Those warps only
+  // follow the stages (barrier waits and arrivals); their few preamble
+  // loads read the first working warp's columns, which are in bounds.
+  const int idle = (ring >> 4) & 7;
+  const bool act = warp >= idle;
+  const int wl = act ? warp : idle;            // the warp whose columns this one addresses
+  const int i0 = c0 + wl * kCols;              // this warp's first column
   const int i = i0 + 4 * lane;                 // this lane's first column
-  const int xr = C::kHalo + warp * kCols + 4 * lane;   // its staged column
+  const int xr = C::kHalo + wl * kCols + 4 * lane;     // its staged column
   // the warp's edge column: lane 0 the one left of the warp, the other lanes
   // (for use: lane 31) the one right of it
   const int xc = lane == 0 ? i0 - 1 : i0 + kCols;
@@ -465,7 +479,7 @@ __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const in
     }
     const unsigned char* st = R.stage + s * C::kStageBytes;
     const int jr = jb + k * C::kRows;
-    const int rows_here = min(C::kRows, jb + rows_n - jr);
+    const int rows_here = act ? min(C::kRows, jb + rows_n - jr) : 0;
     for (int r = 0; r < rows_here; ++r) {
       const int j = jr + r;
       const int jn = j + 1 <= j1 ? j + 1 : j;
@@ -524,7 +538,7 @@ __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const in
           St::stcs4(hxm + o, hxn);
           St::stcs4(hym + o, hyn);
           St::stcs4(jzm + o, jzn);
-        } else if ((ring & kRingLeft) && warp == 0 && lane == 0) {
+        } else if ((ring & kRingLeft) && warp == idle && lane == 0) {
           St::st1(ezm + o, ezs_n[0]);
           St::st1(hxm + o, hxn[0]);
           St::st1(hym + o, hyn[0]);
@@ -636,7 +650,7 @@ step_tmat_kernel(const __grid_constant__ DevShot S, const __grid_constant__ Tens
   if (n < 1 || n > S.n_steps) return;
   for (int u = blockIdx.x; u < n_units; u += gridDim.x) {
     const int4 ud = __ldg(units + u);
-    tband<C>(S, M, R, ud.y, ud.z, ud.w, n, err);
+    tband<C>(S, M, R, ud.y, ud.z, ud.w, (ud.x >> 4) & 7, n, err);
     if (*(volatile int*)err) return;
   }
 }

@@ -240,6 +240,35 @@ def test_two_step_equals_one_step(gpu, monkeypatch, shape, storage):
         assert np.array_equal(ref[k], got[k]), (shape, k)
 
 
+@pytest.mark.parametrize("tma,nx,storage", [("1,3", 2600, F.STORE_F32), ("2,2", 2600, F.STORE_F16),
+                                             ("1,2", 2344, F.STORE_BF16), ("1,4", 2344, F.STORE_F32)])
+def test_two_step_region_not_whole_units(gpu, monkeypatch, tma, nx, storage):
+    """The two-step region R spans whole one-row bands, not whole tensor
+    units: its first unit starts left of R and that unit's leading warps idle
+    (one band kernel of 128 columns at nx = 2600: 1 idle warp of 4; 256
+    columns: 2; 128 columns at nx = 2344: 3).  Every cell, psi value, trace
+    sample and DFT sum keeps the one-row kernel's bits, with sources and
+    detectors on R's first columns."""
+    monkeypatch.delenv("FDTD2D_KERNEL", raising=False)
+    ny, P, steps = 301, 11, 21
+    prob = F.Problem.from_spec(nx=nx, ny=ny, npml=P, n_steps=steps, profile=1, x_lo=nx // 3, x_hi=nx - 3,
+                               ne_peak=2e19, nu=3e9, n_elem=40, src_i=P + 1, src_j=P + 1, src_di=7, src_dj=7,
+                               n_det=40, det_i=P + 3, det_j=P + 2, det_di=5, det_dj=7, dft_freq=40e9,
+                               storage=storage, field_max=100.0)
+    st = _random_fields(nx, ny, P, 31)
+    chunks = (6, 1, 8, 6)
+    monkeypatch.setenv("FDTD2D_TMA", tma)
+    monkeypatch.setenv("FDTD2D_TMAT", "0")
+    name0, ref = _stepped_all(gpu, prob, st, steps, chunks)
+    assert "tmat" not in name0
+    monkeypatch.setenv("FDTD2D_TMAT", "4,2,2")
+    monkeypatch.setenv("FDTD2D_TB", "1")
+    name1, got = _stepped_all(gpu, prob, st, steps, chunks)
+    assert name1 == f"step_tmat2_kernel<4,2,2>+step_tma_kernel<{tma}>", name1
+    for k in ref:
+        assert np.array_equal(ref[k], got[k]), (tma, k)
+
+
 def test_two_step_fields_written_between_runs(gpu, monkeypatch):
     """Fields and psi written between run calls reach every buffer the
     two-step path rotates through: runs of 9, then a write, then 6 and 2
