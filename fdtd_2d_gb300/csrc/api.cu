@@ -453,7 +453,8 @@ std::map<ChoiceKey, KernelChoice> g_choice;
 
 ChoiceKey choice_key(const fdtd2d_ctx* c, int device, const char* what) {
   std::string env = what;
-  for (const char* v : {"FDTD2D_TMAT", "FDTD2D_TB", "FDTD2D_TMA", "FDTD2D_TMA_AUTOTUNE", "FDTD2D_TMAT_AUTOTUNE"}) {
+  for (const char* v : {"FDTD2D_TMAT", "FDTD2D_TB", "FDTD2D_TMA", "FDTD2D_TMA_AUTOTUNE", "FDTD2D_TMAT_AUTOTUNE",
+                        "FDTD2D_KERNEL", "FDTD2D_PERSIST"}) {
     const char* x = std::getenv(v);
     env += '|';
     env += x ? x : "-";
@@ -552,6 +553,98 @@ bool material_as_uniform(const fdtd2d_setup* s, double beta, float* ca, float* c
 // choice.  FDTD2D_TMAT=0 leaves the tensor path off, FDTD2D_TMAT=W,R,ST
 // forces a shape; FDTD2D_TB=0 leaves the two-step form out, FDTD2D_TB=1
 // keeps only it.
+// Grids up to this many cells are tried on the persistent kernel: there a
+// step's fields stay in L2 and the per-launch gaps, not bytes, set the
+// step time.
+constexpr int64_t kPersistMaxCells = int64_t(1) << 22;
+// Steps per persistent launch (a launch of a few tens of ms at most).
+constexpr int kPersistSteps = 4096;
+
+// The persistent form: FP32 single shots of at most kPersistMaxCells cells
+// whose path at create was timed (path_ms) or whose class chose it before.
+// Trial: one launch that repeats step 1 sixteen times with traces and the
+// DFT off (each repeat reads the same buffers and writes the same values),
+// against the chosen path's per-step time; kept when at least 10 % faster.
+// FDTD2D_PERSIST=0 never, =1 always (where it can run); not tried when
+// FDTD2D_TMA, FDTD2D_TMAT or FDTD2D_TB names a staged path.
+int setup_persist(fdtd2d_ctx* c, int device) {
+  const char* env = std::getenv("FDTD2D_PERSIST");
+  const int mode = env ? std::atoi(env) : -1;
+  DevShot& h = c->h;
+  if (mode == 0 || h.store != FDTD2D_STORE_F32 || c->n_steps < 2) return FDTD2D_OK;
+  if (mode < 0 && (int64_t)c->nx * c->ny > kPersistMaxCells) return FDTD2D_OK;
+  // a staged path forced by name is kept
+  if (mode < 0 && (std::getenv("FDTD2D_TMA") || std::getenv("FDTD2D_TMAT") || std::getenv("FDTD2D_TB")))
+    return FDTD2D_OK;
+  const int ctas = persist_resident_ctas(c->medium, device);
+  const int work = ctas * (kThreads / 32) - c->n_rc - (c->line_n > 0 ? 1 : 0);
+  if (ctas <= 0 || work < 1) return FDTD2D_OK;
+  const ChoiceKey key = choice_key(c, device, c->medium == FDTD2D_MEDIUM_UNIFORM ? "persist0" : "persist1");
+  KernelChoice known;
+  const bool have = mode < 0 && find_choice(key, &known);
+  if (have && known.k != 1) return FDTD2D_OK;
+  if (mode < 0 && !have && c->path_ms <= 0.f && c->tma) return FDTD2D_OK;   // nothing to compare with
+  const std::vector<int4> units = make_units(0, c->nx, c->ny, work, kCols, 2);
+  cudaError_t e = dalloc(c, &c->d_punits, units.size());
+  if (e == cudaSuccess) e = dalloc(c, &c->d_bar, 1);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->d_punits, units.data(), units.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  c->n_punits = (int)units.size();
+  c->persist_ctas = ctas;
+  bool use = mode == 1 || have;
+  if (!use) {
+    DevShot t = h;
+    t.record = 0;
+    t.dft = nullptr;
+    const int n1 = t.base_n + 1;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    float path = c->path_ms, ms = -1.f;
+    if (e == cudaSuccess && !c->tma) {
+      // the streaming kernel's step (never timed at create)
+      for (int r = 0; r < 4 && e == cudaSuccess; ++r) {
+        if (r == 1) e = cudaEventRecord(e0, c->stream);
+        if (e == cudaSuccess) e = launch_step(t, c->d_units, c->n_units, n1, c->medium, c->grid_warps, c->stream);
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&path, e0, e1);
+      path /= 3;
+    }
+    const PersistAux none{};
+    if (e == cudaSuccess)
+      e = launch_step_persist(t, c->d_punits, c->n_punits, n1, n1, 4, none, c->medium, ctas, c->d_bar, c->d_err,
+                              c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+    if (e == cudaSuccess)
+      e = launch_step_persist(t, c->d_punits, c->n_punits, n1, n1, 16, none, c->medium, ctas, c->d_bar, c->d_err,
+                              c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (e != cudaSuccess) return fail_cuda(c, e);
+    int derr = 0;
+    if (cudaMemcpy(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return FDTD2D_ERR_CUDA;
+    if (derr != kErrNone) return FDTD2D_ERR_TIMEOUT;
+    use = ms / 16 < 0.9f * path;
+    if (mode < 0) {
+      KernelChoice ch;
+      ch.k = use ? 1 : 0;
+      keep_choice(key, ch);
+    }
+  }
+  if (use) {
+    c->persist = true;
+    std::snprintf(c->kernel_name, sizeof c->kernel_name, "step_persist_kernel<%d>",
+                  c->medium == FDTD2D_MEDIUM_UNIFORM ? 0 : 1);
+  }
+  return FDTD2D_OK;
+}
+
 int setup_tmat(fdtd2d_ctx* c, int device) {
   const char* env = std::getenv("FDTD2D_TMAT");
   if (env && std::strcmp(env, "0") == 0) return FDTD2D_OK;
@@ -778,6 +871,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (psi_trial) cudaFreeAsync(psi_trial, c->stream);
+  if (!have && best > 0.f && best < 1e29f) c->path_ms = best / 3;   // trials time 3 steps
   if (h.fb[2] && !(best_k >= 0 && best_l == 2)) {
     // the two-step form lost: give its buffers back
     for (int b = 2; b < 4; ++b) {
@@ -840,7 +934,7 @@ void fdtd2d::adopt_ctx(fdtd2d_ctx* c, cudaStream_t batch_stream) {
   c->batch = true;
 }
 
-int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out) {
+int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out, bool solo) {
   if (!out) return FDTD2D_ERR_INVALID;
   *out = nullptr;
   int rc = validate(s);
@@ -1206,6 +1300,7 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
         return FDTD2D_ERR_TIMEOUT;
       }
       c->tma_shape = best_k;
+      c->path_ms = best / 3;   // three timed launches
       KernelChoice ch;
       ch.q = best_k;
       keep_choice(choice_key(c, device, "tma"), ch);
@@ -1225,6 +1320,7 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
   CK(cudaMemcpyAsync(c->d_units, units.data(), units.size() * sizeof(int4), cudaMemcpyHostToDevice,
                      c->stream));
   if (c->tma && !member) CK_RC(setup_tmat(c, device));
+  if (!member && !solo) CK_RC(setup_persist(c, device));
   CK(dalloc(c, &c->d_flag, 1));
   CK(cudaStreamSynchronize(c->stream));
 #undef CK
@@ -1245,6 +1341,40 @@ int fdtd2d_run(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
     cudaError_t e = cudaEventRecord(c->ev_m, c->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_m, 0);
     if (e != cudaSuccess) return fail_cuda(c, e);
+  }
+  if (c->persist) {
+    // all the steps in persistent launches, the tracker and the line probe
+    // on their service warps
+    PersistAux A{};
+    if (c->n_rc > 0) {
+      A.n_rc = c->n_rc;
+      A.scan_i = c->d_rc_scan;
+      A.max_i = c->d_rc_max;
+      A.j_cut = c->rc_j_cut;
+      A.level = c->rc_level;
+      A.edge = c->d_edge;
+      A.spd = c->d_spd;
+    }
+    if (c->line_n > 0) {
+      A.line_n = c->line_n;
+      A.line_j = c->line_j;
+      A.line_i0 = c->line_i0;
+      A.line_first = c->line_first;
+      A.line_last = c->line_last;
+      A.line = c->d_line;
+    }
+    for (int32_t n = n_first; n <= n_last;) {
+      const int32_t m = (int32_t)std::min<int64_t>(n_last, (int64_t)n + kPersistSteps - 1);
+      cudaEvent_t p0 = prof_mark(c, nullptr, 0, m - n + 1);
+      const cudaError_t e = launch_step_persist(c->h, c->d_punits, c->n_punits, n, m, 0, A, c->medium,
+                                                c->persist_ctas, c->d_bar, c->d_err, c->stream);
+      if (p0) prof_mark(c, p0, (int64_t)c->nx * c->ny, m - n + 1);
+      if (e != cudaSuccess) return fail_cuda(c, e);
+      ++c->launches;
+      c->step = m;
+      n = m + 1;
+    }
+    return FDTD2D_OK;
   }
   bool paired = false;   // the last iteration issued a pair
   for (int32_t n = n_first; n <= n_last; ++n) {

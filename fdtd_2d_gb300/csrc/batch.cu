@@ -232,7 +232,7 @@ int add_solo(fdtd2d_batch* b, const fdtd2d_setup* s, int64_t bytes, int32_t* sho
     slot = (int)b->m.size() - 1;
   }
   fdtd2d_ctx* c = nullptr;
-  const int rc = create_ctx(s, b->device, false, &c);   // its own streams, kernel choice timed
+  const int rc = create_ctx(s, b->device, false, &c, true);   // its own streams, kernel choice timed
   if (rc) return rc;
   // the bytes it holds: two more field buffers on the two-step path
   if (c->tb) bytes += 2 * c->h.cells * 4 * store_bytes(c->h.store);

@@ -44,6 +44,16 @@ struct fdtd2d_ctx {
   int4* d_eunits = nullptr;   // the rest (staged kernel)
   int n_eunits = 0;
   fdtd2d::TensorMaps maps{};
+  // the per-step time of the path chosen at create, from its trials (0:
+  // not timed here: forced, or the class's choice was remembered)
+  float path_ms = 0.f;
+  // persistent form (step_persist_kernel): many steps per cooperative
+  // launch, its own units and barrier word
+  bool persist = false;
+  int persist_ctas = 0;
+  int4* d_punits = nullptr;
+  int n_punits = 0;
+  unsigned* d_bar = nullptr;
   // the CPML-band kernel runs on a second stream beside the interior one:
   // ev_t marks the interior kernel of the last step, ev_e the CPML kernel,
   // ev_m the shot stream's work before a run
@@ -72,7 +82,10 @@ struct fdtd2d_ctx {
 namespace fdtd2d {
 // fdtd2d_create; member = true makes a shot for a batch: no launch-shape
 // timing, and the batch adopts it (adopt_ctx) once its uploads are done.
-int create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out);
+// solo = true makes a batch's solo member, which runs beside the batch's
+// kernel: never the persistent form, whose cooperative launch wants the
+// whole GPU.
+int create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out, bool solo = false);
 // Hand a member shot to the batch's stream: its own stream is released and
 // fdtd2d_run is refused from then on (the batch steps it).
 void adopt_ctx(fdtd2d_ctx* c, cudaStream_t batch_stream);

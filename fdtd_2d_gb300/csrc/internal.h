@@ -132,6 +132,33 @@ cudaError_t launch_step(const DevShot& shot, const int4* units, int n_units,
 // Launch capacity: number of warps the step kernel keeps resident at once.
 int resident_warps(int medium, int device);
 
+// What the persistent kernel's service warps do after each step, while the
+// other warps run the next one: the wave-front tracker's lines (launch_rc's
+// work, one warp per line) and the line probe (launch_line's), for the steps
+// they cover.  Zero counts: none.
+struct PersistAux {
+  int n_rc;
+  const int* scan_i;
+  const int* max_i;
+  int j_cut;
+  float level;
+  float* edge;                // [n_rc]
+  int* spd;                   // [step][n_rc], row n-1 for step n
+  int line_n, line_j, line_i0, line_first, line_last;
+  float* line;                // [n - line_first][line_n]
+};
+
+// The register-streaming step for steps n_first..n_last (global numbering)
+// in one cooperative launch of `ctas` CTAs (at most persist_resident_ctas):
+// the warps step the units, a grid barrier (bounded in time; *err set when
+// it gives out) between steps.  repeat > 0: step n_first `repeat` times
+// instead (a timing trial: the same reads and writes each time).  bar: one
+// device word the launch zeroes first.
+cudaError_t launch_step_persist(const DevShot& shot, const int4* units, int n_units, int n_first, int n_last,
+                                int repeat, const PersistAux& aux, int medium, int ctas, unsigned* bar, int* err,
+                                cudaStream_t stream);
+int persist_resident_ctas(int medium, int device);
+
 // Device error codes written by kernels with bounded waits.
 enum DeviceError : int { kErrNone = 0, kErrWaitTimeout = 1 };
 

@@ -58,6 +58,37 @@ __device__ __forceinline__ void ld4_nc(float (&d)[4], const float* p) {
   const float4 v = __ldcs(reinterpret_cast<const float4*>(p));
   d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
 }
+// Loads of arrays a launch also writes (fields, psi).  kCoh false: through
+// the read-only path (ldf4) or streaming (ldfs4), for kernels that run one
+// step.  kCoh true: from L2, the point of coherence, because the array may
+// have been written earlier in the same launch by another CTA (the
+// persistent kernel's later steps); a read-only or L1-cached copy could be
+// stale there.
+template <bool kCoh>
+__device__ __forceinline__ void ldf4(float (&d)[4], const float* p) {
+  if constexpr (kCoh) {
+    const float4 v = __ldcg(reinterpret_cast<const float4*>(p));
+    d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+  } else {
+    ld4(d, p);
+  }
+}
+template <bool kCoh>
+__device__ __forceinline__ void ldfs4(float (&d)[4], const float* p) {
+  if constexpr (kCoh) {
+    ldf4<true>(d, p);
+  } else {
+    ld4_nc(d, p);
+  }
+}
+template <bool kCoh>
+__device__ __forceinline__ float ldf1(const float* p) {
+  if constexpr (kCoh) {
+    return __ldcg(p);
+  } else {
+    return *p;
+  }
+}
 __device__ __forceinline__ void st4(float* p, const float (&d)[4]) {
   *reinterpret_cast<float4*>(p) = make_float4(d[0], d[1], d[2], d[3]);
 }
@@ -143,13 +174,13 @@ __device__ __forceinline__ void h_coef(const DevShot& S, const MatH* mat_h, cons
 
 // New Hy at one cell (c, j) from old values, CPML included.  Used for the
 // lane-0 halo value Hy_new(i0-1, j).  Reads only the old buffers.
-template <int MEDIUM>
+template <int MEDIUM, bool kCoh = false>
 __device__ float hy_cell(const DevShot& S, const MatH* mat_h, int par, int c, int j,
                          float ez_c, float ez_c1) {
   const int64_t off = (int64_t)j * S.pitch + c;
   float da, db;
   h_coef<MEDIUM>(S, mat_h, S.id2, off, da, db);
-  const float hyo = field_ptr(S, kHy, par)[off];
+  const float hyo = ldf1<kCoh>(field_ptr(S, kHy, par) + off);
   float h = covered<MEDIUM>(S, kCovHy, (long long)j * (S.nx - 1) + c)
                 ? upd_h(da, hyo, db, ez_c1, ez_c, S.den_hx[c]) : hyo;
   const int P = S.npml;
@@ -159,7 +190,7 @@ __device__ float hy_cell(const DevShot& S, const MatH* mat_h, int par, int c, in
   if (side >= 0 && covered<MEDIUM>(S, kCovHyPml, (long long)j * (P - 1) + r)) {
     const float* tb = S.cpml + (side ? kBhX2 : kBhX1) * P;
     const float* tc = S.cpml + (side ? kChX2 : kChX1) * P;
-    const float psi = S.psi[par * S.psi_buf + S.o_hyx + ((int64_t)side * S.ny + j) * P + r];
+    const float psi = ldf1<kCoh>(S.psi + par * S.psi_buf + S.o_hyx + ((int64_t)side * S.ny + j) * P + r);
     const float pn = upd_psi(tb[r], psi, tc[r], ez_c1, ez_c);
     h = __fmaf_rn(db, pn, h);
   }
@@ -169,7 +200,7 @@ __device__ float hy_cell(const DevShot& S, const MatH* mat_h, int par, int c, in
 // One Hx row segment (i..i+3, j): bulk update + y-strip CPML.  `own` writes
 // the new psi: only the owning unit does, and only from lanes that hold real
 // columns (inactive lanes run with their address clamped to column 0).
-template <int MEDIUM>
+template <int MEDIUM, bool kCoh = false>
 __device__ __forceinline__ void hx_row(const DevShot& S, const MediumRow<MEDIUM>& m, int par, int i, int j, const float (&ezj)[4],
                                        const float (&ezj1)[4], const float (&hxo)[4],
                                        float (&out)[4], bool own) {
@@ -189,7 +220,7 @@ __device__ __forceinline__ void hx_row(const DevShot& S, const MediumRow<MEDIUM>
     const float c = S.cpml[(side ? kChY2 : kChY1) * P + r];
     const int64_t poff = ((int64_t)side * (P - 1) + r) * S.pitch + i;
     float psi[4], pn[4];
-    ld4(psi, S.psi + par * S.psi_buf + poff);
+    ldf4<kCoh>(psi, S.psi + par * S.psi_buf + poff);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       pn[k] = psi[k];

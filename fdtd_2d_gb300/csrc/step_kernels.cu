@@ -25,12 +25,13 @@
 
 #include "internal.h"
 #include "step_common.cuh"
+#include "tma_common.cuh"
 
 #include <cstdio>
 
 namespace fdtd2d {
 
-template <int MEDIUM>
+template <int MEDIUM, bool kCoh = false>
 __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e, const MatH* mat_h,
                                              int i0, int j0, int j1, int n, int lane) {
   const int nx = S.nx, ny = S.ny, P = S.npml;
@@ -60,17 +61,17 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
   float ezc[4], hxp[4];
   zero4(ezc);
   zero4(hxp);
-  if (act) ld4(ezc, ezo + (int64_t)j0 * pitch + ic);
+  if (act) ldf4<kCoh>(ezc, ezo + (int64_t)j0 * pitch + ic);
   if (j0 >= 1) {
     // Hx_new(j0-1): recomputed from old values (the unit below owns it).
     float ezp[4], hxo[4];
     zero4(ezp); zero4(hxo);
     if (act) {
-      ld4(ezp, ezo + (int64_t)(j0 - 1) * pitch + ic);
-      ld4(hxo, hxo_p + (int64_t)(j0 - 1) * pitch + ic);
+      ldf4<kCoh>(ezp, ezo + (int64_t)(j0 - 1) * pitch + ic);
+      ldf4<kCoh>(hxo, hxo_p + (int64_t)(j0 - 1) * pitch + ic);
     }
     m.load(S, mat_e, mat_h, (int64_t)(j0 - 1) * pitch + ic);
-    hx_row<MEDIUM>(S, m, par, ic, j0 - 1, ezp, ezc, hxo, hxp, false);
+    hx_row<MEDIUM, kCoh>(S, m, par, ic, j0 - 1, ezp, ezc, hxo, hxp, false);
   }
 
   // Prefetched row j data.
@@ -78,10 +79,10 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
   zero4(ezn); zero4(hxo); zero4(hyo); zero4(jzo);
   if (act) {
     const int64_t o = (int64_t)j0 * pitch + ic;
-    ld4_nc(ezn, ezo + o + pitch);   // j0 + 1 <= ny - 1 always (units stop at ny-1)
-    ld4_nc(hxo, hxo_p + o);
-    ld4_nc(hyo, hyo_p + o);
-    ld4_nc(jzo, jzo_p + o);
+    ldfs4<kCoh>(ezn, ezo + o + pitch);   // j0 + 1 <= ny - 1 always (units stop at ny-1)
+    ldfs4<kCoh>(hxo, hxo_p + o);
+    ldfs4<kCoh>(hyo, hyo_p + o);
+    ldfs4<kCoh>(jzo, jzo_p + o);
   }
 
   for (int j = j0; j < j1; ++j) {
@@ -92,20 +93,20 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
     float ezn2[4], hxo2[4], hyo2[4], jzo2[4];
     zero4(ezn2); zero4(hxo2); zero4(hyo2); zero4(jzo2);
     if (act && j + 1 < j1) {
-      ld4_nc(ezn2, ezo + o + 2 * pitch);
-      ld4_nc(hxo2, hxo_p + o + pitch);
-      ld4_nc(hyo2, hyo_p + o + pitch);
-      ld4_nc(jzo2, jzo_p + o + pitch);
+      ldfs4<kCoh>(ezn2, ezo + o + 2 * pitch);
+      ldfs4<kCoh>(hxo2, hxo_p + o + pitch);
+      ldfs4<kCoh>(hyo2, hyo_p + o + pitch);
+      ldfs4<kCoh>(jzo2, jzo_p + o + pitch);
     }
 
     // ---- H update (Dev_HxCalc/Dev_HxPML_Jdir_Calc, Dev_HyCalc/Dev_HyPML_Idir_Calc)
     float hxn[4];
-    hx_row<MEDIUM>(S, m, par, ic, j, ezc, ezn, hxo, hxn, act);
+    hx_row<MEDIUM, kCoh>(S, m, par, ic, j, ezc, ezn, hxo, hxn, act);
 
     float ezr_next = __shfl_down_sync(0xffffffffu, ezc[0], 1);
     if (lane == 31) {
       const int c = i0 + kCols;
-      ezr_next = (c < nx) ? ezo[(int64_t)j * pitch + c] : 0.f;
+      ezr_next = (c < nx) ? ldf1<kCoh>(ezo + (int64_t)j * pitch + c) : 0.f;
     }
     const float ezr[4] = {ezc[1], ezc[2], ezc[3], ezr_next};
     float hyn[4];
@@ -127,7 +128,7 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
           const float b = S.cpml[(side ? kBhX2 : kBhX1) * P + r];
           const float cc = S.cpml[(side ? kChX2 : kChX1) * P + r];
           const int64_t po = S.o_hyx + ((int64_t)side * ny + j) * P + r;
-          pn[k] = upd_psi(b, psr[po], cc, ezr[k], ezc[k]);
+          pn[k] = upd_psi(b, ldf1<kCoh>(psr + po), cc, ezr[k], ezc[k]);
           hyn[k] = __fmaf_rn(m.dby(k), pn[k], hyn[k]);
           psw[po] = pn[k];
         }
@@ -137,8 +138,8 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
     if (lane == 0) {
       hyl = 0.f;
       if (i0 >= 1) {
-        const float ezl = ezo[(int64_t)j * pitch + i0 - 1];
-        hyl = hy_cell<MEDIUM>(S, mat_h, par, i0 - 1, j, ezl, ezc[0]);
+        const float ezl = ldf1<kCoh>(ezo + (int64_t)j * pitch + i0 - 1);
+        hyl = hy_cell<MEDIUM, kCoh>(S, mat_h, par, i0 - 1, j, ezl, ezc[0]);
       }
     }
 
@@ -173,7 +174,7 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
           const float b = S.cpml[(side ? kBeX2 : kBeX1) * P + r];
           const float cc = S.cpml[(side ? kCeX2 : kCeX1) * P + r];
           const int64_t po = S.o_ezx + ((int64_t)side * ny + j) * P + r;
-          const float pn = upd_psi(b, psr[po], cc, hyn[k], hyl4[k]);
+          const float pn = upd_psi(b, ldf1<kCoh>(psr + po), cc, hyn[k], hyl4[k]);
           ezw4[k] = __fmaf_rn(m.cB(k), pn, ezw4[k]);
           psw[po] = pn;
         }
@@ -186,7 +187,7 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
       const float cc = S.cpml[(side ? kCeY2 : kCeY1) * P + r];
       const int64_t po = S.o_ezy + ((int64_t)side * P + r) * pitch + ic;
       float psi[4], pn[4];
-      ld4(psi, psr + po);
+      ldf4<kCoh>(psi, psr + po);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         const int c = i + k;
@@ -287,6 +288,151 @@ cudaError_t launch_step(const DevShot& shot, const int4* units, int n_units, int
     step_stream_kernel<1><<<blocks, kThreads, 0, stream>>>(shot, units, n_units, n_global);
   }
   return cudaGetLastError();
+}
+
+// ---- persistent form: many steps per cooperative launch ------------------
+
+// Grid-wide barrier of a cooperative launch.  Thread 0 of each CTA releases
+// the CTA's writes, adds one to *count and waits until the count reaches
+// `target` (every CTA has arrived), for at most kWaitNs, or until another
+// CTA has set *err.  False when the barrier did not complete.
+__device__ bool grid_barrier(unsigned* count, unsigned target, int* err) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(count, 1u);
+    int ok = 1;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+      unsigned v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(count) : "memory");
+      if (v >= target) break;
+      if (*(volatile int*)err != kErrNone) {
+        ok = 0;
+        break;
+      }
+      if (global_ns() - t0 > kWaitNs) {
+        atomicExch(err, kErrWaitTimeout);
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// One wave-front tracker line of one step with one warp: rc_kernel's
+// outputs (the column maximum from row j_cut with row 0 as the start, the
+// edge level kept as a running maximum, the deepest row in [1, ny-3] at or
+// above it), from L2.
+__device__ void rc_warp(const float* ez, int64_t pitch, int ny, int is, int im, int j_cut, float level, float* edge,
+                        int* spd, int lane) {
+  float m = -INFINITY;
+  for (int j = j_cut + lane; j < ny - 2; j += 32) m = fmaxf(m, __ldcg(ez + (int64_t)j * pitch + im));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  float e = 0.f;
+  if (lane == 0) {
+    float temp = __ldcg(ez + im);
+    if (m > temp) temp = m;
+    const float cand = temp * level;
+    e = *edge;
+    if (cand > e) e = cand;
+    *edge = e;
+  }
+  e = __shfl_sync(0xffffffffu, e, 0);
+  int best = 0;
+  for (int j = 1 + lane; j <= ny - 3; j += 32)
+    if (!(fabsf(__ldcg(ez + (int64_t)j * pitch + is)) < e)) best = j;
+  for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if (lane == 0) *spd = best;
+}
+
+// Service warp k's work after step n (global) of a single shot: tracker
+// line k, or (k == n_rc) the line probe's row.
+__device__ void persist_service(const DevShot& S, const PersistAux& A, int n, int k, int lane) {
+  const float* ez = field_ptr(S, kEz, (n - S.base_n) & 1);
+  if (k < A.n_rc) {
+    rc_warp(ez, S.pitch, S.ny, __ldg(A.scan_i + k), __ldg(A.max_i + k), A.j_cut, A.level, A.edge + k,
+            A.spd + (int64_t)(n - 1) * A.n_rc + k, lane);
+  } else if (n >= A.line_first && n <= A.line_last) {
+    float* dst = A.line + (int64_t)(n - A.line_first) * A.line_n;
+    const float* src = ez + (int64_t)A.line_j * S.pitch + A.line_i0;
+    for (int t = lane; t < A.line_n; t += 32) dst[t] = __ldcg(src + t);
+  }
+}
+
+// Steps n_first..n_last of one shot in one launch.  Warps [0, n_work) step
+// the units (the same unit to the same warp every step, so a detector's DFT
+// sum is always the same thread's); the last warps serve step n (tracker,
+// line probe) while the others run step n+1, which writes the other buffer.
+// Every mutable array is read from L2 (process_unit<M, true>), the grid
+// barrier orders the steps, and the arithmetic is step_stream_kernel's, so
+// the results are its bits.
+template <int MEDIUM>
+__global__ void __launch_bounds__(kThreads, 2)
+step_persist_kernel(const __grid_constant__ DevShot S, const int4* __restrict__ units, int n_units, int n_first,
+                    int n_last, int repeat, const __grid_constant__ PersistAux A, unsigned* bar, int* err) {
+  __shared__ MatE s_mat_e[MEDIUM ? 256 : 1];
+  __shared__ MatH s_mat_h[MEDIUM ? 256 : 1];
+  if (MEDIUM) {
+    for (int t = threadIdx.x; t < 256; t += blockDim.x) {
+      s_mat_e[t] = S.mat_e[t];
+      s_mat_h[t] = S.mat_h[t];
+    }
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31;
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int n_warps = (int)((gridDim.x * blockDim.x) >> 5);
+  const int n_work = n_warps - A.n_rc - (A.line_n > 0 ? 1 : 0);
+  const int steps = repeat > 0 ? repeat : n_last - n_first + 1;
+  unsigned target = 0;
+  for (int s = 0; s <= steps; ++s) {
+    if (warp < n_work) {
+      const int nl = (repeat > 0 ? n_first : n_first + s) - S.base_n;
+      if (s < steps && nl >= 1 && nl <= S.n_steps)
+        for (int u = warp; u < n_units; u += n_work) {
+          const int4 ud = __ldg(units + u);
+          process_unit<MEDIUM, true>(S, s_mat_e, s_mat_h, ud.y, ud.z, ud.w, nl, lane);
+        }
+    } else if (s > 0 && repeat == 0) {
+      persist_service(S, A, n_first + s - 1, warp - n_work, lane);
+    }
+    if (s == steps) break;
+    target += gridDim.x;
+    if (!grid_barrier(bar, target, err)) return;
+  }
+}
+
+cudaError_t launch_step_persist(const DevShot& shot, const int4* units, int n_units, int n_first, int n_last,
+                                int repeat, const PersistAux& aux, int medium, int ctas, unsigned* bar, int* err,
+                                cudaStream_t stream) {
+  if (ctas <= 0 || ctas * (kThreads / 32) <= aux.n_rc + (aux.line_n > 0 ? 1 : 0)) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(unsigned), stream);
+  if (e != cudaSuccess) return e;
+  DevShot s = shot;
+  PersistAux a = aux;
+  void* args[] = {&s, (void*)&units, &n_units, &n_first, &n_last, &repeat, &a, &bar, &err};
+  const void* fn = medium == 0 ? (const void*)step_persist_kernel<0> : (const void*)step_persist_kernel<1>;
+  return cudaLaunchCooperativeKernel(fn, dim3(ctas), dim3(kThreads), args, 0, stream);
+}
+
+int persist_resident_ctas(int medium, int device) {
+  int sms = 0, per_sm = 0, coop = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+  if (!coop) return 0;
+  if (medium == 0) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_persist_kernel<0>, kThreads, 0);
+  } else {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_persist_kernel<1>, kThreads, 0);
+  }
+  return sms * per_sm;
 }
 
 int resident_warps(int medium, int device) {

@@ -165,6 +165,7 @@ def test_material_medium_as_uniform(gpu, monkeypatch, tmp_path):
             out["rc"] = shot.rc()
         return name, out
 
+    monkeypatch.setenv("FDTD2D_PERSIST", "0")
     monkeypatch.setenv("FDTD2D_MATERIAL_AS_UNIFORM", "0")
     name0, ref = stepped()
     assert name0 == "step_stream_kernel<1>", name0
@@ -173,3 +174,51 @@ def test_material_medium_as_uniform(gpu, monkeypatch, tmp_path):
     assert name1.startswith("step_tma"), name1
     for k in ref:
         assert np.array_equal(ref[k], got[k]), k
+
+
+def test_persistent_settings_ini(gpu, monkeypatch, tmp_path):
+    """The persistent kernel on a Settings.ini shot (the golden
+    sphere-and-fluctuation case at 500 x 1200 cells, 21 tracker lines, a
+    line-probe window), in the material medium and as the uniform medium:
+    fields, psi, traces, tracker rows and probe rows are the streaming
+    material kernel's bits, the tracker and the probe running on service
+    warps beside the next step.  Run calls of 1 to 170 steps."""
+    ini = (GOLDEN / "sphere_fluc_chirp" / "Settings.ini").read_text()
+    for key, val in (("Imax", "250"), ("Jmax", "600"), ("Use_Exp_time", "0"), ("Max_time", "300")):
+        ini = re.sub(rf"(?m)^{key}\s*=.*$", f"{key} = {val}", ini)
+    path = tmp_path / "Settings.ini"
+    path.write_text(ini)
+    prob = F.Problem.from_ini(path)
+    s = prob.setup
+    assert (s.nx, s.ny) == (500, 1200) and s.n_rc > 0
+    s.line_n, s.line_i0, s.line_j, s.line_first, s.line_last = 400, 50, 700, 120, 180
+    chunks = (1, 118, 3, 170, prob.n_steps - 292)
+    assert chunks[-1] >= 1
+
+    def stepped():
+        with F.Shot(prob, gpu) as shot:
+            name = shot.kernel_name()
+            n = 1
+            for c in chunks:
+                shot.run(n, n + c - 1)
+                n += c
+            out = {w: shot.read_field(w) for w in FIELDS + PSI_FIELDS}
+            out["det"] = shot.traces()["det_ez"]
+            out["rc"] = shot.rc()
+            out["line"] = shot.line(120, 180)
+        return name, out
+
+    monkeypatch.setenv("FDTD2D_MATERIAL_AS_UNIFORM", "0")
+    monkeypatch.setenv("FDTD2D_PERSIST", "0")
+    name0, ref = stepped()
+    assert name0 == "step_stream_kernel<1>", name0
+    monkeypatch.setenv("FDTD2D_PERSIST", "1")
+    name1, got = stepped()
+    assert name1 == "step_persist_kernel<1>", name1
+    for k in ref:
+        assert np.array_equal(ref[k], got[k]), ("material", k)
+    monkeypatch.delenv("FDTD2D_MATERIAL_AS_UNIFORM")
+    name2, got = stepped()
+    assert name2 == "step_persist_kernel<0>", name2
+    for k in ref:
+        assert np.array_equal(ref[k], got[k]), ("as uniform", k)

@@ -16,15 +16,20 @@ pytestmark = pytest.mark.gpu
 
 # Uniform-medium shots run on the shared-memory staged kernel by default;
 # FDTD2D_KERNEL=stream selects the register-streaming kernel.  Both are checked.
-KERNELS = ["tma", "stream"]
+KERNELS = ["tma", "stream", "persist"]
 
 
 @pytest.fixture(params=KERNELS)
 def kernel(request, monkeypatch):
-    if request.param == "stream":
-        monkeypatch.setenv("FDTD2D_KERNEL", "stream")
-    else:
+    """tma: the staged kernels as timed at create; stream: the streaming
+    kernel; persist: the streaming kernel's persistent form (many steps per
+    cooperative launch)."""
+    if request.param == "tma":
         monkeypatch.delenv("FDTD2D_KERNEL", raising=False)
+        monkeypatch.setenv("FDTD2D_PERSIST", "0")
+    else:
+        monkeypatch.setenv("FDTD2D_KERNEL", "stream")
+        monkeypatch.setenv("FDTD2D_PERSIST", "1" if request.param == "persist" else "0")
     return request.param
 
 
@@ -269,6 +274,34 @@ def test_two_step_region_not_whole_units(gpu, monkeypatch, tma, nx, storage):
         assert np.array_equal(ref[k], got[k]), (tma, k)
 
 
+@pytest.mark.parametrize("nx,ny,P", [(520, 300, 11), (1000, 613, 20)])
+def test_persistent_equals_stream(gpu, monkeypatch, nx, ny, P):
+    """The persistent kernel (FDTD2D_PERSIST=1: a run call's steps in one
+    cooperative launch, a grid barrier between steps, the line probe on a
+    service warp) gives every cell, psi value, trace sample, DFT sum and
+    line-probe row the streaming kernel's bits: 40 sources and 40 detectors
+    across warp edges and the CPML, random state, run calls of 1 to 9 steps,
+    a probe window across a call boundary."""
+    monkeypatch.setenv("FDTD2D_KERNEL", "stream")
+    steps = 25
+    prob = F.Problem.from_spec(nx=nx, ny=ny, npml=P, n_steps=steps, profile=1, x_lo=nx // 3, x_hi=nx - 3,
+                               ne_peak=2e19, nu=3e9, n_elem=40, src_i=P - 3, src_j=P + 1, src_di=13, src_dj=7,
+                               n_det=40, det_i=P - 2, det_j=P + 2, det_di=11, det_dj=7, dft_freq=40e9,
+                               field_max=100.0)
+    s = prob.setup
+    s.line_n, s.line_i0, s.line_j, s.line_first, s.line_last = nx // 2, 3, ny // 3, 6, 12
+    st = _random_fields(nx, ny, P, 41)
+    chunks = (7, 2, 9, 1, 6)
+    monkeypatch.setenv("FDTD2D_PERSIST", "0")
+    name0, ref = _stepped_all(gpu, prob, st, steps, chunks)
+    assert name0 == "step_stream_kernel<0>", name0
+    monkeypatch.setenv("FDTD2D_PERSIST", "1")
+    name1, got = _stepped_all(gpu, prob, st, steps, chunks)
+    assert name1 == "step_persist_kernel<0>", name1
+    for k in ref:
+        assert np.array_equal(ref[k], got[k]), k
+
+
 def test_two_step_fields_written_between_runs(gpu, monkeypatch):
     """Fields and psi written between run calls reach every buffer the
     two-step path rotates through: runs of 9, then a write, then 6 and 2
@@ -350,9 +383,9 @@ def test_autotuned_shape_and_deep_cpml(gpu, monkeypatch):
     monkeypatch.delenv("FDTD2D_KERNEL", raising=False)
     monkeypatch.delenv("FDTD2D_TMA", raising=False)
     assert _random_state_case(gpu, 700, 130, 16).startswith(("step_tma_kernel<", "step_tmat_kernel<",
-                                                             "step_tmat2_kernel<"))
+                                                             "step_tmat2_kernel<", "step_persist_kernel<0>"))
     _random_state_case(gpu, 1600, 140, 12)   # interior bands: the tensor pair competes in the timing
-    assert _random_state_case(gpu, 300, 260, 121, steps=20) == "step_stream_kernel<0>"
+    assert _random_state_case(gpu, 300, 260, 121, steps=20) in ("step_stream_kernel<0>", "step_persist_kernel<0>")
 
 
 def test_phased_array_traces_and_dft(gpu, kernel):
