@@ -584,7 +584,10 @@ int setup_persist(fdtd2d_ctx* c, int device) {
   const bool have = mode < 0 && find_choice(key, &known);
   if (have && known.k != 1) return FDTD2D_OK;
   if (mode < 0 && !have && c->path_ms <= 0.f && c->tma) return FDTD2D_OK;   // nothing to compare with
-  const std::vector<int4> units = make_units(0, c->nx, c->ny, work, kCols, 2);
+  // units down to one row: a step's time is the longest warp's chain of
+  // dependent loads, which grows with its rows (512^2: 6.8 against 12.7 us
+  // per step with two-row units)
+  const std::vector<int4> units = make_units(0, c->nx, c->ny, work, kCols, 1);
   cudaError_t e = dalloc(c, &c->d_punits, units.size());
   if (e == cudaSuccess) e = dalloc(c, &c->d_bar, 1);
   if (e == cudaSuccess)
