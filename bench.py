@@ -183,14 +183,19 @@ def profile_traffic(kernel: str, cells: int) -> float | None:
 
 
 def workload_config(args) -> dict:
+    bpc = BYTES_PER_CELL if getattr(args, "storage", "f32") == "f32" else 18
+    touched = bpc * args.size * args.size   # bytes one time step reads and writes
+    l2 = (f"no flush: {touched / 1e9:.2g} GB touched per time step >> 129 MB L2" if touched > 4 * 129e6 else
+          f"no flush: {touched / 1e6:.3g} MB touched per time step, L2-resident (a small-grid case, not the "
+          "HBM-bound workload)")
     return {"workload": f"{args.size}x{args.size} TMz phased-array reflectometry shot: 32-cell CPML, "
                         "tanh x GRF plasma, nu 2e9/s, 16 elements at 50 GHz steered 15 deg, 16 Ez "
                         "detectors + FP64 DFT",
             "nx": args.size, "ny": args.size, "npml": 32, "shot_steps": 20000, "block_steps": args.block,
             "dx_mm": 0.25, "courant": 0.99,
-            "bytes_per_cell_update": BYTES_PER_CELL if getattr(args, "storage", "f32") == "f32" else 18,
+            "bytes_per_cell_update": bpc,
             "storage": getattr(args, "storage", "f32"),
-            "l2": "no flush: 2.4 GB touched per time step >> 129 MB L2",
+            "l2": l2,
             "parallelism": f"replicas x{args.gpus}"}
 
 
@@ -524,10 +529,12 @@ def run_ours(args, world, rank, local, dist) -> None:
 
     # roofline of the interior step kernel: algorithmic bytes of one launch
     # (bpc per cell of its region: each field read and written once per
-    # launch, whether it advances them one time step or two) over its mean
+    # pass, whether a pass advances them one time step or two; the
+    # persistent kernel's launch makes one pass per step) over its mean
     # event-timed launch duration
     per_launch_s = kt["ms"] / 1e3 / max(kt["launches"], 1)
-    alg_bytes = bpc * kt["cells"]
+    passes = kt["steps"] if kernel.startswith("step_persist") else 1
+    alg_bytes = bpc * kt["cells"] * passes
     achieved = alg_bytes / per_launch_s / 1e9
     step_gbs = bpc * cells / ((ms / 1e3) / (K * S)) / 1e9   # bpc per cell-update at the whole-step rate
     peaks = measured_peaks()
