@@ -560,6 +560,30 @@ constexpr int64_t kPersistMaxCells = int64_t(1) << 22;
 // Steps per persistent launch (a launch of a few tens of ms at most).
 constexpr int kPersistSteps = 4096;
 
+// Persistent launches of every shot of this process on a device run one at a
+// time: each waits for the previous one (on whichever stream it ran) and
+// leaves an event for the next.  Two cooperative grids that each fill the
+// GPU then never wait on each other's CTAs.
+std::mutex g_persist_mu;
+cudaEvent_t g_persist_last[64] = {};
+
+cudaError_t launch_persist_ordered(fdtd2d_ctx* c, int32_t n, int32_t m, const PersistAux& A) {
+  if (c->device < 0 || c->device >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_persist_mu);
+  cudaEvent_t& last = g_persist_last[c->device];
+  cudaError_t e = cudaSuccess;
+  if (!last) {
+    e = cudaEventCreateWithFlags(&last, cudaEventDisableTiming);
+  } else {
+    e = cudaStreamWaitEvent(c->stream, last, 0);
+  }
+  if (e == cudaSuccess)
+    e = launch_step_persist(c->h, c->d_punits, c->n_punits, n, m, 0, A, c->medium, c->persist_ctas, c->d_bar,
+                            c->d_err, c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(last, c->stream);
+  return e;
+}
+
 // The persistent form: FP32 single shots of at most kPersistMaxCells cells
 // whose path at create was timed (path_ms) or whose class chose it before.
 // Trial: one launch that repeats step 1 sixteen times with traces and the
@@ -1369,8 +1393,7 @@ int fdtd2d_run(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
     for (int32_t n = n_first; n <= n_last;) {
       const int32_t m = (int32_t)std::min<int64_t>(n_last, (int64_t)n + kPersistSteps - 1);
       cudaEvent_t p0 = prof_mark(c, nullptr, 0, m - n + 1);
-      const cudaError_t e = launch_step_persist(c->h, c->d_punits, c->n_punits, n, m, 0, A, c->medium,
-                                                c->persist_ctas, c->d_bar, c->d_err, c->stream);
+      const cudaError_t e = launch_persist_ordered(c, n, m, A);
       if (p0) prof_mark(c, p0, (int64_t)c->nx * c->ny, m - n + 1);
       if (e != cudaSuccess) return fail_cuda(c, e);
       ++c->launches;

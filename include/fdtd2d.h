@@ -220,7 +220,8 @@ int64_t fdtd2d_device_bytes(const fdtd2d_setup *setup);
 int64_t fdtd2d_launch_count(const fdtd2d_ctx *ctx);
 
 /* Name of the step kernel this context launches, with its launch shape
-   (e.g. "step_tma_kernel<4,3>"; no counterpart in the reference). */
+   (e.g. "step_tma_kernel<4,3>", "step_tmat2_kernel<4,2,2>+step_tma_kernel<2,2>",
+   "step_persist_kernel<0>"; no counterpart in the reference). */
 const char *fdtd2d_kernel_name(const fdtd2d_ctx *ctx);
 
 /* ---- Batched and continuous stepping (no counterpart in the reference, which

@@ -302,6 +302,43 @@ def test_persistent_equals_stream(gpu, monkeypatch, nx, ny, P):
         assert np.array_equal(ref[k], got[k]), k
 
 
+def test_persistent_shots_interleaved(gpu, monkeypatch):
+    """Two shots on the persistent kernel, their run calls interleaved with
+    no wait between them (a cooperative launch each, on their own streams):
+    the launches run one after another, and each shot keeps the bits it
+    has alone."""
+    monkeypatch.setenv("FDTD2D_KERNEL", "stream")
+    monkeypatch.setenv("FDTD2D_PERSIST", "1")
+    probs = [F.Problem.from_spec(nx=nx, ny=ny, npml=P, n_steps=40, profile=1, x_lo=nx // 3, x_hi=nx - 3,
+                                 ne_peak=2e19, nu=3e9, src_i=P + 5, src_j=ny // 2, det_i=P + 9, det_j=ny // 2,
+                                 n_det=1, dft_freq=40e9)
+             for nx, ny, P in ((520, 300, 11), (700, 257, 16))]
+
+    def result(shot):
+        out = {w: shot.read_field(w) for w in FIELDS}
+        out["dft"] = shot.dft()
+        return out
+
+    alone = []
+    for p in probs:
+        with F.Shot(p, gpu) as shot:
+            assert shot.kernel_name() == "step_persist_kernel<0>", shot.kernel_name()
+            shot.run(1, 40)
+            alone.append(result(shot))
+    shots = [F.Shot(p, gpu) for p in probs]
+    try:
+        for a, b in ((1, 10), (11, 25), (26, 40)):
+            for shot in shots:
+                shot.run(a, b)
+        for shot, ref in zip(shots, alone):
+            got = result(shot)
+            for k in ref:
+                assert np.array_equal(ref[k], got[k]), k
+    finally:
+        for shot in shots:
+            shot.close()
+
+
 def test_two_step_fields_written_between_runs(gpu, monkeypatch):
     """Fields and psi written between run calls reach every buffer the
     two-step path rotates through: runs of 9, then a write, then 6 and 2
