@@ -567,7 +567,8 @@ constexpr int kPersistSteps = 4096;
 std::mutex g_persist_mu;
 cudaEvent_t g_persist_last[64] = {};
 
-cudaError_t launch_persist_ordered(fdtd2d_ctx* c, int32_t n, int32_t m, const PersistAux& A) {
+cudaError_t launch_persist_ordered(fdtd2d_ctx* c, const DevShot& t, int32_t n, int32_t m, int repeat,
+                                   const PersistAux& A) {
   if (c->device < 0 || c->device >= 64) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(g_persist_mu);
   cudaEvent_t& last = g_persist_last[c->device];
@@ -578,7 +579,7 @@ cudaError_t launch_persist_ordered(fdtd2d_ctx* c, int32_t n, int32_t m, const Pe
     e = cudaStreamWaitEvent(c->stream, last, 0);
   }
   if (e == cudaSuccess)
-    e = launch_step_persist(c->h, c->d_punits, c->n_punits, n, m, 0, A, c->medium, c->persist_ctas, c->d_bar,
+    e = launch_step_persist(t, c->d_punits, c->n_punits, n, m, repeat, A, c->medium, c->persist_ctas, c->d_bar,
                             c->d_err, c->stream);
   if (e == cudaSuccess) e = cudaEventRecord(last, c->stream);
   return e;
@@ -641,13 +642,9 @@ int setup_persist(fdtd2d_ctx* c, int device) {
       path /= 3;
     }
     const PersistAux none{};
-    if (e == cudaSuccess)
-      e = launch_step_persist(t, c->d_punits, c->n_punits, n1, n1, 4, none, c->medium, ctas, c->d_bar, c->d_err,
-                              c->stream);
+    if (e == cudaSuccess) e = launch_persist_ordered(c, t, n1, n1, 4, none);
     if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
-    if (e == cudaSuccess)
-      e = launch_step_persist(t, c->d_punits, c->n_punits, n1, n1, 16, none, c->medium, ctas, c->d_bar, c->d_err,
-                              c->stream);
+    if (e == cudaSuccess) e = launch_persist_ordered(c, t, n1, n1, 16, none);
     if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
     if (e == cudaSuccess) e = cudaEventSynchronize(e1);
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
@@ -1393,7 +1390,7 @@ int fdtd2d_run(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
     for (int32_t n = n_first; n <= n_last;) {
       const int32_t m = (int32_t)std::min<int64_t>(n_last, (int64_t)n + kPersistSteps - 1);
       cudaEvent_t p0 = prof_mark(c, nullptr, 0, m - n + 1);
-      const cudaError_t e = launch_persist_ordered(c, n, m, A);
+      const cudaError_t e = launch_persist_ordered(c, c->h, n, m, 0, A);
       if (p0) prof_mark(c, p0, (int64_t)c->nx * c->ny, m - n + 1);
       if (e != cudaSuccess) return fail_cuda(c, e);
       ++c->launches;
