@@ -356,6 +356,29 @@ struct Maps {
   void cube(int I, int J, int t) { face(I, J, t, 'z'); }
 };
 
+// The level of every sampled point (i, j) = (si*a, sj*b), i < nx - 1,
+// j < ny - 1, evaluated in parallel (the pow/sqrt work); the callers then
+// write the maps serially in the reference's loop order, so overlapping
+// writes resolve as there.
+template <class Level>
+std::vector<int> sample_levels(int nx, int ny, int si, int sj, const Level& level) {
+  const int ni = (nx - 1 + si - 1) / si, nj = (ny - 1 + sj - 1) / sj;
+  std::vector<int> v((size_t)std::max(ni, 0) * std::max(nj, 0));
+#pragma omp parallel for schedule(static)
+  for (int a = 0; a < ni; ++a)
+    for (int b = 0; b < nj; ++b) v[(size_t)a * nj + b] = level(a * si, b * sj);
+  return v;
+}
+
+// One pass of sampled faces in the reference's order: apply(i, j, level).
+template <class Level, class Apply>
+void face_pass(const Maps& M, int si, int sj, const Level& level, const Apply& apply) {
+  const std::vector<int> v = sample_levels(M.nx, M.ny, si, sj, level);
+  const int nj = (M.ny - 1 + sj - 1) / sj;
+  for (int i = 0, a = 0; i < M.nx - 1; i += si, ++a)
+    for (int j = 0, b = 0; j < M.ny - 1; j += sj, ++b) apply(i, j, v[(size_t)a * nj + b]);
+}
+
 // buildSphericalMedium, equation type 2 (FDTD_cuda.cu:3114-3209).  The
 // reference evaluates with its global k = 0 against MediumCen.K = 1.
 void sphere_medium(const IniParams& p, Maps& M) {
@@ -368,21 +391,9 @@ void sphere_medium(const IniParams& p, Maps& M) {
         ((p.sph_n * std::pow((float)k - p.med_k, 2)) / std::pow((float)p.sph_c, 2)));
     return (int)((kMCoef * std::pow((1 - std::pow(((chis) / ra), alpha)), beta)) + 8);
   };
-  for (int i = 0; i < M.nx - 1; i += 1)
-    for (int j = 0; j < M.ny - 1; j += 2) {
-      const int m = level(i, j);
-      if (m >= 8) M.face(i, j, m, 'x');
-    }
-  for (int i = 0; i < M.nx - 1; i += 2)
-    for (int j = 0; j < M.ny - 1; j += 1) {
-      const int m = level(i, j);
-      if (m >= 8) M.face(i, j, m, 'y');
-    }
-  for (int i = 0; i < M.nx - 1; i += 2)
-    for (int j = 0; j < M.ny - 1; j += 2) {
-      const int m = level(i, j);
-      if (m >= 8) M.face(i, j, m, 'z');
-    }
+  face_pass(M, 1, 2, level, [&](int i, int j, int m) { if (m >= 8) M.face(i, j, m, 'x'); });
+  face_pass(M, 2, 1, level, [&](int i, int j, int m) { if (m >= 8) M.face(i, j, m, 'y'); });
+  face_pass(M, 2, 2, level, [&](int i, int j, int m) { if (m >= 8) M.face(i, j, m, 'z'); });
 }
 
 // buildSphericalMediumFluc, equation type 2 (FDTD_cuda.cu:3211-3311).
@@ -410,21 +421,10 @@ void fluc_medium(const IniParams& p, const std::vector<float>& pne, Maps& M) {
                                         ((p.fluc_n * std::pow((float)k_, 2)) / std::pow((float)p.fluc_c, 2)));
     return (int)std::floor(ne0 * std::pow((1 - std::pow(((chis) / ra), alpha)), beta));
   };
-  for (int i = 0; i < M.nx - 1; i += 1)
-    for (int j = 0; j < M.ny - 1; j += 2) {
-      const int m = level(i, j);
-      if (m >= 0) M.add_face(i, j, p.fluc_sign * m, 'x');
-    }
-  for (int i = 0; i < M.nx - 1; i += 2)
-    for (int j = 0; j < M.ny - 1; j += 1) {
-      const int m = level(i, j);
-      if (m >= 0) M.add_face(i, j, p.fluc_sign * m, 'y');
-    }
-  for (int i = 0; i < M.nx - 1; i += 2)
-    for (int j = 0; j < M.ny - 1; j += 2) {
-      const int m = level(i, j);
-      if (m >= 0) M.add_face(i, j, p.fluc_sign * m, 'z');
-    }
+  const int sg = p.fluc_sign;
+  face_pass(M, 1, 2, level, [&](int i, int j, int m) { if (m >= 0) M.add_face(i, j, sg * m, 'x'); });
+  face_pass(M, 2, 1, level, [&](int i, int j, int m) { if (m >= 0) M.add_face(i, j, sg * m, 'y'); });
+  face_pass(M, 2, 2, level, [&](int i, int j, int m) { if (m >= 0) M.add_face(i, j, sg * m, 'z'); });
 }
 
 // buildTorusMedium, equation type 2 (FDTD_cuda.cu:3314-3378); M_PI is the
@@ -435,23 +435,21 @@ void torus_medium(const IniParams& p, Maps& M) {
   const int ne0 = kMCoef;
   const float nea = 8, alpha = (float)p.eq_alpha, beta = (float)p.eq_beta, a = (float)p.eq_r;
   const float kk = 1;
-  for (int i = 0; i < M.nx - 1; i++) {
-    for (int j = 0; j < M.ny - 1; j++) {
-      float px = (float)(i - p.med_i), py = (float)(j - p.med_j), pz = kk - Z0;
-      float phi;
-      if (px > 0) {
-        phi = std::atan(py / px);
-      } else {
-        const int sign = (py >= 0) - (py < 0);
-        phi = (px < 0) ? (float)(std::atan(py / px) + sign * kPiMacro) : (float)(sign * (kPiMacro / 2));
-      }
-      px = px * std::cos(phi) + py * std::sin(phi) - R0;
-      pz /= kk;
-      const float r_ = std::sqrt(px * px + pz * pz);
-      const int m = (int)((ne0 - nea) * std::pow(1 - std::pow(r_ / a, alpha), beta) + nea);
-      if (m >= 8) M.cube(i, j + 1, m);
+  auto level = [&](int i, int j) {
+    float px = (float)(i - p.med_i), py = (float)(j - p.med_j), pz = kk - Z0;
+    float phi;
+    if (px > 0) {
+      phi = std::atan(py / px);
+    } else {
+      const int sign = (py >= 0) - (py < 0);
+      phi = (px < 0) ? (float)(std::atan(py / px) + sign * kPiMacro) : (float)(sign * (kPiMacro / 2));
     }
-  }
+    px = px * std::cos(phi) + py * std::sin(phi) - R0;
+    pz /= kk;
+    const float r_ = std::sqrt(px * px + pz * pz);
+    return (int)((ne0 - nea) * std::pow(1 - std::pow(r_ / a, alpha), beta) + nea);
+  };
+  face_pass(M, 1, 1, level, [&](int i, int j, int m) { if (m >= 8) M.cube(i, j + 1, m); });
 }
 
 // buildPlateMedium (FDTD_cuda.cu:3079-3111): steel (material 5) from WallPos up.

@@ -255,3 +255,33 @@ def test_plasma_map_pinned():
         p = F.Problem.from_spec(F.production_spec(n_steps=10, **kw))
         ne = p.array("ne", p.nx * p.ny, np.float32)
         assert hashlib.sha256(ne.tobytes()).hexdigest()[:32] == digest, (nx, ny, prof)
+
+
+def test_ini_medium_maps_pinned():
+    """The Settings.ini medium producers (sphere, fluctuation blob, torus,
+    plate wall) are pinned by checksum of the three material-ID maps for the
+    golden Settings.ini cases, with and without the medium: their levels are
+    evaluated in parallel and written in the reference's loop order, and must
+    give the sequential construction's maps.  Checksums taken with x86-64
+    glibc's pow, sqrt and atan."""
+    import hashlib
+    import platform
+
+    if platform.machine() not in ("x86_64", "AMD64"):
+        pytest.skip("checksums taken with x86-64 glibc")
+
+    golden = Path(__file__).resolve().parent / "golden"
+    want = {("long_rc", False): "9ca2aaf4b6bab419f053719c", ("long_rc", True): "75855919076ba96440de78fc",
+            ("s2d_sphere", False): "2073c6bd93dd0cc70de96000", ("s2d_sphere", True): "9f61f5db87599033ea2d027f",
+            ("sphere_fluc_chirp", False): "cd010246bfe51d4822ba8f1b",
+            ("sphere_fluc_chirp", True): "9f61f5db87599033ea2d027f",
+            ("tof_line", False): "049331094256b59e63a5e8f7", ("tof_line", True): "d8b443032200e143b1c49820",
+            ("torus_wall_tof", False): "869e2c00813aef741b2f7e08",
+            ("torus_wall_tof", True): "1f7b71c5a5d376d4b5b6a779"}
+    for (case, vacuum), digest in want.items():
+        p = F.Problem.from_ini(golden / case / "Settings.ini", vacuum=vacuum)
+        n = p.nx * p.ny
+        h = hashlib.sha256()
+        for k in ("id1", "id2", "id3"):
+            h.update(p.array(k, n, np.int32).tobytes())
+        assert h.hexdigest()[:24] == digest, (case, vacuum)
