@@ -172,15 +172,15 @@ __device__ __forceinline__ void h_coef(const DevShot& S, const MatH* mat_h, cons
   }
 }
 
-// New Hy at one cell (c, j) from old values, CPML included.  Used for the
-// lane-0 halo value Hy_new(i0-1, j).  Reads only the old buffers.
+// New Hy at one cell (c, j) from old values (hyo: the old Hy there), CPML
+// included.  Used for the lane-0 halo value Hy_new(i0-1, j).  Reads only the
+// old buffers.
 template <int MEDIUM, bool kCoh = false>
 __device__ float hy_cell(const DevShot& S, const MatH* mat_h, int par, int c, int j,
-                         float ez_c, float ez_c1) {
+                         float ez_c, float ez_c1, float hyo) {
   const int64_t off = (int64_t)j * S.pitch + c;
   float da, db;
   h_coef<MEDIUM>(S, mat_h, S.id2, off, da, db);
-  const float hyo = ldf1<kCoh>(field_ptr(S, kHy, par) + off);
   float h = covered<MEDIUM>(S, kCovHy, (long long)j * (S.nx - 1) + c)
                 ? upd_h(da, hyo, db, ez_c1, ez_c, S.den_hx[c]) : hyo;
   const int P = S.npml;

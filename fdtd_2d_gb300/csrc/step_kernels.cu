@@ -99,15 +99,57 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
       ldfs4<kCoh>(jzo2, jzo_p + o + pitch);
     }
 
+    // The row's other loads, issued together before its arithmetic: the
+    // warp-edge Ez (lane 31: column i0+128; lane 0: i0-1) and lane 0's old
+    // Hy(i0-1), and (uniform medium; the material form has no registers to
+    // spare) the old psi of the row's CPML strip cells.
+    constexpr bool kHoist = MEDIUM == 0;
+    const bool row_in = (j >= 1) && (j <= ny - 2);
+    float ez_edge = 0.f, hy_edge = 0.f;
+    if (lane == 31 && i0 + kCols < nx) ez_edge = ldf1<kCoh>(ezo + (int64_t)j * pitch + i0 + kCols);
+    if (lane == 0 && i0 >= 1) {
+      ez_edge = ldf1<kCoh>(ezo + (int64_t)j * pitch + i0 - 1);
+      hy_edge = ldf1<kCoh>(hyo_p + (int64_t)j * pitch + i0 - 1);
+    }
+    const bool xs_h = act && (i <= P - 2 || i + 3 >= nx - P);
+    const bool xs_e = act && row_in && (i <= P - 1 || i + 3 >= nx - P);
+    const bool ys_e = act && row_in && (j <= P - 1 || j >= ny - P);
+    float psi_h[4], psi_e[4], psi_y[4];
+    zero4(psi_h);
+    zero4(psi_e);
+    zero4(psi_y);
+    if (kHoist && xs_h) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int c = i + k;
+        int side = -1, r = 0;
+        if (c <= P - 2) { side = 0; r = c; }
+        else if (c >= nx - P && c <= nx - 2) { side = 1; r = nx - 2 - c; }
+        if (side >= 0) psi_h[k] = ldf1<kCoh>(psr + S.o_hyx + ((int64_t)side * ny + j) * P + r);
+      }
+    }
+    if (kHoist && xs_e) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int c = i + k;
+        int side = -1, r = 0;
+        if (c >= 1 && c <= P - 1) { side = 0; r = c; }
+        else if (c >= nx - P && c <= nx - 2) { side = 1; r = nx - 1 - c; }
+        if (side >= 0) psi_e[k] = ldf1<kCoh>(psr + S.o_ezx + ((int64_t)side * ny + j) * P + r);
+      }
+    }
+    if (kHoist && ys_e) {
+      const int side = (j <= P - 1) ? 0 : 1;
+      const int r = side ? (ny - 1 - j) : j;
+      ldf4<kCoh>(psi_y, psr + S.o_ezy + ((int64_t)side * P + r) * pitch + ic);
+    }
+
     // ---- H update (Dev_HxCalc/Dev_HxPML_Jdir_Calc, Dev_HyCalc/Dev_HyPML_Idir_Calc)
     float hxn[4];
     hx_row<MEDIUM, kCoh>(S, m, par, ic, j, ezc, ezn, hxo, hxn, act);
 
     float ezr_next = __shfl_down_sync(0xffffffffu, ezc[0], 1);
-    if (lane == 31) {
-      const int c = i0 + kCols;
-      ezr_next = (c < nx) ? ldf1<kCoh>(ezo + (int64_t)j * pitch + c) : 0.f;
-    }
+    if (lane == 31) ezr_next = ez_edge;
     const float ezr[4] = {ezc[1], ezc[2], ezc[3], ezr_next};
     float hyn[4];
 #pragma unroll
@@ -116,7 +158,7 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
                    ? upd_h(m.day(k), hyo[k], m.dby(k), ezr[k], ezc[k], dhx[k]) : hyo[k];
     }
     // Hy x-strip CPML (edge columns only).
-    if (act && (i <= P - 2 || i + 3 >= nx - P)) {
+    if (xs_h) {
       float pn[4];
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
@@ -128,7 +170,7 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
           const float b = S.cpml[(side ? kBhX2 : kBhX1) * P + r];
           const float cc = S.cpml[(side ? kChX2 : kChX1) * P + r];
           const int64_t po = S.o_hyx + ((int64_t)side * ny + j) * P + r;
-          pn[k] = upd_psi(b, ldf1<kCoh>(psr + po), cc, ezr[k], ezc[k]);
+          pn[k] = upd_psi(b, kHoist ? psi_h[k] : ldf1<kCoh>(psr + po), cc, ezr[k], ezc[k]);
           hyn[k] = __fmaf_rn(m.dby(k), pn[k], hyn[k]);
           psw[po] = pn[k];
         }
@@ -137,14 +179,10 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
     float hyl = __shfl_up_sync(0xffffffffu, hyn[3], 1);
     if (lane == 0) {
       hyl = 0.f;
-      if (i0 >= 1) {
-        const float ezl = ldf1<kCoh>(ezo + (int64_t)j * pitch + i0 - 1);
-        hyl = hy_cell<MEDIUM, kCoh>(S, mat_h, par, i0 - 1, j, ezl, ezc[0]);
-      }
+      if (i0 >= 1) hyl = hy_cell<MEDIUM, kCoh>(S, mat_h, par, i0 - 1, j, ez_edge, ezc[0], hy_edge);
     }
 
     // ---- Jz (Dev_JzCalc) and Ez (Dev_EzCalc) on interior cells
-    const bool row_in = (j >= 1) && (j <= ny - 2);
     const float dey = S.den_ey[j];
     const float hyl4[4] = {hyl, hyn[0], hyn[1], hyn[2]};
     float ezw4[4], jzw4[4];
@@ -163,7 +201,7 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
       ezw4[k] = e;
     }
     // Ez x-strip CPML (Dev_EzPML_Idir_Calc), then y-strip (Dev_EzPML_Jdir_Calc).
-    if (act && row_in && (i <= P - 1 || i + 3 >= nx - P)) {
+    if (xs_e) {
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         const int c = i + k;
@@ -174,26 +212,26 @@ __device__ __forceinline__ void process_unit(const DevShot& S, const MatE* mat_e
           const float b = S.cpml[(side ? kBeX2 : kBeX1) * P + r];
           const float cc = S.cpml[(side ? kCeX2 : kCeX1) * P + r];
           const int64_t po = S.o_ezx + ((int64_t)side * ny + j) * P + r;
-          const float pn = upd_psi(b, ldf1<kCoh>(psr + po), cc, hyn[k], hyl4[k]);
+          const float pn = upd_psi(b, kHoist ? psi_e[k] : ldf1<kCoh>(psr + po), cc, hyn[k], hyl4[k]);
           ezw4[k] = __fmaf_rn(m.cB(k), pn, ezw4[k]);
           psw[po] = pn;
         }
       }
     }
-    if (act && row_in && (j <= P - 1 || j >= ny - P)) {
+    if (ys_e) {
       const int side = (j <= P - 1) ? 0 : 1;
       const int r = side ? (ny - 1 - j) : j;
       const float b = S.cpml[(side ? kBeY2 : kBeY1) * P + r];
       const float cc = S.cpml[(side ? kCeY2 : kCeY1) * P + r];
       const int64_t po = S.o_ezy + ((int64_t)side * P + r) * pitch + ic;
-      float psi[4], pn[4];
-      ldf4<kCoh>(psi, psr + po);
+      if (!kHoist) ldf4<kCoh>(psi_y, psr + po);
+      float pn[4];
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         const int c = i + k;
-        pn[k] = psi[k];
+        pn[k] = psi_y[k];
         if (c >= 1 && c <= nx - 2 && covered<MEDIUM>(S, kCovEzPmlJ, (long long)(r - 1) * (nx - 2) + (c - 1))) {
-          pn[k] = upd_psi(b, psi[k], cc, hxp[k], hxn[k]);
+          pn[k] = upd_psi(b, psi_y[k], cc, hxp[k], hxn[k]);
           ezw4[k] = __fmaf_rn(m.cB(k), pn[k], ezw4[k]);
         }
       }
