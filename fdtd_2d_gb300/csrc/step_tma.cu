@@ -53,9 +53,11 @@ struct Cfg {
   static constexpr uint32_t kXOffB = kPsiOffB + 2 * kPsiBytes;
   static constexpr uint32_t kStageBytes = kXOffB + 4 * kXSlot * 4;
   static constexpr size_t kSmem = (size_t)ST * kStageBytes;
-  // CTAs per SM the launch bounds ask for: W = 1 and 2 cap registers near
-  // 128 per thread (16 and 8 CTAs; no spills), W = 8 at 128 (2 CTAs)
-  static constexpr int kMinBlocks = W == 1 ? 16 : (W == 2 ? 8 : (W <= 4 ? 4 : 2));
+  // CTAs per SM the launch bounds ask for: W = 1 at 16 CTAs (no spills),
+  // W = 2 at 10 (96 registers; 8 bytes of spills in FP32, none for 16-bit
+  // storage; measured a little faster than 8 CTAs at 128 registers), W = 8
+  // at 128 registers (2 CTAs)
+  static constexpr int kMinBlocks = W == 1 ? 16 : (W == 2 ? 10 : (W <= 4 ? 4 : 2));
   static_assert(kSegBytes % 16 == 0 && kPsiOffB % 16 == 0 && kXOffB % 16 == 0 && kStageBytes % 16 == 0,
                 "16-byte aligned stage slots");
 };
