@@ -230,10 +230,12 @@ int rc_post_write(const Problem& p, const std::vector<int>& spd, int nmax, int n
   const IniParams& A = p.ini;
   // RClineFilterPostTime (kernel.cu:3250-3270): moving average of width w
   // over samples j in (i - w/2, i + w/2], 0 < j < nMax, accumulated in FP32
-  // from the top of the window down.
+  // from the top of the window down.  Lines are independent: one thread
+  // each, every sum in the reference's order.
   std::vector<float> fl((size_t)nmax * nl, 0.f);
   const int w = A.rc_window;
   const float weight = (float)(1.0 / std::abs(w));
+#pragma omp parallel for schedule(dynamic, 1)
   for (int k = 0; k < nl; k++) {
     int wb = w / 2, we = -w / 2;
     for (int i = 0; i < nmax; i++) {
