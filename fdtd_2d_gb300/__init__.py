@@ -172,6 +172,7 @@ def _lib():
         "fdtd2d_device_count": (C.c_int, []),
         "fdtd2d_write_rc_lines": (C.c_int, [vp, _ip, C.c_int32, C.c_char_p]),
         "fdtd2d_write_tof": (C.c_int, [vp, _fp, C.c_int32, C.c_char_p]),
+        "fdtd2d_tof_width": (C.c_int32, [vp]),
         "fdtd2d_run_timed": (C.c_int, [vp, C.c_int32, C.c_int32, _fp]),
         "fdtd2d_time_step_kernel": (C.c_int, [vp, C.c_int]),
         "fdtd2d_clear_kernel_choices": (None, []),
@@ -300,9 +301,16 @@ class Problem:
         _check(_lib().fdtd2d_write_rc_lines(self._h, a.ctypes.data_as(_ip), a.shape[0], str(out_dir).encode()),
                "write_rc_lines")
 
+    @property
+    def tof_width(self) -> int:
+        """Row length of the saved line write_tof takes (SizeI in grid points)."""
+        return int(_lib().fdtd2d_tof_width(self._h))
+
     def write_tof(self, field, out_dir) -> None:
-        """Time-of-flight files from a saved Ez line field[t][i]."""
+        """Time-of-flight files from a saved Ez line field[t][i], i < tof_width."""
         a = np.ascontiguousarray(field, dtype=np.float32)
+        if a.ndim != 2 or a.shape[1] != self.tof_width:
+            raise ValueError(f"write_tof wants a [times][{self.tof_width}] array, got shape {a.shape}")
         _check(_lib().fdtd2d_write_tof(self._h, a.ctypes.data_as(_fp), a.shape[0], str(out_dir).encode()),
                "write_tof")
 

@@ -308,6 +308,11 @@ extern "C" int fdtd2d_write_rc_lines(const fdtd2d_problem* h, const int32_t* spd
   return rc_post_write(*p, rows, n_rows, nl, out_dir ? out_dir : "");
 }
 
+extern "C" int32_t fdtd2d_tof_width(const fdtd2d_problem* h) {
+  const Problem* p = problem_internal(const_cast<fdtd2d_problem*>(h));
+  return (p && p->from_ini) ? std::max(0, p->ini.p_size_i) : 0;
+}
+
 extern "C" int fdtd2d_write_tof(const fdtd2d_problem* h, const float* field, int32_t times,
                                 const char* out_dir) {
   Problem* p = problem_internal(const_cast<fdtd2d_problem*>(h));

@@ -377,12 +377,18 @@ void fdtd2d_problem_free(fdtd2d_problem *p);
    before step 1, as the reference's PspdLine) -> RC_Line.txt and
    TAU_Line.txt in out_dir (RClineFilterPostTime, CalculateRCfromPwrLines,
    CalculateTaufromPwrLines, FDTD_2D_Full/kernel.cu:3188-3270).
-   fdtd2d_write_tof: saved Ez line field[t][i] (t < times, i < SizeI) ->
-   the time-of-flight files (processing_core, FDTD_2D_Full/processing.cu:6-144).
+   fdtd2d_write_tof: saved Ez line field[t][i] (t < times, i <
+   fdtd2d_tof_width(p): the Settings.ini SizeI in grid points, SizeI / ds,
+   as the reference's proc_field[t][size_i]) -> the time-of-flight files
+   (processing_core, FDTD_2D_Full/processing.cu:6-144).  field must hold
+   times * fdtd2d_tof_width(p) floats.
    Both use the Settings.ini parameters the problem was built from.          */
 int fdtd2d_write_rc_lines(const fdtd2d_problem *p, const int32_t *spd, int32_t n_rows,
                           const char *out_dir);
 int fdtd2d_write_tof(const fdtd2d_problem *p, const float *field, int32_t times, const char *out_dir);
+/* Row length fdtd2d_write_tof reads: 0 for a problem not built from a
+   Settings.ini, or whose [Processing] line is empty. */
+int32_t fdtd2d_tof_width(const fdtd2d_problem *p);
 
 /* Whole reference program on top of this ABI: Settings.ini in, the reference's
    output files (Detect.txt, detAll.txt, detEz/Hx/Hy.txt, Ez.txt,

@@ -256,3 +256,21 @@ def test_tof_window_after_the_run(tmp_path):
         rows = np.atleast_2d(np.loadtxt(tmp_path / f))
         assert rows.shape[0] > 0, f
         assert np.all(rows[:, 1] == int(key["BeginAfter"]) - 1), f
+
+
+def test_tof_width_and_wrong_width_refused(tmp_path):
+    """fdtd2d_tof_width reports the row length fdtd2d_write_tof reads (the
+    Settings.ini SizeI in grid points, SizeI / ds); the Python call refuses
+    a field of another width instead of letting the library read past it."""
+    p, _, _ = load("tof_line")
+    ini = (GOLDEN / "tof_line" / "Settings.ini").read_text()
+    key = {ln.split("=")[0].strip(): ln.split("=")[1].split(";")[0].strip()
+           for ln in ini.splitlines() if "=" in ln and not ln.startswith(";")}
+    size = int(int(key["SizeI"]) / float(key["ds"]))
+    assert p.tof_width == size > 0
+    with pytest.raises(ValueError):
+        p.write_tof(np.zeros((10, size - 1), np.float32), tmp_path)
+    with pytest.raises(ValueError):
+        p.write_tof(np.zeros(10 * size, np.float32), tmp_path)
+    spec = F.Problem.from_spec(nx=64, ny=64, npml=6, n_steps=5)
+    assert spec.tof_width == 0
