@@ -1,0 +1,43 @@
+"""The host code under AddressSanitizer and UndefinedBehaviorSanitizer: the
+problem builders, the Settings.ini parser and medium producers, the TOF and
+wave-front post-processing, and the oracle, built from their sources with
+-fsanitize=address,undefined and driven by tests/sanitize/harness.cpp over
+edge sizes and the golden Settings.ini cases.  No GPU."""
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+CSRC = ROOT / "fdtd_2d_gb300" / "csrc"
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.mark.slow
+def test_host_code_sanitized(tmp_path):
+    if not shutil.which("g++") or not shutil.which("gcc"):
+        pytest.skip("no host compiler")
+    flags = ["-O1", "-g", "-fsanitize=address,undefined", "-fno-omit-frame-pointer", "-fopenmp",
+             "-fno-sanitize-recover=undefined"]
+    obj = tmp_path / "oracle.o"
+    r = subprocess.run(["gcc", "-std=c11", *flags, "-c", str(ROOT / "oracle" / "oracle.c"), f"-I{ROOT / 'include'}",
+                        f"-I{ROOT / 'oracle'}", "-o", str(obj)], capture_output=True, text=True)
+    if r.returncode != 0 and "sanitize" in (r.stderr or ""):
+        pytest.skip("no sanitizer runtime")
+    assert r.returncode == 0, r.stderr[-2000:]
+    exe = tmp_path / "harness"
+    r = subprocess.run(["g++", "-std=c++17", *flags, f"-I{CSRC}", str(Path(__file__).parent / "sanitize" / "harness.cpp"),
+                        str(obj), str(CSRC / "problem.cpp"), str(CSRC / "ini.cpp"), str(CSRC / "processing.cpp"),
+                        "-o", str(exe)], capture_output=True, text=True)
+    if r.returncode != 0 and ("asan" in (r.stderr or "") or "ubsan" in (r.stderr or "")):
+        pytest.skip("no sanitizer runtime")
+    assert r.returncode == 0, r.stderr[-2000:]
+    (tmp_path / "sanitize_out").mkdir()
+    inis = [str(GOLDEN / c / "Settings.ini") for c in ("sphere_fluc_chirp", "torus_wall_tof", "tof_line")]
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0", OMP_NUM_THREADS="4")
+    r = subprocess.run([str(exe), *inis], capture_output=True, text=True, cwd=tmp_path, env=env, timeout=600)
+    out = r.stdout + r.stderr
+    assert "AddressSanitizer" not in out and "runtime error" not in out, out[-4000:]
+    assert r.returncode == 0 and "SANITIZE OK" in r.stdout, out[-4000:]
