@@ -41,3 +41,33 @@ def test_host_code_sanitized(tmp_path):
     out = r.stdout + r.stderr
     assert "AddressSanitizer" not in out and "runtime error" not in out, out[-4000:]
     assert r.returncode == 0 and "SANITIZE OK" in r.stdout, out[-4000:]
+
+
+@pytest.mark.slow
+def test_driver_host_code_sanitized(tmp_path):
+    """fdtd2d_run_settings end to end under ASan/UBSan on golden Settings.ini
+    cases (wave-front lines, TOF window, torus and wall, S2D second shot),
+    with the device entry points replaced by a host stand-in
+    (tests/sanitize/driver_harness.cpp): the parsing, the run schedule and
+    every writer of the drop-in driver."""
+    if not shutil.which("g++"):
+        pytest.skip("no host compiler")
+    exe = tmp_path / "driver_harness"
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-g", "-fsanitize=address,undefined", "-fno-omit-frame-pointer",
+                        "-fno-sanitize-recover=undefined", "-fopenmp", f"-I{CSRC}",
+                        str(Path(__file__).parent / "sanitize" / "driver_harness.cpp"), str(CSRC / "driver.cpp"),
+                        str(CSRC / "problem.cpp"), str(CSRC / "ini.cpp"), str(CSRC / "processing.cpp"), "-lpthread",
+                        "-o", str(exe)], capture_output=True, text=True)
+    if r.returncode != 0 and ("asan" in (r.stderr or "") or "ubsan" in (r.stderr or "")):
+        pytest.skip("no sanitizer runtime")
+    assert r.returncode == 0, r.stderr[-2000:]
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0", OMP_NUM_THREADS="4")
+    for case in ("long_rc", "tof_line", "torus_wall_tof", "s2d_sphere"):
+        out = tmp_path / case
+        out.mkdir()
+        r = subprocess.run([str(exe), str(GOLDEN / case / "Settings.ini"), str(out)], capture_output=True, text=True,
+                           env=env, timeout=600)
+        log = r.stdout + r.stderr
+        assert "AddressSanitizer" not in log and "runtime error" not in log, (case, log[-4000:])
+        assert r.returncode == 0 and "DRIVER OK" in r.stdout, (case, log[-4000:])
+        assert (out / "Detect.txt").exists() and (out / "log.txt").exists(), case
