@@ -319,7 +319,8 @@ int fdtd2d_abi_version(void);
 typedef struct fdtd2d_problem fdtd2d_problem;   /* owns the arrays its setup points to */
 
 /* Parameterised shot (synthetic workloads): grid, CPML grading, plasma profile,
-   phased array and detectors.  Units are SI; see the design doc for each field. */
+   phased array and detectors.  Units are SI; each field's meaning is given
+   beside it. */
 typedef struct fdtd2d_spec {
     int32_t nx, ny, npml, n_steps;
     double  dx, dy;

@@ -11,7 +11,7 @@ FIELDS = (F.FIELD_EZ, F.FIELD_HX, F.FIELD_HY, F.FIELD_JZ)
 PSI_FIELDS = (F.FIELD_PSI_EZX_1, F.FIELD_PSI_EZX_2, F.FIELD_PSI_EZY_1, F.FIELD_PSI_EZY_2,
               F.FIELD_PSI_HYX_1, F.FIELD_PSI_HYX_2, F.FIELD_PSI_HXY_1, F.FIELD_PSI_HXY_2)
 
-# Field tolerance: relative L2 error against the FP64 oracle (spec 1e-5).
+# Field tolerance: relative L2 error against the FP64 oracle (the parity bound, 1e-5).
 FIELD_TOL = 1e-5
 # Detector phase tolerance (rad).
 PHASE_TOL = 1e-4
