@@ -33,6 +33,7 @@
 #include <cstring>
 #include <ctime>
 #include <string>
+#include <new>
 #include <thread>
 #include <vector>
 
@@ -223,8 +224,20 @@ void write_difference(const Traces& m, const Traces& v, double dt, FILE* f) {
 
 }  // namespace
 
+static int run_settings_body(const char* ini_path, const char* out_dir, int device);
+
 extern "C" int fdtd2d_run_settings(const char* ini_path, const char* out_dir, int device) {
   if (!ini_path) return FDTD2D_ERR_INVALID;
+  try {
+    return run_settings_body(ini_path, out_dir, device);
+  } catch (const std::bad_alloc&) {
+    return FDTD2D_ERR_NOMEM;
+  } catch (...) {
+    return FDTD2D_ERR_CONFIG;   // no C++ exception leaves the C ABI
+  }
+}
+
+static int run_settings_body(const char* ini_path, const char* out_dir, int device) {
   const std::string dir = out_dir ? out_dir : "";
   const auto t_start = std::chrono::steady_clock::now();
   IniParams raw;

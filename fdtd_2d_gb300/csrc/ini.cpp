@@ -309,9 +309,15 @@ void ini_to_metric(IniParams& p) {
   p.p_pos_k = (int)(p.p_pos_k / p.ds);
   p.p_size_i = (int)(p.p_size_i / p.ds);
   if (p.exp_time_key == 1) {
-    p.n_max = (int)((p.exp_time * 1e-9) / p.dt);
-    p.fronts = (int)((p.fronts_ns * 1e-9) / p.dt);
-    p.plato = (int)((p.plato_ns * 1e-9) / p.dt);
+    // a time in steps; -1 (rejected when the problem is built) when it is
+    // not finite, negative or beyond 2^28 steps
+    auto steps = [&](double ns) {
+      const double v = (ns * 1e-9) / p.dt;
+      return (std::isfinite(v) && v >= 0 && v < 268435456.0) ? (int)v : -1;
+    };
+    p.n_max = steps(p.exp_time);
+    p.fronts = steps(p.fronts_ns);
+    p.plato = steps(p.plato_ns);
     p.p_begin_after = (int)(p.p_begin_after * (1e-9 / p.dt));
     p.p_finish_at = (int)(p.p_finish_at * (1e-9 / p.dt));
   }
@@ -480,6 +486,14 @@ int build_from_ini(const IniParams& ip, Problem& p, bool objects) {
     return FDTD2D_ERR_CONFIG;
   }
   if (ip.s_di <= 0 || ip.d_di <= 0) return FDTD2D_ERR_CONFIG;
+  // Values the reference would index or allocate with out of range: array
+  // sizes below zero, and the TOF filter windows and delays (its moving
+  // average and constant-fraction search step by them).
+  if (ip.s_pi < 0 || ip.d_pi < 0 || (ip.rc_delta > 0 && ip.rc_size < 0)) return FDTD2D_ERR_CONFIG;
+  // pulse fronts and plateau in steps (the envelope table is written from them)
+  if (ip.fronts < 0 || ip.plato < 0 || ip.fronts > (1 << 28) || ip.plato > (1 << 28)) return FDTD2D_ERR_CONFIG;
+  if (ip.p_perform && (ip.p_filter_win < 1 || ip.p_sdf_win < 1 || ip.p_cf_tau < 0 || ip.p_arc_tau < 0))
+    return FDTD2D_ERR_CONFIG;
   const double dt = ip.dt;
   const double eps = eps0(), mu = mu0();
 

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <new>
 
 namespace fdtd2d {
@@ -260,14 +261,8 @@ void fdtd2d_spec_defaults(fdtd2d_spec* sp) {
   sp->record_traces = 1; sp->dft_freq = 0; sp->storage = FDTD2D_STORE_F32;
 }
 
-int fdtd2d_problem_from_spec(const fdtd2d_spec* sp, fdtd2d_problem** out) {
-  if (!sp || !out) return FDTD2D_ERR_INVALID;
-  *out = nullptr;
-  if (sp->nx < 8 || sp->ny < 8 || sp->npml < 2 || sp->n_steps < 1 || !(sp->dx > 0) || !(sp->dy > 0))
-    return FDTD2D_ERR_INVALID;
-  if (sp->n_elem < 0 || sp->n_det < 0) return FDTD2D_ERR_INVALID;
-  fdtd2d_problem* pr = new (std::nothrow) fdtd2d_problem();
-  if (!pr) return FDTD2D_ERR_NOMEM;
+static int problem_from_spec_try(const fdtd2d_spec* sp, fdtd2d_problem** out) {
+  std::unique_ptr<fdtd2d_problem> pr(new fdtd2d_problem());
   Problem& p = pr->p;
   const int nx = sp->nx, ny = sp->ny;
   double dt = sp->dt;
@@ -343,8 +338,23 @@ int fdtd2d_problem_from_spec(const fdtd2d_spec* sp, fdtd2d_problem** out) {
   p.s.storage = sp->storage;
   p.s.field_max = sp->field_max;
   p.bind();
-  *out = pr;
+  *out = pr.release();
   return FDTD2D_OK;
+}
+
+int fdtd2d_problem_from_spec(const fdtd2d_spec* sp, fdtd2d_problem** out) {
+  if (!sp || !out) return FDTD2D_ERR_INVALID;
+  *out = nullptr;
+  if (sp->nx < 8 || sp->ny < 8 || sp->npml < 2 || sp->n_steps < 1 || !(sp->dx > 0) || !(sp->dy > 0))
+    return FDTD2D_ERR_INVALID;
+  if (sp->n_elem < 0 || sp->n_det < 0) return FDTD2D_ERR_INVALID;
+  try {
+    return problem_from_spec_try(sp, out);
+  } catch (const std::bad_alloc&) {
+    return FDTD2D_ERR_NOMEM;
+  } catch (...) {
+    return FDTD2D_ERR_INVALID;   // no C++ exception leaves the C ABI
+  }
 }
 
 int fdtd2d_problem_from_ini(const char* path, fdtd2d_problem** out) {
@@ -363,26 +373,31 @@ void fdtd2d_problem_free(fdtd2d_problem* p) { delete p; }
 
 namespace fdtd2d {
 
+namespace {
+int problem_from_ini_try(const char* path, bool objects, fdtd2d_problem** out) {
+  std::unique_ptr<fdtd2d_problem> pr(new fdtd2d_problem());
+  std::string log;
+  int rc = parse_ini(path, pr->p.ini, log);
+  if (rc) return rc;
+  ini_to_metric(pr->p.ini);
+  rc = build_from_ini(pr->p.ini, pr->p, objects);
+  if (rc) return rc;
+  pr->p.bind();
+  *out = pr.release();
+  return FDTD2D_OK;
+}
+}  // namespace
+
 int problem_from_ini_ex(const char* path, bool objects, fdtd2d_problem** out) {
   if (!path || !out) return FDTD2D_ERR_INVALID;
   *out = nullptr;
-  fdtd2d_problem* pr = new (std::nothrow) fdtd2d_problem();
-  if (!pr) return FDTD2D_ERR_NOMEM;
-  std::string log;
-  int rc = parse_ini(path, pr->p.ini, log);
-  if (rc) {
-    delete pr;
-    return rc;
+  try {
+    return problem_from_ini_try(path, objects, out);
+  } catch (const std::bad_alloc&) {
+    return FDTD2D_ERR_NOMEM;
+  } catch (...) {
+    return FDTD2D_ERR_CONFIG;   // no C++ exception leaves the C ABI
   }
-  ini_to_metric(pr->p.ini);
-  rc = build_from_ini(pr->p.ini, pr->p, objects);
-  if (rc) {
-    delete pr;
-    return rc;
-  }
-  pr->p.bind();
-  *out = pr;
-  return FDTD2D_OK;
 }
 
 Problem* problem_internal(fdtd2d_problem* p) { return p ? &p->p : nullptr; }

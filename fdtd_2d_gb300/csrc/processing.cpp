@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdio>
 #include <fstream>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -298,14 +299,29 @@ int rc_run_and_write(fdtd2d_ctx* ctx, const Problem& p, const std::string& dir, 
 
 using namespace fdtd2d;
 
+// No C++ exception leaves the C ABI: allocation failures become
+// FDTD2D_ERR_NOMEM, anything else FDTD2D_ERR_INVALID.
+template <class F>
+static int guarded(F&& f) {
+  try {
+    return f();
+  } catch (const std::bad_alloc&) {
+    return FDTD2D_ERR_NOMEM;
+  } catch (...) {
+    return FDTD2D_ERR_INVALID;
+  }
+}
+
 extern "C" int fdtd2d_write_rc_lines(const fdtd2d_problem* h, const int32_t* spd, int32_t n_rows,
                                      const char* out_dir) {
   Problem* p = problem_internal(const_cast<fdtd2d_problem*>(h));
   if (!p || !spd || n_rows < 1 || !p->from_ini) return FDTD2D_ERR_INVALID;
   const int nl = p->s.n_rc;
   if (nl <= 0) return FDTD2D_ERR_STATE;
-  std::vector<int> rows(spd, spd + (size_t)n_rows * nl);
-  return rc_post_write(*p, rows, n_rows, nl, out_dir ? out_dir : "");
+  return guarded([&] {
+    std::vector<int> rows(spd, spd + (size_t)n_rows * nl);
+    return rc_post_write(*p, rows, n_rows, nl, out_dir ? out_dir : "");
+  });
 }
 
 extern "C" int32_t fdtd2d_tof_width(const fdtd2d_problem* h) {
@@ -318,8 +334,10 @@ extern "C" int fdtd2d_write_tof(const fdtd2d_problem* h, const float* field, int
   Problem* p = problem_internal(const_cast<fdtd2d_problem*>(h));
   if (!p || (!field && times > 0) || times < 0 || !p->from_ini) return FDTD2D_ERR_INVALID;
   const int sz = p->ini.p_size_i;
-  std::vector<std::vector<float>> f(times, std::vector<float>(std::max(0, sz)));
-  for (int t = 0; t < times; ++t)
-    for (int i = 0; i < sz; ++i) f[t][i] = field[(size_t)t * sz + i];
-  return processing_run(*p, f, out_dir ? out_dir : "");
+  return guarded([&] {
+    std::vector<std::vector<float>> f(times, std::vector<float>(std::max(0, sz)));
+    for (int t = 0; t < times; ++t)
+      for (int i = 0; i < sz; ++i) f[t][i] = field[(size_t)t * sz + i];
+    return processing_run(*p, f, out_dir ? out_dir : "");
+  });
 }

@@ -48,9 +48,28 @@ typedef struct oracle {
     o32_state *f;
 } oracle;
 
+/* The checks fdtd2d_create makes on the grid and the point lists, so that
+   the oracle refuses what the library refuses instead of indexing outside
+   its arrays: NULL for a grid below 8 cells or one that the CPML strips do
+   not fit, or a source, detector or component detector outside the cells
+   1..nx-2 x 1..ny-2. */
+static int oracle_points_ok(const fdtd2d_point *pts, int n, const fdtd2d_setup *s) {
+    int e;
+    if (n < 0 || (n > 0 && !pts)) return 0;
+    for (e = 0; e < n; ++e)
+        if (pts[e].i < 1 || pts[e].i > s->nx - 2 || pts[e].j < 1 || pts[e].j > s->ny - 2) return 0;
+    return 1;
+}
+
 oracle *oracle_create(const fdtd2d_setup *s, int fp32) {
     oracle *o;
     if (!s) return NULL;
+    if (s->nx < 8 || s->ny < 8 || s->npml < 2 || 2 * s->npml + 2 > s->nx || 2 * s->npml + 2 > s->ny ||
+        s->n_steps < 1)
+        return NULL;
+    if (!oracle_points_ok(s->src, s->n_src, s) || !oracle_points_ok(s->det, s->n_det, s) ||
+        !oracle_points_ok(s->comp, s->n_comp, s))
+        return NULL;
     o = (oracle *)calloc(1, sizeof(*o));
     if (!o) return NULL;
     o->fp32 = fp32;

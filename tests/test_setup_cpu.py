@@ -285,3 +285,36 @@ def test_ini_medium_maps_pinned():
         for k in ("id1", "id2", "id3"):
             h.update(p.array(k, n, np.int32).tobytes())
         assert h.hexdigest()[:24] == digest, (case, vacuum)
+
+
+@pytest.mark.parametrize("edit", [
+    {"FilterWin": "-1"},                       # TOF moving average with a negative window
+    {"CFTau": "-100"},                         # constant-fraction delay below zero
+    {"SIsize": "-100"},                        # negative array size (a vector of negative length)
+    {"Plato_ns": "1e9"},                       # plateau beyond 2^28 steps
+    {"Fronts_ns": "-0.5"},                     # negative fronts
+])
+def test_malformed_settings_ini_is_a_config_error(tmp_path, edit):
+    """Values the reference would index or allocate with out of range (found
+    by mutating the golden Settings.ini files under AddressSanitizer) are
+    refused with FDTD2D_ERR_CONFIG instead of crashing the process."""
+    golden = Path(__file__).resolve().parent / "golden"
+    ini = (golden / "tof_line" / "Settings.ini").read_text()
+    for key, val in edit.items():
+        ini, n = re.subn(rf"(?m)^{key}\s*=.*$", f"{key} = {val}", ini)
+        assert n == 1, key
+    path = tmp_path / "Settings.ini"
+    path.write_text(ini)
+    with pytest.raises(F.FdtdError) as e:
+        F.Problem.from_ini(path)
+    assert e.value.status == F.ERR_CONFIG
+
+
+def test_oracle_refuses_points_off_the_grid():
+    """The oracle makes fdtd2d_create's range checks: a source outside the
+    cells 1..nx-2 x 1..ny-2 is refused instead of indexed."""
+    p = F.Problem.from_spec(nx=64, ny=64, npml=6, n_steps=5, src_i=80, src_j=30, det_i=20, det_j=30)
+    with pytest.raises(RuntimeError):
+        O.Oracle(p.setup_ptr)
+    ok = F.Problem.from_spec(nx=64, ny=64, npml=6, n_steps=5, src_i=20, src_j=30, det_i=22, det_j=30)
+    O.Oracle(ok.setup_ptr)
