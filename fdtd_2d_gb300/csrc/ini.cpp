@@ -17,6 +17,7 @@
 // integer truncations and FP32 storage.
 #include <algorithm>
 #include <cctype>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -153,6 +154,13 @@ class Ini {
 
 inline double f32(double x) { return (double)(float)x; }
 
+// A double to int as the reference's x86 build converts it (cvttsd2si): the
+// value truncated toward zero when it fits an int, else INT_MIN (NaN, the
+// infinities and out-of-range values alike).  C++ leaves those cases
+// undefined and Arm saturates them; degenerate Settings.ini values (a zero
+// radius, a fractional power of a negative base) reach them.
+inline int x86_int(double v) { return (v > -2147483649.0 && v < 2147483648.0) ? (int)v : INT_MIN; }
+
 }  // namespace
 
 int parse_ini(const char* path, IniParams& p, std::string& log) {
@@ -281,33 +289,33 @@ void ini_to_metric(IniParams& p) {
   p.dx = p.ds * 1E-3;
   p.dy = p.ds * 1E-3;
   p.dz = p.ds * 1E-3;
-  p.imax = (int)(p.imax * inv);
-  p.jmax = (int)(p.jmax * inv);
-  p.src_i = (int)(p.src_i * inv);
-  p.src_j = (int)(p.src_j * inv);
-  p.det_i = (int)(p.det_i * inv);
-  p.det_j = (int)(p.det_j * inv);
-  p.med_i = (int)(p.med_i * inv);
-  p.med_j = (int)(p.med_j * inv);
+  p.imax = x86_int(p.imax * inv);
+  p.jmax = x86_int(p.jmax * inv);
+  p.src_i = x86_int(p.src_i * inv);
+  p.src_j = x86_int(p.src_j * inv);
+  p.det_i = x86_int(p.det_i * inv);
+  p.det_j = x86_int(p.det_j * inv);
+  p.med_i = x86_int(p.med_i * inv);
+  p.med_j = x86_int(p.med_j * inv);
   p.med_k = 1;
-  p.eq_r = (int)(p.eq_r * inv);
-  p.s_pi = (int)(p.s_pi * inv);
-  p.s_di = (int)(p.s_di * inv);
-  p.d_pi = (int)(p.d_pi * inv);
-  p.d_di = (int)(p.d_di * inv);
-  p.fluc_i = (int)(p.fluc_i * inv);
-  p.fluc_j = (int)(p.fluc_j * inv);
+  p.eq_r = x86_int(p.eq_r * inv);
+  p.s_pi = x86_int(p.s_pi * inv);
+  p.s_di = x86_int(p.s_di * inv);
+  p.d_pi = x86_int(p.d_pi * inv);
+  p.d_di = x86_int(p.d_di * inv);
+  p.fluc_i = x86_int(p.fluc_i * inv);
+  p.fluc_j = x86_int(p.fluc_j * inv);
   p.fluc_k = 1;
-  p.fluc_r = (int)(p.fluc_r * inv);
+  p.fluc_r = x86_int(p.fluc_r * inv);
   p.dt = (0.99 / (kC0 * std::sqrt(1.0 / (p.dx * p.dx) + 1.0 / (p.dy * p.dy) + 1.0 / (p.dz * p.dz)))) *
          p.dt_coef;
-  p.rc_i = (int)(p.rc_i / p.ds);
-  p.rc_size = (int)(p.rc_size / p.ds);
-  p.rc_delta = (int)(p.rc_delta / p.ds);
-  p.p_pos_i = (int)(p.p_pos_i / p.ds);
-  p.p_pos_j = (int)(p.p_pos_j / p.ds);
-  p.p_pos_k = (int)(p.p_pos_k / p.ds);
-  p.p_size_i = (int)(p.p_size_i / p.ds);
+  p.rc_i = x86_int(p.rc_i / p.ds);
+  p.rc_size = x86_int(p.rc_size / p.ds);
+  p.rc_delta = x86_int(p.rc_delta / p.ds);
+  p.p_pos_i = x86_int(p.p_pos_i / p.ds);
+  p.p_pos_j = x86_int(p.p_pos_j / p.ds);
+  p.p_pos_k = x86_int(p.p_pos_k / p.ds);
+  p.p_size_i = x86_int(p.p_size_i / p.ds);
   if (p.exp_time_key == 1) {
     // a time in steps; -1 (rejected when the problem is built) when it is
     // not finite, negative or beyond 2^28 steps
@@ -318,8 +326,8 @@ void ini_to_metric(IniParams& p) {
     p.n_max = steps(p.exp_time);
     p.fronts = steps(p.fronts_ns);
     p.plato = steps(p.plato_ns);
-    p.p_begin_after = (int)(p.p_begin_after * (1e-9 / p.dt));
-    p.p_finish_at = (int)(p.p_finish_at * (1e-9 / p.dt));
+    p.p_begin_after = x86_int(p.p_begin_after * (1e-9 / p.dt));
+    p.p_finish_at = x86_int(p.p_finish_at * (1e-9 / p.dt));
   }
 }
 
@@ -395,7 +403,7 @@ void sphere_medium(const IniParams& p, Maps& M) {
         ((p.sph_p * std::pow((float)i - p.med_i, 2)) / std::pow((float)p.sph_a, 2)) +
         ((p.sph_q * std::pow((float)j - p.med_j, 2)) / std::pow((float)p.sph_b, 2)) +
         ((p.sph_n * std::pow((float)k - p.med_k, 2)) / std::pow((float)p.sph_c, 2)));
-    return (int)((kMCoef * std::pow((1 - std::pow(((chis) / ra), alpha)), beta)) + 8);
+    return x86_int((kMCoef * std::pow((1 - std::pow(((chis) / ra), alpha)), beta)) + 8);
   };
   face_pass(M, 1, 2, level, [&](int i, int j, int m) { if (m >= 8) M.face(i, j, m, 'x'); });
   face_pass(M, 2, 1, level, [&](int i, int j, int m) { if (m >= 8) M.face(i, j, m, 'y'); });
@@ -414,18 +422,18 @@ void fluc_medium(const IniParams& p, const std::vector<float>& pne, Maps& M) {
   const float ra = (float)p.fluc_r, alpha = (float)p.fluc_alpha, beta = (float)p.fluc_beta;
   const int Ic = p.fluc_i, Jc = p.fluc_j, Kc = p.fluc_k;
   auto level = [&](int i, int j) {
-    const int i_ = (int)((k - Kc) * std::sin(ay) + (i - Ic) * std::cos(ay) * std::cos(az) -
+    const int i_ = x86_int((k - Kc) * std::sin(ay) + (i - Ic) * std::cos(ay) * std::cos(az) -
                          (j - Jc) * std::cos(ay) * std::sin(az));
-    const int j_ = (int)((i - Ic) * (std::cos(ax) * std::sin(az) + std::cos(az) * std::sin(ax) * std::sin(ay)) +
+    const int j_ = x86_int((i - Ic) * (std::cos(ax) * std::sin(az) + std::cos(az) * std::sin(ax) * std::sin(ay)) +
                          (j - Jc) * (std::cos(ax) * std::cos(az) - std::sin(ax) * std::sin(ay) * std::sin(az)) -
                          (k - Kc) * std::cos(ay) * std::sin(ax));
-    const int k_ = (int)((i - Ic) * (std::sin(ax) * std::sin(az) - std::cos(ax) * std::cos(az) * std::sin(ay)) +
+    const int k_ = x86_int((i - Ic) * (std::sin(ax) * std::sin(az) - std::cos(ax) * std::cos(az) * std::sin(ay)) +
                          (j - Jc) * (std::cos(az) * std::sin(ax) + std::cos(ax) * std::sin(ay) * std::sin(az)) +
                          (k - Kc) * std::cos(ax) * std::cos(ay));
     const float chis = (float)std::sqrt(((p.fluc_p * std::pow((float)i_, 2)) / std::pow((float)p.fluc_a, 2)) +
                                         ((p.fluc_q * std::pow((float)j_, 2)) / std::pow((float)p.fluc_b, 2)) +
                                         ((p.fluc_n * std::pow((float)k_, 2)) / std::pow((float)p.fluc_c, 2)));
-    return (int)std::floor(ne0 * std::pow((1 - std::pow(((chis) / ra), alpha)), beta));
+    return x86_int(std::floor(ne0 * std::pow((1 - std::pow(((chis) / ra), alpha)), beta)));
   };
   const int sg = p.fluc_sign;
   face_pass(M, 1, 2, level, [&](int i, int j, int m) { if (m >= 0) M.add_face(i, j, sg * m, 'x'); });
@@ -453,7 +461,7 @@ void torus_medium(const IniParams& p, Maps& M) {
     px = px * std::cos(phi) + py * std::sin(phi) - R0;
     pz /= kk;
     const float r_ = std::sqrt(px * px + pz * pz);
-    return (int)((ne0 - nea) * std::pow(1 - std::pow(r_ / a, alpha), beta) + nea);
+    return x86_int((ne0 - nea) * std::pow(1 - std::pow(r_ / a, alpha), beta) + nea);
   };
   face_pass(M, 1, 1, level, [&](int i, int j, int m) { if (m >= 8) M.cube(i, j + 1, m); });
 }
@@ -477,6 +485,10 @@ std::vector<int> array_positions(int cen, int size, int d, int* count) {
 
 }  // namespace
 
+bool processing_params_ok(const IniParams& ip) {
+  return ip.p_filter_win >= 1 && ip.p_sdf_win >= 1 && ip.p_cf_tau >= 0 && ip.p_arc_tau >= 0;
+}
+
 int build_from_ini(const IniParams& ip, Problem& p, bool objects) {
   p.from_ini = true;
   const int nx = ip.imax, ny = ip.jmax, P = kPmlSize;
@@ -492,8 +504,7 @@ int build_from_ini(const IniParams& ip, Problem& p, bool objects) {
   if (ip.s_pi < 0 || ip.d_pi < 0 || (ip.rc_delta > 0 && ip.rc_size < 0)) return FDTD2D_ERR_CONFIG;
   // pulse fronts and plateau in steps (the envelope table is written from them)
   if (ip.fronts < 0 || ip.plato < 0 || ip.fronts > (1 << 28) || ip.plato > (1 << 28)) return FDTD2D_ERR_CONFIG;
-  if (ip.p_perform && (ip.p_filter_win < 1 || ip.p_sdf_win < 1 || ip.p_cf_tau < 0 || ip.p_arc_tau < 0))
-    return FDTD2D_ERR_CONFIG;
+  if (ip.p_perform && !processing_params_ok(ip)) return FDTD2D_ERR_CONFIG;
   const double dt = ip.dt;
   const double eps = eps0(), mu = mu0();
 

@@ -348,6 +348,17 @@ int fdtd2d_problem_from_spec(const fdtd2d_spec* sp, fdtd2d_problem** out) {
   if (sp->nx < 8 || sp->ny < 8 || sp->npml < 2 || sp->n_steps < 1 || !(sp->dx > 0) || !(sp->dy > 0))
     return FDTD2D_ERR_INVALID;
   if (sp->n_elem < 0 || sp->n_det < 0) return FDTD2D_ERR_INVALID;
+  // every real parameter finite, and the random field's correlation length
+  // positive and within a few grid sizes (its kernel spans 4 half-lengths)
+  const double reals[] = {sp->dx, sp->dy, sp->courant, sp->dt, sp->cpml_m, sp->cpml_ma, sp->sigma_factor,
+                          sp->kappa_max, sp->alpha_max, sp->ne_peak, sp->x_lo, sp->x_hi, sp->x_center,
+                          sp->width, sp->grf_rms, sp->grf_corr, sp->nu, sp->freq, sp->steer_deg, sp->amp,
+                          sp->pulse_width, sp->pulse_t0, sp->dft_freq, sp->field_max};
+  for (const double v : reals)
+    if (!std::isfinite(v)) return FDTD2D_ERR_INVALID;
+  if (sp->profile == 3 && sp->grf_rms != 0 &&
+      !(sp->grf_corr > 0 && sp->grf_corr <= 4.0 * std::max(sp->nx, sp->ny)))
+    return FDTD2D_ERR_INVALID;
   try {
     return problem_from_spec_try(sp, out);
   } catch (const std::bad_alloc&) {

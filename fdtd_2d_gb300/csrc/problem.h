@@ -104,6 +104,9 @@ int parse_ini(const char* path, IniParams& ip, std::string& log);
 void ini_to_metric(IniParams& ip);
 // objects = false is the SourceToDetect vacuum run: no medium, no fluctuation
 // (buildObject with ObjectsEnable == false, FDTD_2D_Full/FDTD_cuda.cu:2602-2625).
+// The TOF processing's windows and delays are usable: filter windows of at
+// least one sample, delays not negative.
+bool processing_params_ok(const IniParams& ip);
 int build_from_ini(const IniParams& ip, Problem& p, bool objects = true);
 
 // fdtd2d_problem_from_ini with the objects switch of build_from_ini.

@@ -333,6 +333,7 @@ extern "C" int fdtd2d_write_tof(const fdtd2d_problem* h, const float* field, int
                                 const char* out_dir) {
   Problem* p = problem_internal(const_cast<fdtd2d_problem*>(h));
   if (!p || (!field && times > 0) || times < 0 || !p->from_ini) return FDTD2D_ERR_INVALID;
+  if (!processing_params_ok(p->ini)) return FDTD2D_ERR_CONFIG;
   const int sz = p->ini.p_size_i;
   return guarded([&] {
     std::vector<std::vector<float>> f(times, std::vector<float>(std::max(0, sz)));

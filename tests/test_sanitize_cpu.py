@@ -4,6 +4,7 @@ wave-front post-processing, and the oracle, built from their sources with
 -fsanitize=address,undefined and driven by tests/sanitize/harness.cpp over
 edge sizes and the golden Settings.ini cases.  No GPU."""
 import os
+import re
 import shutil
 import subprocess
 from pathlib import Path
@@ -19,8 +20,8 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 def test_host_code_sanitized(tmp_path):
     if not shutil.which("g++") or not shutil.which("gcc"):
         pytest.skip("no host compiler")
-    flags = ["-O1", "-g", "-fsanitize=address,undefined", "-fno-omit-frame-pointer", "-fopenmp",
-             "-fno-sanitize-recover=undefined"]
+    flags = ["-O1", "-g", "-fsanitize=address,undefined,float-cast-overflow", "-fno-omit-frame-pointer", "-fopenmp",
+             "-fno-sanitize-recover=undefined,float-cast-overflow"]
     obj = tmp_path / "oracle.o"
     r = subprocess.run(["gcc", "-std=c11", *flags, "-c", str(ROOT / "oracle" / "oracle.c"), f"-I{ROOT / 'include'}",
                         f"-I{ROOT / 'oracle'}", "-o", str(obj)], capture_output=True, text=True)
@@ -36,6 +37,18 @@ def test_host_code_sanitized(tmp_path):
     assert r.returncode == 0, r.stderr[-2000:]
     (tmp_path / "sanitize_out").mkdir()
     inis = [str(GOLDEN / c / "Settings.ini") for c in ("sphere_fluc_chirp", "torus_wall_tof", "tof_line")]
+    # degenerate files: a sphere semi-axis of 0 (an infinite level, converted
+    # as the reference's x86 build converts it) and a zero TOF window with the
+    # processing switch commented out (refused by fdtd2d_write_tof)
+    for name, case, edits in (("zero_axis.ini", "sphere_fluc_chirp", {"A": "0"}),
+                              ("zero_window.ini", "tof_line", {"FilterWin": "0", "Perform": None})):
+        text = (GOLDEN / case / "Settings.ini").read_text()
+        for key, val in edits.items():
+            repl = f";{key} = 1" if val is None else f"{key} = {val}"
+            text, n = re.subn(rf"(?m)^{key}\s*=.*$", repl, text)
+            assert n == 1, (name, key)
+        (tmp_path / name).write_text(text)
+        inis.append(str(tmp_path / name))
     env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0", OMP_NUM_THREADS="4")
     r = subprocess.run([str(exe), *inis], capture_output=True, text=True, cwd=tmp_path, env=env, timeout=600)
     out = r.stdout + r.stderr

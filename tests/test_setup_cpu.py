@@ -318,3 +318,19 @@ def test_oracle_refuses_points_off_the_grid():
         O.Oracle(p.setup_ptr)
     ok = F.Problem.from_spec(nx=64, ny=64, npml=6, n_steps=5, src_i=20, src_j=30, det_i=22, det_j=30)
     O.Oracle(ok.setup_ptr)
+
+
+def test_tof_processing_refuses_a_zero_window(tmp_path):
+    """With the processing switch off the file loads, but the standalone TOF
+    call still checks its windows: FilterWin = 0 is a configuration error,
+    not a moving average over minus one samples."""
+    golden = Path(__file__).resolve().parent / "golden"
+    ini = (golden / "tof_line" / "Settings.ini").read_text()
+    ini = re.sub(r"(?m)^FilterWin\s*=.*$", "FilterWin = 0", ini)
+    ini = re.sub(r"(?m)^Perform\s*=.*$", ";Perform = 1", ini)
+    path = tmp_path / "Settings.ini"
+    path.write_text(ini)
+    p = F.Problem.from_ini(path)
+    with pytest.raises(F.FdtdError) as e:
+        p.write_tof(np.zeros((4, p.tof_width), np.float32), tmp_path)
+    assert e.value.status == F.ERR_CONFIG
