@@ -321,7 +321,7 @@ int64_t fdtd2d_device_bytes(const fdtd2d_setup* s) {
 }
 
 int fdtd2d_create(const fdtd2d_setup* s, int device, fdtd2d_ctx** out) {
-  return fdtd2d::create_ctx(s, device, false, out);
+  return abi_guard([&] { return fdtd2d::create_ctx(s, device, false, out); });
 }
 
 }  // extern "C"

@@ -324,7 +324,14 @@ int fdtd2d_batch_create(int device, int64_t hbm_budget_bytes, fdtd2d_batch** out
   return FDTD2D_OK;
 }
 
+static int fdtd2d_batch_add_body(fdtd2d_batch* b, const fdtd2d_setup* s, int32_t* shot);
+
+// The entry point: its body, below, runs behind abi_guard.
 int fdtd2d_batch_add(fdtd2d_batch* b, const fdtd2d_setup* s, int32_t* shot) {
+  return abi_guard([&] { return fdtd2d_batch_add_body(b, s, shot); });
+}
+
+static int fdtd2d_batch_add_body(fdtd2d_batch* b, const fdtd2d_setup* s, int32_t* shot) {
   if (!b || !s || !shot) return FDTD2D_ERR_INVALID;
   *shot = -1;
   if (s->medium != FDTD2D_MEDIUM_UNIFORM || s->npml > tma_max_pml() || s->n_rc > 0 || s->line_n > 0 ||
@@ -373,7 +380,14 @@ int fdtd2d_batch_add(fdtd2d_batch* b, const fdtd2d_setup* s, int32_t* shot) {
   return FDTD2D_OK;
 }
 
+static int fdtd2d_batch_run_body(fdtd2d_batch* b, int32_t n_steps);
+
+// The entry point: its body, below, runs behind abi_guard.
 int fdtd2d_batch_run(fdtd2d_batch* b, int32_t n_steps) {
+  return abi_guard([&] { return fdtd2d_batch_run_body(b, n_steps); });
+}
+
+static int fdtd2d_batch_run_body(fdtd2d_batch* b, int32_t n_steps) {
   if (!b || n_steps < 0) return FDTD2D_ERR_INVALID;
   cudaSetDevice(b->device);
   if (n_steps > 0) {
@@ -620,7 +634,14 @@ int fdtd2d_server_create(int device, int64_t hbm_budget_bytes, int32_t block_ste
   return FDTD2D_OK;
 }
 
+static int fdtd2d_server_submit_body(fdtd2d_server* s, const fdtd2d_setup* setup, int64_t tag);
+
+// The entry point: its body, below, runs behind abi_guard.
 int fdtd2d_server_submit(fdtd2d_server* s, const fdtd2d_setup* setup, int64_t tag) {
+  return abi_guard([&] { return fdtd2d_server_submit_body(s, setup, tag); });
+}
+
+static int fdtd2d_server_submit_body(fdtd2d_server* s, const fdtd2d_setup* setup, int64_t tag) {
   if (!s || !setup) return FDTD2D_ERR_INVALID;
   if (setup->medium != FDTD2D_MEDIUM_UNIFORM || setup->npml > tma_max_pml() || setup->n_rc > 0 ||
       setup->line_n > 0 || setup->storage != FDTD2D_STORE_F32)
@@ -632,7 +653,14 @@ int fdtd2d_server_submit(fdtd2d_server* s, const fdtd2d_setup* setup, int64_t ta
   return FDTD2D_OK;
 }
 
+static int fdtd2d_server_step_body(fdtd2d_server* s);
+
+// The entry point: its body, below, runs behind abi_guard.
 int fdtd2d_server_step(fdtd2d_server* s) {
+  return abi_guard([&] { return fdtd2d_server_step_body(s); });
+}
+
+static int fdtd2d_server_step_body(fdtd2d_server* s) {
   if (!s) return FDTD2D_ERR_INVALID;
   fdtd2d_batch* b = s->b;
   cudaSetDevice(b->device);

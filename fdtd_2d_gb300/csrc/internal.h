@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cstdint>
+#include <new>
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -161,6 +162,20 @@ int persist_resident_ctas(int medium, int device);
 
 // Device error codes written by kernels with bounded waits.
 enum DeviceError : int { kErrNone = 0, kErrWaitTimeout = 1 };
+
+// Runs the body of a C-ABI entry point so that no C++ exception crosses the
+// ABI: a host allocation failure becomes FDTD2D_ERR_NOMEM (-2), anything
+// else FDTD2D_ERR_INVALID (-1).
+template <class F>
+int abi_guard(F&& f) noexcept {
+  try {
+    return f();
+  } catch (const std::bad_alloc&) {
+    return -2;
+  } catch (...) {
+    return -1;
+  }
+}
 
 // Shared-memory staged step (step_tma.cu), uniform medium: one CTA per unit
 // of a band of columns.  Compiled launch shapes (warps per CTA, ring stages)
