@@ -386,10 +386,12 @@ def run_serving(args, local: int, capacity: float) -> dict:
 
 def run_precision(args, local: int) -> dict:
     """Reduced field storage on the production shot: F16 (per-array 2^k
-    scales) and BF16 storage, FP32 arithmetic, FP64 DFT.  Throughput is
-    device-timed like `value`; errors are against the FP32 GPU run of the same
-    shot after --prec-steps steps, and against the FP64 oracle on a small
-    shot of the same physics (384 x 320, 8 elements, 1500 steps)."""
+    scales) and BF16 storage, FP32 arithmetic, FP64 DFT.  Errors are against
+    the FP32 GPU run of the same shot over --prec-steps time steps (default
+    20000: the whole shot), and against the FP64 oracle on a small shot of the
+    same physics (384 x 320, 8 elements, 1500 steps).  Throughput is
+    device-timed like `value`; the interior kernel's rate is its launches'
+    bytes over their event-timed duration."""
     import fdtd_2d_gb300 as F
     import oracle as O
 
@@ -400,29 +402,49 @@ def run_precision(args, local: int) -> dict:
         return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-300))
 
     out = {}
-    S, K, W = args.block, max(3, args.steps // 3), args.warmup
+    S, K = args.block, max(3, args.steps // 3)
     n_err = args.prec_steps
+    peak = measured_peaks().get("hbm_gbs") or 6800.0
     ref32 = None
     for name, store in (("f32", F.STORE_F32), ("f16", F.STORE_F16), ("bf16", F.STORE_BF16)):
-        prob = make_problem(max(20000, (W + K) * S, n_err), args.size, storage=store)
+        prob = make_problem(n_err + K * S, args.size, storage=store)
         cells = prob.nx * prob.ny
         with F.Shot(prob, local) as shot:
+            t = time.perf_counter()
             shot.run(1, n_err)
+            shot.synchronize()
+            wall = time.perf_counter() - t
             ez = shot.read_field("ez").astype(np.float64)
             tr = shot.traces(1, n_err)["det_ez"].astype(np.float64)
             dft = shot.dft()
-            entry = {"kernel": shot.kernel_name()}
+            entry = {"kernel": shot.kernel_name(), "shot_seconds": wall}
             if store != F.STORE_F32:
+                shot.time_step_kernel(True)
                 ms = shot.run_timed(n_err + 1, n_err + K * S)
-                bpc = 18
+                kt = shot.step_kernel_time()
+                shot.time_step_kernel(False)
                 val = cells * K * S / (ms / 1e3) / 1e9
-                entry.update({"value": val, "unit": UNIT, "bytes_per_cell_update": bpc,
-                              "achieved_gbs": bpc * val, "ok_finite": shot.check_finite()})
+                two = kt["steps"] == 2
+                # 16-bit Ez, Hx, Hy, Jz read and written and the drive read once
+                # per launch: 18 B per cell of the launch's region, for the one
+                # or two time steps the launch advances
+                per_launch = kt["ms"] / 1e3 / max(kt["launches"], 1)
+                kgbs = 18 * kt["cells"] / per_launch / 1e9
+                entry.update({"value": val, "unit": UNIT, "bytes_per_cell_update": 9 if two else 18,
+                              "step_rate_gbs": (9 if two else 18) * val,
+                              "interior_kernel": {"achieved_gbs": kgbs, "frac": kgbs / peak,
+                                                  "bytes_per_cell_per_launch": 18, "steps_per_launch": kt["steps"],
+                                                  "mean_launch_us": per_launch * 1e6},
+                              "ok_finite": shot.check_finite()})
         if store == F.STORE_F32:
             ref32 = (ez, tr, dft)
+            out["f32"] = entry
             continue
+        perr = phase_err(dft, ref32[2])
         entry.update({"ez_rel_l2_vs_f32": rel(ez, ref32[0]), "trace_rel_l2_vs_f32": rel(tr, ref32[1]),
-                      "dft_phase_err_vs_f32_rad": phase_err(dft, ref32[2]), "steps_compared": n_err})
+                      "dft_phase_err_vs_f32_rad": perr, "dft_amp_rel_err_vs_f32":
+                          float(np.max(np.abs(np.abs(dft) / np.abs(ref32[2]) - 1))),
+                      "phase_within_1e-4_rad": perr <= 1e-4, "steps_compared": n_err})
         out[name] = entry
     # against the FP64 oracle on a small shot of the same physics
     small = dict(nx=384, ny=320, npml=16, n_steps=1500, dx=0.25e-3, dy=0.25e-3, courant=0.99, profile=3,
@@ -444,7 +466,9 @@ def run_precision(args, local: int) -> dict:
                    "dft_phase_err_rad": phase_err(shot.dft(), o_dft)}
         out.setdefault(name, {})["vs_fp64_oracle_384x320_1500_steps"] = res
     out["note"] = ("F16: Ez, Hx, Hy, Jz and the drive map stored as FP16 with a power-of-two scale per array; "
-                   "BF16 the same without scales; 18 B per cell-update (FP32: 36); arithmetic FP32, DFT FP64")
+                   "BF16 the same without scales; 18 B per cell-update per pass (FP32: 36), 9 (18) when a pass "
+                   "advances two time steps; arithmetic FP32, DFT FP64; errors vs FP32 over the whole "
+                   f"{n_err}-step shot")
     return out
 
 
@@ -471,27 +495,34 @@ def cpu_baseline(prob, seconds: float, threads: int | None = None) -> dict:
 
 
 def run_reference(args, world, rank, dist) -> None:
+    """The reference's step on the host cores: the oracle's FP32 restatement
+    of the reference update equations, all threads, on the same shot built by
+    oracle/workload.py with numpy (the product library is never loaded in
+    this process)."""
     if rank != 0:
         return
     import oracle as O
+    from oracle import workload
 
-    prob = make_problem(max(args.steps + args.warmup + 2, 10), args.size)
+    wl = workload.production_setup(max(args.steps + args.warmup + 2, 10), args.size)
     cores = O.threads()
-    o = O.Oracle(prob.setup_ptr, fp32=True)
-    cells = prob.nx * prob.ny
+    o = O.Oracle(wl.setup_ptr, fp32=True)
+    cells = wl.setup.nx * wl.setup.ny
     o.run(1, args.warmup)
     t = time.perf_counter()
     o.run(args.warmup + 1, args.warmup + args.steps)
     dt = time.perf_counter() - t
+    o.close()
     value = cells * args.steps / dt / 1e9
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference", "config": dict(workload_config(args), block_steps=1),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} time steps of the {prob.nx}x{prob.ny} shot per run "
+                             "sample": f"{args.steps} time steps of the {wl.setup.nx}x{wl.setup.ny} shot per run "
                                        "(one time step per bench step), FP32 restatement of the "
-                                       "reference update equations, OpenMP over rows"},
+                                       "reference update equations, OpenMP over rows; setup built with numpy "
+                                       "(oracle/workload.py), no product library loaded"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -565,10 +596,16 @@ def run_ours(args, world, rank, local, dist) -> None:
                 times.append(dt_e)
         te = allreduce_max(dist, sum(times) / len(times))
         e_units = allreduce_sum(dist, float(cells) * s.n_steps)
-        e2e = {"value": e_units / te / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h),
-               "note": f"whole {s.n_steps}-step shots: create (upload) + run + read traces/DFT + destroy, "
-                       "pageable host buffers"}
+        # a bench step is S time steps: a shot of s.n_steps time steps is
+        # s.n_steps / S bench steps, and its copies are spread over them
+        per_shot_steps = s.n_steps / S
+        e2e = {"value": e_units / te / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(h2d / per_shot_steps),
+               "d2h_bytes_per_step": int(d2h / per_shot_steps),
+               "h2d_bytes_per_shot": int(h2d), "d2h_bytes_per_shot": int(d2h),
+               "bench_steps_per_shot": per_shot_steps,
+               "note": f"whole {s.n_steps}-step shots ({per_shot_steps:g} bench steps of {S} time steps): create "
+                       "(uploads the drive map, tables, source envelope) + run + read traces/DFT + destroy, "
+                       "pageable host buffers; bytes per step = bytes per shot / bench steps per shot"}
         del tr, d
 
     cpu = None
@@ -622,7 +659,7 @@ def main() -> None:
     ap.add_argument("--serve-max-side", type=int, default=4096)
     ap.add_argument("--storage", choices=["f32", "f16", "bf16"], default="f32",
                     help="field storage of the main measurement (arithmetic is FP32 in all)")
-    ap.add_argument("--prec-steps", type=int, default=2000,
+    ap.add_argument("--prec-steps", type=int, default=20000,
                     help="steps of the F16/BF16 vs FP32 comparison on the production shot (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

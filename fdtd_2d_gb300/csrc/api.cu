@@ -942,6 +942,8 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
 
 }  // namespace
 
+int fdtd2d::validate_setup(const fdtd2d_setup* s) { return validate(s); }
+
 void fdtd2d::adopt_ctx(fdtd2d_ctx* c, cudaStream_t batch_stream) {
   cudaSetDevice(c->device);
   if (c->stream && !c->batch) {
@@ -985,6 +987,10 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
   c->n_det = s->n_det; c->n_comp = s->n_comp; c->record = s->record_traces ? 1 : 0;
   c->medium = s->medium;
   c->dft = s->dft_freq > 0 && s->n_det > 0;
+  // Test parameters of the persistent kernel's grid barrier (the test that
+  // makes a wait run out): its bound in ns and a count added to its target.
+  if (const char* v = std::getenv("FDTD2D_WAIT_NS")) c->wait_ns = std::strtoull(v, nullptr, 10);
+  if (const char* v = std::getenv("FDTD2D_TEST_BARRIER_EXTRA")) c->bar_extra = std::max(0, std::atoi(v));
 
   DevShot& h = c->h;
   h.nx = nx; h.ny = ny; h.pitch = pitch; h.npml = P; h.n_steps = s->n_steps; h.base_n = 0;
@@ -1355,7 +1361,15 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
 
 extern "C" {
 
+static int run_body(fdtd2d_ctx* c, int32_t n_first, int32_t n_last);
+
+// The entry point: its body (which may grow the event-timing lists) runs
+// behind abi_guard.
 int fdtd2d_run(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
+  return abi_guard([&] { return run_body(c, n_first, n_last); });
+}
+
+static int run_body(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
   if (!c) return FDTD2D_ERR_INVALID;
   if (c->batch) return FDTD2D_ERR_STATE;   // stepped by its batch
   if (n_first != c->step + 1 || n_last < n_first - 1 || n_last > c->n_steps) return FDTD2D_ERR_RANGE;
@@ -1370,6 +1384,8 @@ int fdtd2d_run(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
     // all the steps in persistent launches, the tracker and the line probe
     // on their service warps
     PersistAux A{};
+    A.wait_ns = c->wait_ns;
+    A.bar_extra = c->bar_extra;
     if (c->n_rc > 0) {
       A.n_rc = c->n_rc;
       A.scan_i = c->d_rc_scan;
@@ -1560,8 +1576,18 @@ int fdtd2d_current_step(const fdtd2d_ctx* c, int32_t* n) {
   return FDTD2D_OK;
 }
 
+static int read_traces_body(fdtd2d_ctx* c, int32_t n0, int32_t n1, float* det_ez, float* comp_ez, float* comp_hx,
+                            float* comp_hy);
+
+// The entry points below whose bodies allocate host buffers run them behind
+// abi_guard: a failed allocation is FDTD2D_ERR_NOMEM, not an exception.
 int fdtd2d_read_traces(fdtd2d_ctx* c, int32_t n0, int32_t n1, float* det_ez, float* comp_ez,
                        float* comp_hx, float* comp_hy) {
+  return abi_guard([&] { return read_traces_body(c, n0, n1, det_ez, comp_ez, comp_hx, comp_hy); });
+}
+
+static int read_traces_body(fdtd2d_ctx* c, int32_t n0, int32_t n1, float* det_ez, float* comp_ez, float* comp_hx,
+                            float* comp_hy) {
   if (!c) return FDTD2D_ERR_INVALID;
   if (!c->record) return FDTD2D_ERR_STATE;
   if (n0 < 1 || n1 < n0 || n1 > c->n_steps) return FDTD2D_ERR_RANGE;
@@ -1588,7 +1614,13 @@ int fdtd2d_read_traces(fdtd2d_ctx* c, int32_t n0, int32_t n1, float* det_ez, flo
   return FDTD2D_OK;
 }
 
+static int read_dft_body(fdtd2d_ctx* c, double* re, double* im);
+
 int fdtd2d_read_dft(fdtd2d_ctx* c, double* re, double* im) {
+  return abi_guard([&] { return read_dft_body(c, re, im); });
+}
+
+static int read_dft_body(fdtd2d_ctx* c, double* re, double* im) {
   if (!c || !re || !im) return FDTD2D_ERR_INVALID;
   if (!c->dft) return FDTD2D_ERR_STATE;
   cudaSetDevice(c->device);
@@ -1745,7 +1777,8 @@ int write_field16(fdtd2d_ctx* c, int which, const float* host) {
 
 int fdtd2d_read_field(fdtd2d_ctx* c, int which, float* host) {
   if (!c || !host) return FDTD2D_ERR_INVALID;
-  if (c->h.store != FDTD2D_STORE_F32 && which <= FDTD2D_FIELD_JZ) return read_field16(c, which, host);
+  if (c->h.store != FDTD2D_STORE_F32 && which <= FDTD2D_FIELD_JZ)
+    return abi_guard([&] { return read_field16(c, which, host); });
   FieldView v;
   if (!field_view(c, which, c->step & 1, &v)) return FDTD2D_ERR_INVALID;
   cudaSetDevice(c->device);
@@ -1759,7 +1792,8 @@ int fdtd2d_read_field(fdtd2d_ctx* c, int which, float* host) {
 
 int fdtd2d_write_field(fdtd2d_ctx* c, int which, const float* host) {
   if (!c || !host) return FDTD2D_ERR_INVALID;
-  if (c->h.store != FDTD2D_STORE_F32 && which <= FDTD2D_FIELD_JZ) return write_field16(c, which, host);
+  if (c->h.store != FDTD2D_STORE_F32 && which <= FDTD2D_FIELD_JZ)
+    return abi_guard([&] { return write_field16(c, which, host); });
   cudaSetDevice(c->device);
   cudaError_t e = cudaStreamSynchronize(c->stream);
   for (int b = 0; b < 4 && e == cudaSuccess; ++b) {

@@ -308,6 +308,14 @@ int fdtd2d_batch_create(int device, int64_t hbm_budget_bytes, fdtd2d_batch** out
     hbm_budget_bytes = (int64_t)(free_b * 0.9);
   }
   b->budget = hbm_budget_bytes;
+  // host descriptors first: a failure here leaves no device resource behind
+  try {
+    b->h_shots.resize(kMaxShots);
+  } catch (...) {
+    delete b;
+    return FDTD2D_ERR_NOMEM;
+  }
+  std::memset(b->h_shots.data(), 0, kMaxShots * sizeof(DevShot));
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_shots, kMaxShots * sizeof(DevShot));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_trial, kMaxShots * sizeof(DevShot));
@@ -318,8 +326,6 @@ int fdtd2d_batch_create(int device, int64_t hbm_budget_bytes, fdtd2d_batch** out
     return e == cudaErrorMemoryAllocation ? FDTD2D_ERR_NOMEM : FDTD2D_ERR_CUDA;
   }
   b->d_tmisc = b->d_misc + kMiscWords;
-  b->h_shots.resize(kMaxShots);
-  std::memset(b->h_shots.data(), 0, kMaxShots * sizeof(DevShot));
   *out = b;
   return FDTD2D_OK;
 }
@@ -646,6 +652,9 @@ static int fdtd2d_server_submit_body(fdtd2d_server* s, const fdtd2d_setup* setup
   if (setup->medium != FDTD2D_MEDIUM_UNIFORM || setup->npml > tma_max_pml() || setup->n_rc > 0 ||
       setup->line_n > 0 || setup->storage != FDTD2D_STORE_F32)
     return FDTD2D_ERR_INVALID;
+  // a setup fdtd2d_create would refuse is refused here, not at admission
+  const int vrc = validate_setup(setup);
+  if (vrc) return vrc;
   const int64_t bytes = fdtd2d_device_bytes(setup);
   if (bytes < 0) return FDTD2D_ERR_INVALID;
   if (bytes > s->b->budget) return FDTD2D_ERR_BUDGET;   // could never be admitted
@@ -665,17 +674,23 @@ static int fdtd2d_server_step_body(fdtd2d_server* s) {
   fdtd2d_batch* b = s->b;
   cudaSetDevice(b->device);
   int n_done = 0;
-  // 1. admit in arrival order while the head fits (uploads overlap the queued steps)
-  size_t q = 0;
-  for (; q < s->queue.size(); ++q) {
+  // 1. admit in arrival order while the head fits (uploads overlap the queued
+  // steps).  Each shot leaves the queue as soon as it is admitted and
+  // recorded, so an error on a later one returns with every earlier one
+  // running exactly once; the failing shot stays at the head of the queue.
+  // The running list grows before the add, so nothing can throw between a
+  // successful add and its record.
+  while (!s->queue.empty()) {
+    s->running.reserve(s->running.size() + 1);
+    const Queued head = s->queue.front();
     int32_t slot = -1;
-    const int rc = fdtd2d_batch_add(b, s->queue[q].s, &slot);
-    if (rc == FDTD2D_ERR_BUDGET) break;
-    if (rc) return rc;
+    const int arc = fdtd2d_batch_add(b, head.s, &slot);
+    if (arc == FDTD2D_ERR_BUDGET) break;
+    if (arc) return arc;
     const fdtd2d_ctx* c = b->m[slot].ctx;
-    s->running.push_back({slot, s->queue[q].tag, b->m[slot].base + c->n_steps});
+    s->running.push_back({slot, head.tag, b->m[slot].base + c->n_steps});
+    s->queue.erase(s->queue.begin());
   }
-  s->queue.erase(s->queue.begin(), s->queue.begin() + q);
   // 2. retire what the GPU has finished
   int rc = retire(s, &n_done);
   if (rc) return rc;
@@ -750,7 +765,8 @@ int fdtd2d_server_pop(fdtd2d_server* s, int64_t* tag, int32_t* n_det, int32_t* n
   if (tag) *tag = f.tag;
   if (n_det) *n_det = f.n_det;
   if (n_steps) *n_steps = f.n_steps;
-  if (dft && !f.dft.empty()) std::memcpy(dft, f.dft.data(), std::min<size_t>(f.dft.size(), 2 * (size_t)max_det) * 8);
+  if (dft && !f.dft.empty())
+    std::memcpy(dft, f.dft.data(), std::min<size_t>(f.dft.size(), 2 * (size_t)std::max<int32_t>(0, max_det)) * 8);
   if (trace && !f.trace.empty())
     std::memcpy(trace, f.trace.data(), std::min<size_t>(f.trace.size(), (size_t)std::max<int64_t>(0, max_trace)) * 4);
   s->finished.erase(s->finished.begin());

@@ -54,6 +54,9 @@ struct fdtd2d_ctx {
   int4* d_punits = nullptr;
   int n_punits = 0;
   unsigned* d_bar = nullptr;
+  // test parameters of its grid barrier (PersistAux::wait_ns, bar_extra)
+  unsigned long long wait_ns = 0;
+  int bar_extra = 0;
   // the CPML-band kernel runs on a second stream beside the interior one:
   // ev_t marks the interior kernel of the last step, ev_e the CPML kernel,
   // ev_m the shot stream's work before a run
@@ -86,6 +89,9 @@ namespace fdtd2d {
 // kernel: never the persistent form, whose cooperative launch wants the
 // whole GPU.
 int create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out, bool solo = false);
+// The checks fdtd2d_create makes on a setup before it allocates anything
+// (FDTD2D_OK, FDTD2D_ERR_INVALID or FDTD2D_ERR_RANGE).
+int validate_setup(const fdtd2d_setup* s);
 // Hand a member shot to the batch's stream: its own stream is released and
 // fdtd2d_run is refused from then on (the batch steps it).
 void adopt_ctx(fdtd2d_ctx* c, cudaStream_t batch_stream);

@@ -147,6 +147,13 @@ struct PersistAux {
   int* spd;                   // [step][n_rc], row n-1 for step n
   int line_n, line_j, line_i0, line_first, line_last;
   float* line;                // [n - line_first][line_n]
+  // Bound on each grid-barrier wait in ns (0: the default, 1 s), and a count
+  // added to every barrier's target.  Both exist for the test that makes a
+  // barrier wait run out (FDTD2D_WAIT_NS, FDTD2D_TEST_BARRIER_EXTRA read at
+  // create): with bar_extra = 1 no barrier completes, each CTA gives up after
+  // wait_ns, records the timeout and returns.  Normal runs leave both 0.
+  unsigned long long wait_ns;
+  int bar_extra;
 };
 
 // The register-streaming step for steps n_first..n_last (global numbering)

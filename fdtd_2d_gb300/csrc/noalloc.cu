@@ -17,6 +17,7 @@
 // using the same device) race on it and must be serialised by the caller.
 #include "../../include/fdtd2d.h"
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -63,21 +64,66 @@ __global__ void count_nonfinite_total(unsigned long long* __restrict__ scratch, 
   }
 }
 
-// Device address of the scratch array, looked up once per device.
+// Device address of the scratch array, looked up once per device context.
+// The runtime resolves the symbol for the current device's primary context;
+// a device reset (cudaDeviceReset) destroys that context and the module's
+// memory with it, and the next use creates a new context where the array
+// has another address.  So the cached address is kept together with the
+// identity of the context it was resolved in (cuCtxGetId, through the
+// runtime's driver entry points) and resolved again when that changes.
+// Where the identity cannot be read, the address is resolved on every call.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+struct CtxFns {
+  CtxGetCurrentFn current = nullptr;
+  CtxGetIdFn id = nullptr;
+};
+
+const CtxFns& ctx_fns() {
+  static const CtxFns fns = [] {
+    CtxFns f;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      f.current = reinterpret_cast<CtxGetCurrentFn>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      f.id = reinterpret_cast<CtxGetIdFn>(p);
+    return f;
+  }();
+  return fns;
+}
+
+// Identity of the calling thread's current context, 0 when unknown.
+unsigned long long current_ctx_id() {
+  const CtxFns& f = ctx_fns();
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (f.current && f.id && f.current(&ctx) == CUDA_SUCCESS && ctx && f.id(ctx, &id) == CUDA_SUCCESS) return id;
+  return 0;
+}
+
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 unsigned long long* g_ptr[kMaxDevices] = {};
+unsigned long long g_ctx[kMaxDevices] = {};
 
 int scratch_for_current_device(unsigned long long** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return FDTD2D_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_ptr[dev]) {
+  const unsigned long long id = current_ctx_id();
+  if (!g_ptr[dev] || id == 0 || id != g_ctx[dev]) {
     void* p = nullptr;
     // The symbol's host-side name is only a stand-in; the kernels need the
-    // device address, which the runtime resolves for the current device.
+    // device address, which the runtime resolves for the current device
+    // (creating its primary context if there is none yet).
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return FDTD2D_ERR_CUDA;
     g_ptr[dev] = static_cast<unsigned long long*>(p);
+    g_ctx[dev] = current_ctx_id();   // the context the address belongs to
   }
   *out = g_ptr[dev];
   return FDTD2D_OK;

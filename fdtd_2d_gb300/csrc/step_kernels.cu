@@ -332,9 +332,9 @@ cudaError_t launch_step(const DevShot& shot, const int4* units, int n_units, int
 
 // Grid-wide barrier of a cooperative launch.  Thread 0 of each CTA releases
 // the CTA's writes, adds one to *count and waits until the count reaches
-// `target` (every CTA has arrived), for at most kWaitNs, or until another
+// `target` (every CTA has arrived), for at most wait_ns, or until another
 // CTA has set *err.  False when the barrier did not complete.
-__device__ bool grid_barrier(unsigned* count, unsigned target, int* err) {
+__device__ bool grid_barrier(unsigned* count, unsigned target, int* err, uint64_t wait_ns) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -350,7 +350,7 @@ __device__ bool grid_barrier(unsigned* count, unsigned target, int* err) {
         ok = 0;
         break;
       }
-      if (global_ns() - t0 > kWaitNs) {
+      if (global_ns() - t0 > wait_ns) {
         atomicExch(err, kErrWaitTimeout);
         ok = 0;
         break;
@@ -429,6 +429,7 @@ step_persist_kernel(const __grid_constant__ DevShot S, const int4* __restrict__ 
   const int n_warps = (int)((gridDim.x * blockDim.x) >> 5);
   const int n_work = n_warps - A.n_rc - (A.line_n > 0 ? 1 : 0);
   const int steps = repeat > 0 ? repeat : n_last - n_first + 1;
+  const uint64_t wait_ns = A.wait_ns ? A.wait_ns : kWaitNs;
   unsigned target = 0;
   for (int s = 0; s <= steps; ++s) {
     if (warp < n_work) {
@@ -443,7 +444,7 @@ step_persist_kernel(const __grid_constant__ DevShot S, const int4* __restrict__ 
     }
     if (s == steps) break;
     target += gridDim.x;
-    if (!grid_barrier(bar, target, err)) return;
+    if (!grid_barrier(bar, target + A.bar_extra, err, wait_ns)) return;
   }
 }
 

@@ -7,7 +7,7 @@
  *
  *   cudaError_t DevMemoryAllocation()     FDTD_2D_Full/Kernel.cuh:100  -> fdtd2d_create
  *   cudaError_t DevFieldCalculation()     FDTD_2D_Full/Kernel.cuh:102  -> fdtd2d_run (+ read_*)
- *   cudaError_t DevSourceToDetect...()    FDTD_2D_Full/Kernel.cuh:101  -> two contexts, see INTEGRATION.md
+ *   cudaError_t DevSourceToDetect...()    FDTD_2D_Full/Kernel.cuh:101  -> two contexts (vacuum + medium)
  *   cudaError_t DevMemoryFree()           FDTD_2D_Full/Kernel.cuh:106  -> fdtd2d_destroy
  *
  * Here the data that the reference passes in globals travels in one plain
@@ -204,10 +204,12 @@ int fdtd2d_check_finite(fdtd2d_ctx *ctx);
    Returns FDTD2D_OK when all values are finite, FDTD2D_ERR_NONFINITE when
    some are not (count in *nonfinite if non-NULL), FDTD2D_ERR_RANGE when
    n > 2^31 (the scratch covers at most 2^31 values per call).  `stream` is a
-   cudaStream_t (NULL = default stream); the call waits for it.  The first
-   call on a device resolves the scratch address for that device: make it
-   before capturing any stream into a CUDA graph.  All calls share the one
-   scratch array, so calls whose GPU work overlaps race; serialise them. */
+   cudaStream_t (NULL = default stream) of the calling thread's current
+   device, and d_data memory that device can read; the call waits for the
+   stream.  The first call on a device (and the first after that device was
+   reset) resolves the scratch address for it: make that call before
+   capturing any stream into a CUDA graph.  All calls share the one scratch
+   array, so calls whose GPU work overlaps race; serialise them. */
 int fdtd2d_check_finite_noalloc(const float *d_data, int64_t n, int64_t *nonfinite, void *stream);
 
 /* Release everything.  Replaces DevMemoryFree (FDTD_2D_Full/kernel.cu:2820-2987). */

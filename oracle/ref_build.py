@@ -12,8 +12,11 @@ into oracle/_ref/ (git-ignored) because the sources do not compile as shipped:
   * Ext_kernel.cuh: `extern struct X {...};` (an MSVC extension) becomes
     `struct X {...};`.
 
-Usage: python oracle/ref_build.py [/path/to/reference]  (needs the reference
-tree, so it runs only where the reference is mounted; the GPU machine never runs it).
+Usage: python oracle/ref_build.py [/path/to/reference]
+The reference tree is the argument, else $FDTD2D_REFERENCE, else the build
+container's read-only mount point below.  It needs the reference sources, so
+it runs only where they are mounted; build_if_present() (called by the
+package build) skips it quietly elsewhere.
 """
 from __future__ import annotations
 
@@ -24,7 +27,17 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-DEFAULT_REF = Path("/root/reference")
+MOUNT_POINT = Path("/root/reference")   # where the build container mounts the reference
+
+
+def reference_root(arg: str | None = None) -> Path:
+    """The reference tree: `arg`, else $FDTD2D_REFERENCE, else the mount point."""
+    import os
+
+    if arg:
+        return Path(arg)
+    env = os.environ.get("FDTD2D_REFERENCE")
+    return Path(env) if env else MOUNT_POINT
 
 
 def strip_comments(src: str) -> str:
@@ -100,12 +113,28 @@ def rewrite_launches(src: str) -> str:
     return "".join(out)
 
 
+def build_if_present() -> Path | None:
+    """Build oracle/_ref/ref_fdtd2d when the reference sources are present
+    and the binary is missing or older than the harness; None when absent."""
+    ref = reference_root() / "FDTD_2D_Full"
+    if not (ref / "kernel.cu").exists():
+        return None
+    exe = OUT / "ref_fdtd2d"
+    deps = [HERE / "ref_harness.cpp", HERE / "ref_build.py", *(HERE / "ref_shim").glob("*.h")]
+    if exe.exists() and all(d.stat().st_mtime <= exe.stat().st_mtime for d in deps):
+        return exe
+    return exe if compile_reference(ref) == 0 else None
+
+
 def main() -> int:
-    ref_root = Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_REF
-    ref = ref_root / "FDTD_2D_Full"
+    ref = reference_root(sys.argv[1] if len(sys.argv) > 1 else None) / "FDTD_2D_Full"
     if not (ref / "kernel.cu").exists():
         print(f"reference sources not found under {ref}", file=sys.stderr)
         return 1
+    return compile_reference(ref)
+
+
+def compile_reference(ref: Path) -> int:
     OUT.mkdir(exist_ok=True)
     (OUT / "kernel_emu.cu").write_text(rewrite_launches((ref / "kernel.cu").read_text(errors="replace")),
                                        errors="replace")

@@ -1,0 +1,121 @@
+"""Failure detection on the GPU without a GPU fault, through the C ABI.
+
+* A bounded device wait that runs out: the persistent kernel's grid barrier
+  is given a target one higher than the CTAs that arrive (a test parameter
+  read at create) and a 1 ms bound, so every CTA gives up, records the
+  timeout in the shot's error word and returns.  fdtd2d_synchronize reports
+  FDTD2D_ERR_TIMEOUT; the shot can still be destroyed and the device keeps
+  working for the next shot.  The reference ignores every return code
+  (FDTD_2D_Full/FDTD_cuda.cu:406,418,439).
+* The serving loop's admission: a shot whose admission fails stays at the
+  head of the queue while the shots admitted before it run exactly once.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import fdtd_2d_gb300 as F
+import oracle as O
+from helpers import FIELD_TOL, FIELDS, compare_fields
+
+pytestmark = pytest.mark.gpu
+
+
+def _small(**kw):
+    args = dict(nx=256, ny=192, n_steps=60, x_lo=128, x_hi=246, src_i=30, src_j=96, det_i=34, det_j=96,
+                pulse_width=0.1e-9)
+    args.update(kw)
+    return F.Problem.from_spec(**args)
+
+
+def test_barrier_wait_runs_out(gpu, monkeypatch):
+    monkeypatch.setenv("FDTD2D_PERSIST", "1")
+    monkeypatch.setenv("FDTD2D_WAIT_NS", "1000000")          # 1 ms
+    monkeypatch.setenv("FDTD2D_TEST_BARRIER_EXTRA", "1")     # no barrier completes
+    prob = _small()
+    shot = F.Shot(prob, gpu)
+    assert shot.kernel_name().startswith("step_persist_kernel")
+    shot.run(1, 40)
+    with pytest.raises(F.FdtdError) as e:
+        shot.synchronize()
+    assert e.value.status == F.ERR_TIMEOUT
+    shot.close()   # fdtd2d_destroy after the timeout
+
+    # the device is usable: the same shot, barrier as normal, matches the oracle
+    monkeypatch.delenv("FDTD2D_WAIT_NS")
+    monkeypatch.delenv("FDTD2D_TEST_BARRIER_EXTRA")
+    ref = O.Oracle(prob.setup_ptr)
+    with F.Shot(prob, gpu) as ok:
+        assert ok.kernel_name().startswith("step_persist_kernel")
+        ok.run(1, 40)
+        ok.synchronize()
+        ref.run(1, 40)
+        compare_fields(ok, ref, FIELDS, tol=FIELD_TOL)
+        assert ok.check_finite()
+
+
+def test_server_admission_error_keeps_queue(gpu):
+    """Three shots queued; the second is made invalid after it was accepted
+    (its setup must stay valid until admission, and here it does not).  The
+    scheduling round that meets it returns its error with the first shot
+    admitted once and the second still queued; once the setup is valid again
+    every shot finishes exactly once, each equal to its solo run."""
+    probs = [_small(n_steps=48 + 8 * k, src_j=90 + k) for k in range(3)]
+    solo = []
+    for p in probs:
+        with F.Shot(p, gpu) as s:
+            s.run(1, p.n_steps)
+            solo.append(s.dft())
+    with F.Server(gpu, block_steps=16) as srv:
+        for k, p in enumerate(probs):
+            srv.submit(p, 100 + k)
+        nx = probs[1].setup.nx
+        probs[1].setup.nx = 4            # fdtd2d_create refuses a grid below 8 cells
+        with pytest.raises(F.FdtdError) as e:
+            srv.step()
+        assert e.value.status == F.ERR_INVALID
+        queued, running, finished = srv.counts()
+        assert (queued, running) == (2, 1)
+        probs[1].setup.nx = nx
+        got = {}
+        for _ in range(10000):
+            srv.step()
+            while (r := srv.pop()) is not None:
+                assert r["tag"] not in got
+                got[r["tag"]] = r["dft"]
+            if len(got) == 3 and srv.counts() == (0, 0, 0):
+                break
+        assert sorted(got) == [100, 101, 102]
+        for k in range(3):
+            assert np.array_equal(got[100 + k], solo[k])
+
+
+def test_server_submit_refuses_invalid(gpu):
+    prob = _small()
+    prob.setup.det[0].i = prob.setup.nx + 5   # detector off the grid
+    with F.Server(gpu, block_steps=16) as srv:
+        with pytest.raises(F.FdtdError) as e:
+            srv.submit(prob, 1)
+        assert e.value.status == F.ERR_RANGE
+        assert srv.counts() == (0, 0, 0)
+
+
+def test_server_pop_negative_sizes(gpu):
+    """Negative buffer sizes copy nothing into the caller's buffers."""
+    prob = _small(n_steps=20)
+    with F.Server(gpu, block_steps=16) as srv:
+        srv.submit(prob, 7)
+        for _ in range(10000):
+            srv.step()
+            if srv.counts()[2]:
+                break
+        L = F.lib()
+        dft = np.full(8, 123.0)
+        tr = np.full(8, 5.0, np.float32)
+        tag, nd, ns = C.c_int64(), C.c_int32(), C.c_int32()
+        rc = L.fdtd2d_server_pop(srv._h, C.byref(tag), C.byref(nd), C.byref(ns),
+                                 dft.ctypes.data_as(C.POINTER(C.c_double)), -1,
+                                 tr.ctypes.data_as(C.POINTER(C.c_float)), -1)
+        assert rc == 1 and tag.value == 7
+        assert np.all(dft == 123.0) and np.all(tr == 5.0)

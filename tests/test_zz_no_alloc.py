@@ -56,3 +56,60 @@ def test_noalloc_rejects_oversize(gpu):
     with pytest.raises(F.FdtdError) as e:
         F.check_finite_noalloc(buf.data_ptr(), (1 << 31) + 1)
     assert e.value.status == F.ERR_RANGE
+
+
+def _planted(n, idx, values, torch, device):
+    """A device array of n zeros with `values` at `idx`, and its non-finite count."""
+    a = torch.zeros(n, dtype=torch.float32, device=device)
+    if idx:
+        a[torch.tensor(idx, device=device)] = torch.tensor(values, dtype=torch.float32, device=device)
+    host = np.zeros(len(idx), np.float32)
+    host[:] = values
+    return a, int((~np.isfinite(host)).sum())
+
+
+def test_noalloc_many_blocks_on_a_stream(gpu):
+    """Three full 2^20-value blocks and a ragged tail of 5 values, scanned on a
+    side stream: values planted in the first block, the third and the last
+    element.  Two calls in a row with different counts, so a block slot left
+    from the first call would show up in the second's total."""
+    torch = pytest.importorskip("torch")
+    dev = f"cuda:{gpu}"
+    chunk = 1 << 20
+    n = 3 * chunk + 5
+    side = torch.cuda.Stream(device=dev)
+    cases = [
+        ([7, 2 * chunk + 11, n - 1], [np.nan, np.inf, -np.inf]),
+        ([chunk + 3, chunk + 4, 3 * chunk], [np.nan, 1.0, np.nan]),   # one finite plant
+    ]
+    for idx, vals in cases:
+        a, expected = _planted(n, idx, vals, torch, dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        status, count = F.check_finite_noalloc(a.data_ptr(), n, side.cuda_stream)
+        assert count == expected, (idx, count, expected)
+        assert status == (F.ERR_NONFINITE if expected else F.OK)
+    # all finite after a call that counted some
+    a = torch.ones(n, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize(dev)
+    assert F.check_finite_noalloc(a.data_ptr(), n, side.cuda_stream) == (F.OK, 0)
+
+
+def test_noalloc_largest_call(gpu):
+    """n = 2^31 exactly, the most one call covers (every scratch slot used):
+    NaN/Inf at the first value, the middle and the last."""
+    torch = pytest.importorskip("torch")
+    dev = f"cuda:{gpu}"
+    n = 1 << 31
+    free, _ = torch.cuda.mem_get_info(dev)
+    if free < 12 * (1 << 30):
+        pytest.skip("needs 8 GiB of free device memory")
+    a, expected = _planted(n, [0, (1 << 30) + 1, n - 1], [np.nan, np.inf, np.nan], torch, dev)
+    try:
+        torch.cuda.synchronize(dev)
+        assert F.check_finite_noalloc(a.data_ptr(), n) == (F.ERR_NONFINITE, expected)
+        a[0] = 0.0
+        torch.cuda.synchronize(dev)
+        assert F.check_finite_noalloc(a.data_ptr(), n) == (F.ERR_NONFINITE, expected - 1)
+    finally:
+        del a
+        torch.cuda.empty_cache()
