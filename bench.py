@@ -243,8 +243,13 @@ def mixed_shot_spec(rng, side_lo: float, side_hi: float, f_lo: float, f_hi: floa
 
 def run_batched(args, local: int) -> tuple[dict, float]:
     """64 uneven shots (seed 1002) end to end: one at a time through the
-    single-shot ABI vs all admitted to one batch.  Returns the JSON object and
-    the batch's throughput in cell updates per second."""
+    single-shot ABI vs all admitted to one batch, at --batch-step-scale of
+    their 8000..16000 steps.  The kernel choice of every size class is timed
+    once before the timed passes (a create per shot), so both passes run
+    with the choices kept.  With --batch-storage f16 the batch also runs the
+    same shots with F16 storage, reported with its DFT phase error against
+    the plain FP32 pass.  Returns the JSON object and the batch's throughput
+    in cell updates per second."""
     import fdtd_2d_gb300 as F
 
     rng = np.random.default_rng(1002)
@@ -252,6 +257,13 @@ def run_batched(args, local: int) -> tuple[dict, float]:
              for k in range(args.batch_shots)]
     probs = [F.Problem.from_spec(**sp) for sp in specs]
     cells = sum(p.nx * p.ny * p.n_steps for p in probs)
+    n = len(probs)
+
+    t = time.perf_counter()
+    for p in probs:
+        with F.Shot(p, local):
+            pass
+    t_tune = time.perf_counter() - t
 
     def plain_pass():
         t = time.perf_counter()
@@ -263,52 +275,66 @@ def run_batched(args, local: int) -> tuple[dict, float]:
                 out.append(s.dft())
         return time.perf_counter() - t, out
 
-    # cold: every grid size new to the process (kernel choices timed at
-    # create); warm: the same shots again with the choices kept
-    F.clear_kernel_choices()
-    tp, plain_dft = plain_pass()
-    tw, _ = plain_pass()
-    F.clear_kernel_choices()
-    t = time.perf_counter()
-    with F.Batch(local) as b:
-        ids = [b.add(p) for p in probs]
-        if any(i is None for i in ids):
-            raise RuntimeError("batch budget too small for the mixed-shot sample")
-        while not all(b.finished(i) for i in ids):
-            b.run(256)
-        b.synchronize()
-        batch_dft = []
-        for i in ids:
-            sh = b.shot(i)
-            sh.traces()
-            batch_dft.append(sh.dft())
-        name = b.kernel_name()
-        launches = b.launches()
-        solo = sum(1 for i in ids if b.shot(i).kernel_name().startswith("step_tmat"))
-    tb = time.perf_counter() - t
+    def batch_pass(ps):
+        t = time.perf_counter()
+        with F.Batch(local) as b:
+            ids = [b.add(p) for p in ps]
+            if any(i is None for i in ids):
+                raise RuntimeError("batch budget too small for the mixed-shot sample")
+            while not all(b.finished(i) for i in ids):
+                b.run(256)
+            b.synchronize()
+            dft = []
+            for i in ids:
+                sh = b.shot(i)
+                sh.traces()
+                dft.append(sh.dft())
+            name = b.kernel_name()
+            launches = b.launches()
+            solo = sum(1 for i in ids if b.shot(i).kernel_name().startswith("step_tmat"))
+        return time.perf_counter() - t, dft, name, launches, solo
+
+    tw, plain_dft = plain_pass()
+    tb, batch_dft, name, launches, solo = batch_pass(probs)
     same = all(np.array_equal(x, y) for x, y in zip(plain_dft, batch_dft))
-    n = len(probs)
     out = {"shots": n, "sample": f"{n} shots, seed 1002, sides log-uniform 1024..6144 (aspect 1..3), CPML 16..32, "
                                  f"20..75 GHz at dx = lambda/20, 4..16 elements, 8000..16000 steps x "
                                  f"{args.batch_step_scale} ({sum(p.n_steps for p in probs)} steps in all)",
-           "cell_updates": cells, "plain_shots_per_s": n / tp, "batched_shots_per_s": n / tb,
-           "speedup": tp / tb, "plain_gcells": cells / tp / 1e9, "batched_gcells": cells / tb / 1e9,
-           "plain_warm_shots_per_s": n / tw, "speedup_vs_warm": tw / tb, "plain_warm_gcells": cells / tw / 1e9,
+           "cell_updates": cells, "plain_shots_per_s": n / tw, "batched_shots_per_s": n / tb,
+           "speedup": tw / tb, "plain_gcells": cells / tw / 1e9, "batched_gcells": cells / tb / 1e9,
+           "kernel_choice_timing_s": t_tune,
            "kernel": name, "tensor_path_members": solo, "gpu_launches": int(launches),
            "dft_equal_to_plain": bool(same),
-           "note": "end to end from host setups: create/upload, all steps, traces + DFT read back. plain: one "
-                   "shot at a time through the single-shot ABI, cold (every grid size new, kernel choice "
-                   "timed at create) and warm (the same shots again, choices kept); batch (cold): grids of "
-                   ">= 2^21 cells as solo members (own streams, two-step tensor path), the rest in one "
-                   "persistent launch per step in CUDA-graph blocks of 16"}
+           "note": "end to end from host setups: create/upload, all steps, traces + DFT read back; kernel "
+                   "choices of every size class timed once before both passes. plain: one shot at a time "
+                   "through the single-shot ABI; batch: grids of >= 2^21 cells as solo members (own "
+                   "streams, two-step tensor path, stream priority by size), the rest in one persistent "
+                   "launch per step in CUDA-graph blocks of 16"}
+    if args.batch_storage != "f32":
+        store = {"f16": F.STORE_F16, "bf16": F.STORE_BF16}[args.batch_storage]
+        probs16 = [F.Problem.from_spec(**sp, storage=store) for sp in specs]
+        for p in probs16:
+            with F.Shot(p, local):
+                pass
+        t16, dft16, _, _, _ = batch_pass(probs16)
+        ph = max(float(np.max(np.abs(np.angle(a * np.conj(b))))) for a, b in zip(dft16, plain_dft))
+        out[f"batched_{args.batch_storage}"] = {
+            "shots_per_s": n / t16, "gcells": cells / t16 / 1e9, "speedup_vs_plain_f32": tw / t16,
+            "dft_phase_err_vs_plain_f32_rad": ph, "phase_within_1e-4_rad": ph <= 1e-4,
+            "note": f"the same shots with {args.batch_storage.upper()} field storage (every shot a solo member); "
+                    "phase error: largest over shots and detectors"}
     return out, cells / tb
 
 
 def run_serving(args, local: int, capacity: float) -> dict:
     """Poisson request stream (seed 1004) at 0.8 x the measured batched
     capacity: each request a 4..12-shot frequency sweep over 10..75 GHz on one
-    grid size; served by the continuous-batching loop vs one request at a
-    time through the single-shot ABI."""
+    grid size, tanh plasma profiles as the mixed-shot sample's (seeded peak
+    and position, no random field); served by the continuous-batching loop
+    vs one request at a time through the single-shot ABI.  A request's
+    setups are built when it arrives (inside its latency, for both) and
+    released when it completes, so the host holds only the requests in
+    flight."""
     import fdtd_2d_gb300 as F
 
     rng = np.random.default_rng(1004)
@@ -320,18 +346,19 @@ def run_serving(args, local: int, capacity: float) -> dict:
         shots = []
         for k, f in enumerate(freqs):
             sub = np.random.default_rng([1004, r, k])
-            sp = mixed_shot_spec(sub, side, side, f, f, args.batch_step_scale, 5000 + 100 * r + k, aspect=False,
+            sp = mixed_shot_spec(sub, side, side, f, f, args.serve_step_scale, 5000 + 100 * r + k, aspect=False,
                                  freq=float(f))
-            shots.append(F.Problem.from_spec(**sp))
+            sp.update(profile=2, grf_rms=0.0)
+            shots.append(sp)
         reqs.append(shots)
-    work = [sum(p.nx * p.ny * p.n_steps for p in q) for q in reqs]
+    work = [sum(sp["nx"] * sp["ny"] * sp["n_steps"] for sp in q) for q in reqs]
     rate = 0.8 * capacity / (sum(work) / len(work))      # requests per second
     gaps = rng.exponential(1.0 / rate, len(reqs))
     arrive = np.cumsum(gaps) - gaps[0]
 
     def pct(lat):
         return {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
-                "p99": float(np.percentile(lat, 99))}
+                "p99": float(np.percentile(lat, 99)), "max": float(np.max(lat))}
 
     # continuous batching
     t0 = time.perf_counter()
@@ -342,8 +369,8 @@ def run_serving(args, local: int, capacity: float) -> dict:
         while len(done_at) < len(reqs):
             now = time.perf_counter() - t0
             while nxt < len(reqs) and arrive[nxt] <= now:
-                for k, p in enumerate(reqs[nxt]):
-                    srv.submit(p, nxt * 1000 + k)
+                for k, sp in enumerate(reqs[nxt]):
+                    srv.submit(F.Problem.from_spec(**sp), nxt * 1000 + k)
                 nxt += 1
             q, running, fin = srv.counts()
             if q == 0 and running == 0 and fin == 0 and nxt < len(reqs):
@@ -366,22 +393,26 @@ def run_serving(args, local: int, capacity: float) -> dict:
         now = time.perf_counter() - t0
         if now < arrive[r]:
             time.sleep(arrive[r] - now)
-        for p in q:
+        for sp in q:
+            p = F.Problem.from_spec(**sp)
             with F.Shot(p, local) as s:
                 s.run(1, p.n_steps)
                 s.traces()
                 s.dft()
+            p.close()
         lat_p.append(time.perf_counter() - t0 - arrive[r])
     t_plain = time.perf_counter() - t0
     n_shots = sum(len(q) for q in reqs)
     return {"requests": len(reqs), "shots": n_shots,
             "sample": f"{len(reqs)} Poisson requests (seed 1004) of 4..12-shot sweeps over 10..75 GHz, square "
-                      f"grids log-uniform 512..{args.serve_max_side}, profiles as the mixed-shot sample, "
-                      f"steps x {args.batch_step_scale}; offered load 0.8 x the batched capacity",
+                      f"grids log-uniform 512..{args.serve_max_side}, tanh profiles with seeded peak and position "
+                      f"as the mixed-shot sample, 8000..16000 steps x {args.serve_step_scale} "
+                      f"({sum(work):.3g} cell updates); offered load 0.8 x the batched capacity",
            "rate_req_per_s": rate, "shots_per_s": n_shots / t_batch, "latency_s": pct(lat_b),
            "plain_shots_per_s": n_shots / t_plain, "plain_latency_s": pct(lat_p), "kernel": kernel,
-           "note": "latency = completion of a request's last shot - its arrival; plain = requests one at a "
-                   "time through the single-shot ABI"}
+           "gcells": sum(work) / t_batch / 1e9, "plain_gcells": sum(work) / t_plain / 1e9,
+           "note": "latency = completion of a request's last shot - its arrival (setups built at arrival); "
+                   "plain = requests one at a time through the single-shot ABI"}
 
 
 def run_precision(args, local: int) -> dict:
@@ -653,10 +684,14 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--size", type=int, default=8192, help="grid side (8192 = the production shot)")
     ap.add_argument("--batch-shots", type=int, default=64, help="mixed-shot sample size (0: skip batched/serving)")
-    ap.add_argument("--batch-step-scale", type=float, default=0.05,
+    ap.add_argument("--batch-step-scale", type=float, default=1.0,
                     help="fraction of the 8000..16000 steps each mixed shot runs")
-    ap.add_argument("--serve-requests", type=int, default=6, help="requests in the serving sample (0: skip)")
-    ap.add_argument("--serve-max-side", type=int, default=4096)
+    ap.add_argument("--batch-storage", choices=["f32", "f16", "bf16"], default="f16",
+                    help="also run the batch with this field storage (f32: no second run)")
+    ap.add_argument("--serve-requests", type=int, default=50, help="requests in the serving sample (0: skip)")
+    ap.add_argument("--serve-max-side", type=int, default=8192)
+    ap.add_argument("--serve-step-scale", type=float, default=0.1,
+                    help="fraction of the 8000..16000 steps each serving shot runs")
     ap.add_argument("--storage", choices=["f32", "f16", "bf16"], default="f32",
                     help="field storage of the main measurement (arithmetic is FP32 in all)")
     ap.add_argument("--prec-steps", type=int, default=20000,

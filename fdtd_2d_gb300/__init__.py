@@ -176,6 +176,7 @@ def _lib():
         "fdtd2d_run_timed": (C.c_int, [vp, C.c_int32, C.c_int32, _fp]),
         "fdtd2d_time_step_kernel": (C.c_int, [vp, C.c_int]),
         "fdtd2d_clear_kernel_choices": (None, []),
+        "fdtd2d_kernel_choice_source": (C.c_int, [vp]),
         "fdtd2d_step_kernel_time": (C.c_int, [vp, _dp, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                               C.POINTER(C.c_int32)]),
         "fdtd2d_stability": (C.c_double, [C.POINTER(Setup)]),
@@ -374,6 +375,12 @@ class Shot:
     def kernel_name(self) -> str:
         """The step kernel this shot launches, with its launch shape."""
         return _lib().fdtd2d_kernel_name(self._h).decode()
+
+    def choice_source(self) -> int:
+        """How its kernel choices were made: 0 timed at create (or forced), 1
+        kept by this process from an earlier shot of the class, 2 read from
+        the persisted choices file (fdtd2d_kernel_choice_source)."""
+        return int(_lib().fdtd2d_kernel_choice_source(self._h))
 
     def read_field(self, which) -> np.ndarray:
         w = FIELD_NAMES[which] if isinstance(which, str) else which

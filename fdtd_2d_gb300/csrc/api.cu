@@ -23,6 +23,9 @@
 #include <new>
 #include <vector>
 
+#include <sys/stat.h>
+#include <unistd.h>
+
 using namespace fdtd2d;
 
 #include "ctx.h"
@@ -446,6 +449,7 @@ cudaError_t issue_pair(fdtd2d_ctx* c, const PairPlan& p, DevShot& h, TensorMaps&
 // tensor path's steps per pass.
 struct KernelChoice {
   int k = -1, q = 0, lv = 1;
+  bool from_file = false;   // read from the persisted choices, not timed in this process
 };
 using ChoiceKey = std::tuple<int, int, int, int, int, int, std::string>;
 std::mutex g_choice_mu;
@@ -467,8 +471,109 @@ ChoiceKey choice_key(const fdtd2d_ctx* c, int device, const char* what) {
   return ChoiceKey{device, cls(c->nx), cls(c->ny), (c->npml + 15) / 16, c->h.store, c->h.kp != nullptr, env};
 }
 
+// ---- persisted choices -------------------------------------------------------
+// The choices are also kept in a small JSON file, so that a new process skips
+// the timing of the classes an earlier one timed (0.31 s at 8192^2): the file
+// $FDTD2D_TUNE_CACHE, else $XDG_CACHE_HOME/fdtd2d/kernel_choices.json, else
+// $HOME/.cache/fdtd2d/kernel_choices.json; FDTD2D_TUNE_CACHE=0 (or empty)
+// keeps the choices in memory only.  An entry is keyed by the device's name,
+// SM count and compute capability (not its index) and the shot class.  The
+// file is read once per device, at its first lookup, and rewritten whole
+// (temporary file, then rename) when a choice is added.  A file that cannot
+// be read or written only costs the timing.
+std::map<std::string, KernelChoice> g_file;   // every entry of the file, all devices
+bool g_file_loaded[64] = {};
+
+std::string clean(const std::string& t) {
+  std::string o = t;
+  for (char& ch : o)
+    if (ch == '"' || ch == '\\' || ch < 32) ch = '_';
+  return o;
+}
+
+std::string cache_path() {
+  if (const char* v = std::getenv("FDTD2D_TUNE_CACHE")) return (std::strcmp(v, "0") == 0) ? std::string() : v;
+  if (const char* x = std::getenv("XDG_CACHE_HOME"); x && *x) return std::string(x) + "/fdtd2d/kernel_choices.json";
+  if (const char* h = std::getenv("HOME"); h && *h) return std::string(h) + "/.cache/fdtd2d/kernel_choices.json";
+  return std::string();
+}
+
+std::string device_ident(int device) {
+  static std::string ident[64];
+  if (device < 0 || device >= 64) return std::string();
+  if (ident[device].empty()) {
+    cudaDeviceProp pr{};
+    if (cudaGetDeviceProperties(&pr, device) != cudaSuccess) return std::string();
+    char b[320];
+    std::snprintf(b, sizeof b, "%s|%d|%d.%d", pr.name, pr.multiProcessorCount, pr.major, pr.minor);
+    ident[device] = clean(b);
+  }
+  return ident[device];
+}
+
+// "<device>|<class fields>|<what and overrides>" (the last part holds '|'s)
+std::string key_text(const ChoiceKey& k) {
+  char b[96];
+  std::snprintf(b, sizeof b, "|%d|%d|%d|%d|%d|", std::get<1>(k), std::get<2>(k), std::get<3>(k), std::get<4>(k),
+                std::get<5>(k));
+  return device_ident(std::get<0>(k)) + b + clean(std::get<6>(k));
+}
+
+void load_choices(int device) {   // g_choice_mu held
+  if (device < 0 || device >= 64 || g_file_loaded[device]) return;
+  g_file_loaded[device] = true;
+  const std::string path = cache_path();
+  const std::string id = device_ident(device);
+  if (path.empty() || id.empty()) return;
+  FILE* f = std::fopen(path.c_str(), "r");
+  if (!f) return;
+  char line[1024];
+  while (std::fgets(line, sizeof line, f)) {
+    // one entry per line:  "key": [k, q, lv],
+    const char* a = std::strchr(line, '"');
+    const char* z = a ? std::strchr(a + 1, '"') : nullptr;
+    if (!z) continue;
+    const std::string key(a + 1, z);
+    KernelChoice ch;
+    if (std::sscanf(z + 1, " : [ %d , %d , %d ]", &ch.k, &ch.q, &ch.lv) != 3) continue;
+    ch.from_file = true;
+    if (!g_file.count(key)) g_file[key] = ch;
+    // entries of this device go to the lookup table
+    if (key.compare(0, id.size() + 1, id + "|") != 0) continue;
+    int f1, f2, f3, f4, f5, used = 0;
+    if (std::sscanf(key.c_str() + id.size(), "|%d|%d|%d|%d|%d|%n", &f1, &f2, &f3, &f4, &f5, &used) != 5 || !used)
+      continue;
+    const ChoiceKey ck{device, f1, f2, f3, f4, f5, key.substr(id.size() + used)};
+    if (!g_choice.count(ck)) g_choice[ck] = ch;
+  }
+  std::fclose(f);
+}
+
+void save_choices() {   // g_choice_mu held
+  const std::string path = cache_path();
+  if (path.empty()) return;
+  const size_t slash = path.rfind('/');
+  if (slash != std::string::npos && slash > 0) {
+    // make the directories of the path (one level at a time)
+    for (size_t p = path.find('/', 1); p != std::string::npos && p <= slash; p = path.find('/', p + 1))
+      mkdir(path.substr(0, p).c_str(), 0755);
+  }
+  const std::string tmp = path + ".tmp" + std::to_string((long)getpid());
+  FILE* f = std::fopen(tmp.c_str(), "w");
+  if (!f) return;
+  std::fprintf(f, "{\n \"fdtd2d_kernel_choices\": 1,\n \"choices\": {\n");
+  size_t n = 0;
+  for (const auto& kv : g_file)
+    std::fprintf(f, "  \"%s\": [%d, %d, %d]%s\n", kv.first.c_str(), kv.second.k, kv.second.q, kv.second.lv,
+                 ++n < g_file.size() ? "," : "");
+  std::fprintf(f, " }\n}\n");
+  const bool ok = std::fclose(f) == 0;
+  if (!ok || std::rename(tmp.c_str(), path.c_str()) != 0) std::remove(tmp.c_str());
+}
+
 bool find_choice(const ChoiceKey& key, KernelChoice* out) {
   std::lock_guard<std::mutex> lock(g_choice_mu);
+  load_choices(std::get<0>(key));
   auto it = g_choice.find(key);
   if (it == g_choice.end()) return false;
   *out = it->second;
@@ -477,7 +582,18 @@ bool find_choice(const ChoiceKey& key, KernelChoice* out) {
 
 void keep_choice(const ChoiceKey& key, const KernelChoice& ch) {
   std::lock_guard<std::mutex> lock(g_choice_mu);
-  g_choice[key] = ch;
+  KernelChoice c = ch;
+  c.from_file = false;
+  g_choice[key] = c;
+  const std::string kt = key_text(key);
+  if (device_ident(std::get<0>(key)).empty()) return;
+  g_file[kt] = c;
+  save_choices();
+}
+
+// How the choices of a create were made (fdtd2d_kernel_choice_source).
+void note_choice(fdtd2d_ctx* c, bool have, const KernelChoice& known) {
+  if (have) c->choice_src = std::max(c->choice_src, known.from_file ? 2 : 1);
 }
 
 // A material-ID medium that the uniform medium represents exactly: every
@@ -607,6 +723,7 @@ int setup_persist(fdtd2d_ctx* c, int device) {
   const ChoiceKey key = choice_key(c, device, c->medium == FDTD2D_MEDIUM_UNIFORM ? "persist0" : "persist1");
   KernelChoice known;
   const bool have = mode < 0 && find_choice(key, &known);
+  note_choice(c, have, known);
   if (have && known.k != 1) return FDTD2D_OK;
   if (mode < 0 && !have && c->path_ms <= 0.f && c->tma) return FDTD2D_OK;   // nothing to compare with
   // units down to one row: a step's time is the longest warp's chain of
@@ -688,6 +805,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   const ChoiceKey key = choice_key(c, device, "tmat");
   KernelChoice known;
   const bool have = find_choice(key, &known);
+  note_choice(c, have, known);
   if (have && known.k < 0) return FDTD2D_OK;   // the one-row kernel alone won for this class
   if (have) {
     forced = known.k;
@@ -698,7 +816,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   DevShot& h = c->h;
   const int nx = c->nx, ny = c->ny, P = c->npml;
   if (!c->side) {
-    cudaError_t e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    cudaError_t e = cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, c->priority);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_t, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_e, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_m, cudaEventDisableTiming);
@@ -709,7 +827,8 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   // no kernel writes keep their values in every buffer), its unit counter,
   // and a scratch psi slab for the trials (a trial pair's second step writes
   // psi buffer 0).
-  bool try2 = tb_mode != 0 && c->n_steps >= 2 && ny - 2 * P - 4 >= 8;
+  // (the two-step kernel takes the interior denominators as constants)
+  bool try2 = tb_mode != 0 && c->n_steps >= 2 && ny - 2 * P - 4 >= 8 && h.den_uniform;
   float* psi_trial = nullptr;
   const size_t psi_floats = (size_t)h.psi_buf * 2 + 1024;
   auto give_back = [&](float*& p) {
@@ -960,7 +1079,8 @@ void fdtd2d::adopt_ctx(fdtd2d_ctx* c, cudaStream_t batch_stream) {
   c->batch = true;
 }
 
-int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out, bool solo) {
+int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out, bool solo,
+                       int priority) {
   if (!out) return FDTD2D_ERR_INVALID;
   *out = nullptr;
   int rc = validate(s);
@@ -972,8 +1092,9 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
   fdtd2d_ctx* c = new (std::nothrow) fdtd2d_ctx();
   if (!c) return FDTD2D_ERR_NOMEM;
   c->device = device;
+  c->priority = priority;
   cudaError_t e = cudaSetDevice(device);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, priority);
   if (e == cudaSuccess) keep_pool_memory(device);
   if (e != cudaSuccess) {
     rc = fail_cuda(c, e);
@@ -1147,6 +1268,16 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
     std::vector<float> dex(pitch, 0.f), dhx(pitch, 0.f), dey(ny, 0.f), dhy(ny, 0.f);
     for (int i = 0; i < nx - 1; ++i) { dex[i] = s->den_ex[i]; dhx[i] = s->den_hx[i]; }
     for (int j = 0; j < ny - 1; ++j) { dey[j] = s->den_ey[j]; dhy[j] = s->den_hy[j]; }
+    // each table constant over the CPML-free columns / rows (bitwise)?
+    auto constant = [](const std::vector<float>& v, int a, int b, float* out) {
+      if (b < a) return false;
+      for (int k = a + 1; k <= b; ++k)
+        if (std::memcmp(&v[k], &v[a], sizeof(float)) != 0) return false;
+      *out = v[a];
+      return true;
+    };
+    h.den_uniform = constant(dex, P, nx - P - 1, &h.den_c[0]) && constant(dhx, P, nx - P - 1, &h.den_c[1]) &&
+                    constant(dey, P, ny - P - 1, &h.den_c[2]) && constant(dhy, P, ny - P - 1, &h.den_c[3]);
     float *d_tab, *d_dex, *d_dhx, *d_dey, *d_dhy;
     CK(dalloc(c, &d_tab, tab.size()));
     CK(dalloc(c, &d_dex, (size_t)pitch));
@@ -1283,6 +1414,7 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
     } else if (!(at && std::strcmp(at, "0") == 0) && c->n_steps >= 1 &&
                find_choice(choice_key(c, device, "tma"), &known)) {
       c->tma_shape = known.q;   // timed for a shot of this class before
+      note_choice(c, true, known);
     } else if (!(at && std::strcmp(at, "0") == 0) && c->n_steps >= 1) {
       // Each trial re-runs step 1 with traces and the DFT switched off: a
       // step reads one buffer set and overwrites the other with values that
@@ -1862,5 +1994,7 @@ const char* fdtd2d_kernel_name(const fdtd2d_ctx* c) {
 }
 
 int fdtd2d_last_cuda_error(const fdtd2d_ctx* c) { return c ? c->last_cuda : -1; }
+
+int fdtd2d_kernel_choice_source(const fdtd2d_ctx* c) { return c ? c->choice_src : FDTD2D_ERR_INVALID; }
 
 }  // extern "C"

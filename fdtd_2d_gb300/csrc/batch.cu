@@ -83,6 +83,8 @@ struct fdtd2d_batch {
   int64_t launches = 0;
   int last_cuda = 0;
   char name[64] = {0};
+  // CUDA stream priority range of the device (numerically lower = higher)
+  int prio_least = 0, prio_greatest = 0;
 };
 
 namespace {
@@ -222,6 +224,20 @@ cudaError_t capture_block(fdtd2d_batch* b, int K, cudaGraphExec_t* out) {
   return e;
 }
 
+// Stream priorities: the batch kernel's stream, which steps the smallest
+// shots, has the device's highest priority; a solo member is one level lower
+// than that at the solo threshold and one more level lower per doubling of
+// its cells, down to the default.  The GPU then starts the pending CTAs of
+// smaller shots first, so shots of small requests finish while large ones
+// hold the device.  Only the order of work on the device changes, never a
+// result.
+int solo_priority(const fdtd2d_batch* b, int64_t cells) {
+  const int64_t sc = std::max<int64_t>(1, solo_cells());
+  int level = 1;
+  for (int64_t t = sc * 2; t <= cells && level < 64; t *= 2) ++level;
+  return std::min(b->prio_least, b->prio_greatest + level);
+}
+
 int add_solo(fdtd2d_batch* b, const fdtd2d_setup* s, int64_t bytes, int32_t* shot) {
   int slot = -1;
   for (int k = 0; k < (int)b->m.size(); ++k)
@@ -232,7 +248,8 @@ int add_solo(fdtd2d_batch* b, const fdtd2d_setup* s, int64_t bytes, int32_t* sho
     slot = (int)b->m.size() - 1;
   }
   fdtd2d_ctx* c = nullptr;
-  const int rc = create_ctx(s, b->device, false, &c, true);   // its own streams, kernel choice timed
+  // its own streams (priority by size), kernel choice timed
+  const int rc = create_ctx(s, b->device, false, &c, true, solo_priority(b, (int64_t)s->nx * s->ny));
   if (rc) return rc;
   // the bytes it holds: two more field buffers on the two-step path
   if (c->tb) bytes += 2 * c->h.cells * 4 * store_bytes(c->h.store);
@@ -316,7 +333,8 @@ int fdtd2d_batch_create(int device, int64_t hbm_budget_bytes, fdtd2d_batch** out
     return FDTD2D_ERR_NOMEM;
   }
   std::memset(b->h_shots.data(), 0, kMaxShots * sizeof(DevShot));
-  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  cudaDeviceGetStreamPriorityRange(&b->prio_least, &b->prio_greatest);
+  cudaError_t e = cudaStreamCreateWithPriority(&b->stream, cudaStreamNonBlocking, b->prio_greatest);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_shots, kMaxShots * sizeof(DevShot));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_trial, kMaxShots * sizeof(DevShot));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_misc, 2 * kMiscWords * sizeof(int));
@@ -340,18 +358,21 @@ int fdtd2d_batch_add(fdtd2d_batch* b, const fdtd2d_setup* s, int32_t* shot) {
 static int fdtd2d_batch_add_body(fdtd2d_batch* b, const fdtd2d_setup* s, int32_t* shot) {
   if (!b || !s || !shot) return FDTD2D_ERR_INVALID;
   *shot = -1;
-  if (s->medium != FDTD2D_MEDIUM_UNIFORM || s->npml > tma_max_pml() || s->n_rc > 0 || s->line_n > 0 ||
-      s->storage != FDTD2D_STORE_F32)
+  if (s->medium != FDTD2D_MEDIUM_UNIFORM || s->npml > tma_max_pml() || s->n_rc > 0 || s->line_n > 0)
     return FDTD2D_ERR_INVALID;
   const int64_t bytes = fdtd2d_device_bytes(s);
   if (bytes < 0) return FDTD2D_ERR_INVALID;
   if (b->used + bytes > b->budget) return FDTD2D_ERR_BUDGET;
   // A large grid goes solo when it fits with the two extra field buffers of
-  // the two-step path.
-  const int64_t field_buf = (int64_t)buffer_floats(s->nx, s->ny) * 4 * 4;
+  // the two-step path.  The batch kernel steps FP32 fields only, so a shot
+  // with 16-bit storage is a solo member whatever its size (the single-shot
+  // path, 16-bit forms included), admitted once those buffers fit too.
+  const int64_t field_buf = (int64_t)buffer_floats(s->nx, s->ny) * 4 * store_bytes(s->storage);
   const int64_t cells = (int64_t)s->nx * s->ny;
   const int64_t sc = solo_cells();
-  if (sc > 0 && cells >= sc && b->used + bytes + 2 * field_buf <= b->budget) return add_solo(b, s, bytes, shot);
+  const bool fits2 = b->used + bytes + 2 * field_buf <= b->budget;
+  if (s->storage != FDTD2D_STORE_F32) return fits2 ? add_solo(b, s, bytes, shot) : FDTD2D_ERR_BUDGET;
+  if (sc > 0 && cells >= sc && fits2) return add_solo(b, s, bytes, shot);
   int slot = -1;
   for (int k = 0; k < (int)b->m.size(); ++k)
     if (!b->m[k].live) { slot = k; break; }
@@ -650,14 +671,17 @@ int fdtd2d_server_submit(fdtd2d_server* s, const fdtd2d_setup* setup, int64_t ta
 static int fdtd2d_server_submit_body(fdtd2d_server* s, const fdtd2d_setup* setup, int64_t tag) {
   if (!s || !setup) return FDTD2D_ERR_INVALID;
   if (setup->medium != FDTD2D_MEDIUM_UNIFORM || setup->npml > tma_max_pml() || setup->n_rc > 0 ||
-      setup->line_n > 0 || setup->storage != FDTD2D_STORE_F32)
+      setup->line_n > 0)
     return FDTD2D_ERR_INVALID;
   // a setup fdtd2d_create would refuse is refused here, not at admission
   const int vrc = validate_setup(setup);
   if (vrc) return vrc;
   const int64_t bytes = fdtd2d_device_bytes(setup);
   if (bytes < 0) return FDTD2D_ERR_INVALID;
-  if (bytes > s->b->budget) return FDTD2D_ERR_BUDGET;   // could never be admitted
+  // could never be admitted (a 16-bit shot also needs its two extra buffers)
+  const int64_t extra = setup->storage == FDTD2D_STORE_F32
+                            ? 0 : 2 * (int64_t)buffer_floats(setup->nx, setup->ny) * 4 * store_bytes(setup->storage);
+  if (bytes + extra > s->b->budget) return FDTD2D_ERR_BUDGET;
   s->queue.push_back({setup, tag});
   return FDTD2D_OK;
 }

@@ -68,6 +68,15 @@ struct DevShot {
   const float* den_hx;        // [pitch]
   const float* den_ey;        // [ny]
   const float* den_hy;        // [ny]
+  // The denominators inside the CPML-free part of the grid, when each table
+  // is constant there (den_ex and den_hx over columns [npml, nx-npml-1],
+  // den_ey and den_hy over rows [npml, ny-npml-1]): den_c = (den_ex,
+  // den_hx, den_ey, den_hy) there, and den_uniform = 1.  The two-step
+  // kernel, whose cells and halo all lie inside that part, takes them as
+  // launch constants instead of loading the tables (the same floats, so the
+  // same bits); the host runs it only when den_uniform is set.
+  int den_uniform;
+  float den_c[4];
 
   // sources and detectors, by row
   const int* row_start;       // [ny+1] offsets into pts

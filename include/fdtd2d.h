@@ -235,7 +235,11 @@ const char *fdtd2d_kernel_name(const fdtd2d_ctx *ctx);
    of at least 2^21 cells (FDTD2D_BATCH_SOLO_CELLS overrides; 0 for none) is
    a solo member instead: a full single shot on its own streams with its own
    kernel choice (two steps per pass where that wins), stepped from the same
-   run calls; its budget share counts that path's two extra field buffers. ---- */
+   run calls; its budget share counts that path's two extra field buffers.
+   The batch's kernel steps FP32 fields, so a shot with F16 or BF16 storage
+   is a solo member whatever its size.  Solo members' streams have lower
+   CUDA stream priorities the larger the grid (the batch kernel's stream the
+   highest), so the GPU starts the work of smaller shots first. ---- */
 typedef struct fdtd2d_batch fdtd2d_batch;
 
 /* hbm_budget_bytes <= 0: 90 % of the device memory free now. */
@@ -304,8 +308,20 @@ int fdtd2d_run_timed(fdtd2d_ctx *ctx, int32_t n_first, int32_t n_last, float *el
 int fdtd2d_time_step_kernel(fdtd2d_ctx *ctx, int on);
 
 /* Forget the kernel choices fdtd2d_create keeps per shot class (the next
-   shot of every class is timed again).  No counterpart in the reference. */
+   shot of every class is timed again).  The choices are also persisted in a
+   JSON file keyed by the device's name, SM count and compute capability and
+   the shot class: $FDTD2D_TUNE_CACHE, else
+   $XDG_CACHE_HOME/fdtd2d/kernel_choices.json, else
+   $HOME/.cache/fdtd2d/kernel_choices.json (FDTD2D_TUNE_CACHE=0: memory
+   only).  A process reads the file at the first shot of a device, so a shot
+   of a class an earlier process timed skips the timing; clearing affects
+   this process's memory only.  No counterpart in the reference. */
 void fdtd2d_clear_kernel_choices(void);
+/* How the kernel choices of this context's create were made: 0 timed at
+   create (or forced by FDTD2D_* overrides), 1 a choice this process kept
+   from an earlier shot of the class, 2 a choice read from the persisted
+   file.  No counterpart in the reference. */
+int fdtd2d_kernel_choice_source(const fdtd2d_ctx *ctx);
 int fdtd2d_step_kernel_time(fdtd2d_ctx *ctx, double *ms, int64_t *launches, int64_t *cells, int32_t *steps);
 
 /* Stability number of the explicit update with the Drude current:

@@ -14,10 +14,15 @@ def pytest_configure(config):
 
 
 @pytest.fixture(scope="session", autouse=True)
-def _built():
-    """Build the native pieces once per session (fast when up to date)."""
+def _built(tmp_path_factory):
+    """Build the native pieces once per session (fast when up to date).  The
+    kernel choices persisted across processes go to a file of this session,
+    so no test reads choices an earlier run left behind."""
+    import os
+
     from fdtd_2d_gb300 import build
 
+    os.environ["FDTD2D_TUNE_CACHE"] = str(tmp_path_factory.mktemp("tune") / "kernel_choices.json")
     build.build()
     yield
 

@@ -52,27 +52,33 @@ def test_reduced_storage_against_oracle(gpu, storage):
     assert perr <= b["phase"]
 
 
-# Bounds of the two-step case below (1400 x 260, 400 steps), a few times the
-# errors measured on GB300.
-BOUNDS_TWO_STEP = {F.STORE_F16: {"field": 2e-2, "trace": 1e-2, "phase": 1e-4},
-                   F.STORE_BF16: {"field": 2e-1, "trace": 6e-2, "phase": 1e-3}}
+# Bounds of the two-step case below (1400 x 260, 1000 steps): those of the
+# one-row case above.  The pulse must reach the dense plasma: where the
+# density is ~1e-5..1e-9 of its peak, a step's Jz increment is below half an
+# F16 ulp at Jz's scale and rounds away, so F16 keeps no Jz there (BF16, with
+# FP32's exponent range, does).  Such a Jz is that far below the peak's too
+# and its effect on Ez is of the same order; measured on a 400-step window
+# that ends before the dense plasma: F16 Ez/Hx/Hy within 3..7e-3 of FP64,
+# Jz lost.
+BOUNDS_TWO_STEP = BOUNDS
 
 
 @pytest.mark.parametrize("storage", [F.STORE_F16, F.STORE_BF16])
 def test_two_step_reduced_storage_against_oracle(gpu, monkeypatch, storage):
     """The 16-bit two-step path (stored-unit arithmetic, two time steps per
     pass) against the FP64 oracle directly: a steered array on a tanh x GRF
-    plasma whose pulse crosses the interior region and leaves through the
-    CPML."""
+    plasma whose pulse crosses the interior region into the dense plasma
+    and leaves through the CPML."""
     for k in ("FDTD2D_KERNEL", "FDTD2D_TMA", "FDTD2D_TMAT", "FDTD2D_PERSIST"):
         monkeypatch.delenv(k, raising=False)
     monkeypatch.setenv("FDTD2D_TB", "1")
     n_elem = 8
-    prob = F.Problem.from_spec(nx=1400, ny=260, npml=16, n_steps=400, dx=0.25e-3, dy=0.25e-3, courant=0.99,
-                               profile=3, ne_peak=3e19, x_center=900, width=60, grf_rms=0.05, grf_corr=10, seed=7,
+    prob = F.Problem.from_spec(nx=1400, ny=260, npml=16, n_steps=1000, dx=0.25e-3, dy=0.25e-3, courant=0.99,
+                               profile=3, ne_peak=3e19, x_center=620, width=40, grf_rms=0.05, grf_corr=10, seed=7,
                                nu=2e9, n_elem=n_elem, src_i=300, src_j=100, src_dj=5, src_di=0, freq=50e9,
                                steer_deg=15, pulse=1, pulse_width=0.2e-9, n_det=n_elem, det_i=300, det_j=100,
                                det_dj=5, det_di=0, dft_freq=50e9, storage=storage)
+    assert prob.stability() < 1.0
     ref = O.Oracle(prob.setup_ptr)
     ref.run(1, prob.n_steps)
     with F.Shot(prob, gpu) as shot:
@@ -112,9 +118,41 @@ def test_storage_roundtrip_and_nonfinite(gpu, storage):
 
 def test_reduced_storage_rejected_where_unsupported(gpu):
     """Reduced storage needs the staged kernel: a CPML deeper than its strip
-    slots, or a batch, refuses it."""
+    slots refuses it."""
     with pytest.raises(F.FdtdError):
         F.Shot(array_shot(F.STORE_F16, nx=300, ny=260, npml=121, src_i=130, det_i=130), gpu)
+
+
+@pytest.mark.parametrize("storage", [F.STORE_F16, F.STORE_BF16])
+def test_reduced_storage_in_batch_and_server(gpu, storage):
+    """16-bit shots join a batch (and the serving loop) as solo members, next
+    to FP32 shots on the batch kernel; every result is the same shot's run
+    alone, bit for bit."""
+    probs = [array_shot(storage, n_steps=300), array_shot(F.STORE_F32, n_steps=260, src_j=150),
+             array_shot(storage, n_steps=200, nx=500, ny=300, src_j=120)]
+    solo = []
+    for p in probs:
+        with F.Shot(p, gpu) as s:
+            s.run(1, p.n_steps)
+            solo.append((s.dft(), s.traces()["det_ez"]))
     with F.Batch(gpu) as b:
-        with pytest.raises(F.FdtdError):
-            b.add(array_shot(F.STORE_F16))
+        ids = [b.add(p) for p in probs]
+        assert all(i is not None for i in ids)
+        while not all(b.finished(i) for i in ids):
+            b.run(64)
+        b.synchronize()
+        for k, i in enumerate(ids):
+            sh = b.shot(i)
+            assert np.array_equal(sh.dft(), solo[k][0]) and np.array_equal(sh.traces()["det_ez"], solo[k][1])
+    got = {}
+    with F.Server(gpu, block_steps=32) as srv:
+        for k, p in enumerate(probs):
+            srv.submit(p, k)
+        for _ in range(100000):
+            srv.step()
+            while (r := srv.pop()) is not None:
+                got[r["tag"]] = r
+            if len(got) == len(probs):
+                break
+    for k in range(len(probs)):
+        assert np.array_equal(got[k]["dft"], solo[k][0]) and np.array_equal(got[k]["det_ez"], solo[k][1])
