@@ -816,7 +816,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   DevShot& h = c->h;
   const int nx = c->nx, ny = c->ny, P = c->npml;
   if (!c->side) {
-    cudaError_t e = cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, c->priority);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_t, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_e, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_m, cudaEventDisableTiming);
@@ -1079,8 +1079,7 @@ void fdtd2d::adopt_ctx(fdtd2d_ctx* c, cudaStream_t batch_stream) {
   c->batch = true;
 }
 
-int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out, bool solo,
-                       int priority) {
+int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out, bool solo) {
   if (!out) return FDTD2D_ERR_INVALID;
   *out = nullptr;
   int rc = validate(s);
@@ -1092,9 +1091,8 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
   fdtd2d_ctx* c = new (std::nothrow) fdtd2d_ctx();
   if (!c) return FDTD2D_ERR_NOMEM;
   c->device = device;
-  c->priority = priority;
   cudaError_t e = cudaSetDevice(device);
-  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, priority);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) keep_pool_memory(device);
   if (e != cudaSuccess) {
     rc = fail_cuda(c, e);

@@ -83,8 +83,6 @@ struct fdtd2d_batch {
   int64_t launches = 0;
   int last_cuda = 0;
   char name[64] = {0};
-  // CUDA stream priority range of the device (numerically lower = higher)
-  int prio_least = 0, prio_greatest = 0;
 };
 
 namespace {
@@ -224,20 +222,6 @@ cudaError_t capture_block(fdtd2d_batch* b, int K, cudaGraphExec_t* out) {
   return e;
 }
 
-// Stream priorities: the batch kernel's stream, which steps the smallest
-// shots, has the device's highest priority; a solo member is one level lower
-// than that at the solo threshold and one more level lower per doubling of
-// its cells, down to the default.  The GPU then starts the pending CTAs of
-// smaller shots first, so shots of small requests finish while large ones
-// hold the device.  Only the order of work on the device changes, never a
-// result.
-int solo_priority(const fdtd2d_batch* b, int64_t cells) {
-  const int64_t sc = std::max<int64_t>(1, solo_cells());
-  int level = 1;
-  for (int64_t t = sc * 2; t <= cells && level < 64; t *= 2) ++level;
-  return std::min(b->prio_least, b->prio_greatest + level);
-}
-
 int add_solo(fdtd2d_batch* b, const fdtd2d_setup* s, int64_t bytes, int32_t* shot) {
   int slot = -1;
   for (int k = 0; k < (int)b->m.size(); ++k)
@@ -248,8 +232,7 @@ int add_solo(fdtd2d_batch* b, const fdtd2d_setup* s, int64_t bytes, int32_t* sho
     slot = (int)b->m.size() - 1;
   }
   fdtd2d_ctx* c = nullptr;
-  // its own streams (priority by size), kernel choice timed
-  const int rc = create_ctx(s, b->device, false, &c, true, solo_priority(b, (int64_t)s->nx * s->ny));
+  const int rc = create_ctx(s, b->device, false, &c, true);   // its own streams, kernel choice timed
   if (rc) return rc;
   // the bytes it holds: two more field buffers on the two-step path
   if (c->tb) bytes += 2 * c->h.cells * 4 * store_bytes(c->h.store);
@@ -333,8 +316,7 @@ int fdtd2d_batch_create(int device, int64_t hbm_budget_bytes, fdtd2d_batch** out
     return FDTD2D_ERR_NOMEM;
   }
   std::memset(b->h_shots.data(), 0, kMaxShots * sizeof(DevShot));
-  cudaDeviceGetStreamPriorityRange(&b->prio_least, &b->prio_greatest);
-  cudaError_t e = cudaStreamCreateWithPriority(&b->stream, cudaStreamNonBlocking, b->prio_greatest);
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_shots, kMaxShots * sizeof(DevShot));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_trial, kMaxShots * sizeof(DevShot));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_misc, 2 * kMiscWords * sizeof(int));
@@ -620,6 +602,13 @@ int retire(fdtd2d_server* s, int* n_done) {
       continue;
     }
     fdtd2d_ctx* c = b->m[x.slot].ctx;
+    // A shot whose kernels gave up on a bounded wait has skipped work: its
+    // results are not handed out (the batch kernel's error word for its
+    // members, a solo member's own one), and the call reports the timeout.
+    int derr = 0;
+    const int* ew = mem.solo ? c->d_err : b->d_misc + kErr;
+    if (cudaMemcpy(&derr, ew, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return fail(b, cudaGetLastError());
+    if (derr) return FDTD2D_ERR_TIMEOUT;
     Finished f;
     f.tag = x.tag;
     f.n_det = c->n_det;

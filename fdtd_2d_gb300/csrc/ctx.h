@@ -15,7 +15,6 @@
 
 struct fdtd2d_ctx {
   int device = 0;
-  int priority = 0;         // CUDA stream priority of its streams (0: default)
   cudaStream_t stream = nullptr;
   bool batch = false;       // member of a batch: stream borrowed, stepped by the batch
   int nx = 0, ny = 0, pitch = 0, npml = 0, n_steps = 0;
@@ -91,10 +90,8 @@ namespace fdtd2d {
 // timing, and the batch adopts it (adopt_ctx) once its uploads are done.
 // solo = true makes a batch's solo member, which runs beside the batch's
 // kernel: never the persistent form, whose cooperative launch wants the
-// whole GPU.  priority: the CUDA stream priority of the shot's streams (a
-// batch gives smaller solo members higher priority).
-int create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out, bool solo = false,
-               int priority = 0);
+// whole GPU.
+int create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out, bool solo = false);
 // The checks fdtd2d_create makes on a setup before it allocates anything
 // (FDTD2D_OK, FDTD2D_ERR_INVALID or FDTD2D_ERR_RANGE).
 int validate_setup(const fdtd2d_setup* s);

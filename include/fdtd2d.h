@@ -237,9 +237,7 @@ const char *fdtd2d_kernel_name(const fdtd2d_ctx *ctx);
    kernel choice (two steps per pass where that wins), stepped from the same
    run calls; its budget share counts that path's two extra field buffers.
    The batch's kernel steps FP32 fields, so a shot with F16 or BF16 storage
-   is a solo member whatever its size.  Solo members' streams have lower
-   CUDA stream priorities the larger the grid (the batch kernel's stream the
-   highest), so the GPU starts the work of smaller shots first. ---- */
+   is a solo member whatever its size. ---- */
 typedef struct fdtd2d_batch fdtd2d_batch;
 
 /* hbm_budget_bytes <= 0: 90 % of the device memory free now. */
