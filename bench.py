@@ -644,13 +644,23 @@ def run_ours(args, world, rank, local, dist) -> None:
         cpu = cpu_baseline(prob, args.cpu_seconds)
     del shot
     batched = serving = precision = None
+
+    def leg(fn, *a):
+        # an extra leg that fails is reported in its own key; the main
+        # measurement above stands
+        try:
+            return fn(*a)
+        except Exception as e:  # noqa: BLE001
+            return {"error": f"{type(e).__name__}: {e}"}
+
     if args.prec_steps > 0 and world == 1:
-        precision = run_precision(args, local)
+        precision = leg(run_precision, args, local)
     if args.batch_shots > 0:
         barrier(dist)
-        batched, capacity = run_batched(args, local)
-        if args.serve_requests > 0:
-            serving = run_serving(args, local, capacity)
+        res = leg(run_batched, args, local)
+        batched, capacity = (res, None) if "error" in res else res
+        if args.serve_requests > 0 and capacity:
+            serving = leg(run_serving, args, local, capacity)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,

@@ -804,8 +804,18 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   int tb_mode = tbe ? std::atoi(tbe) : -1;   // -1 both forms, 0 one-step only, 1 two-step only
   const ChoiceKey key = choice_key(c, device, "tmat");
   KernelChoice known;
-  const bool have = find_choice(key, &known);
+  bool have = find_choice(key, &known);
   note_choice(c, have, known);
+  if (!have && c->untimed && forced < 0 && tb_mode != 0) {
+    // no timing: the shapes the timing keeps most often on GB300 (two steps
+    // per pass; 4 warps x 2 rows x 2 stages in FP32, 4 x 4 x 2 with 16-bit
+    // storage; 2-warp, 2-stage one-row shape on the CPML bands), not stored
+    known.k = c->h.store == FDTD2D_STORE_F32 ? tmat_shape_find(4, 2, 2) : tmat_shape_find(4, 4, 2);
+    known.q = tma_shape_find(2, 2);
+    known.lv = 2;
+    have = known.k >= 0 && known.q >= 0;
+    if (have) c->choice_src = std::max(c->choice_src, 3);
+  }
   if (have && known.k < 0) return FDTD2D_OK;   // the one-row kernel alone won for this class
   if (have) {
     forced = known.k;
@@ -1079,7 +1089,8 @@ void fdtd2d::adopt_ctx(fdtd2d_ctx* c, cudaStream_t batch_stream) {
   c->batch = true;
 }
 
-int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out, bool solo) {
+int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out, bool solo,
+                       bool untimed) {
   if (!out) return FDTD2D_ERR_INVALID;
   *out = nullptr;
   int rc = validate(s);
@@ -1091,6 +1102,7 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
   fdtd2d_ctx* c = new (std::nothrow) fdtd2d_ctx();
   if (!c) return FDTD2D_ERR_NOMEM;
   c->device = device;
+  c->untimed = untimed;
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) keep_pool_memory(device);
@@ -1413,6 +1425,8 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
                find_choice(choice_key(c, device, "tma"), &known)) {
       c->tma_shape = known.q;   // timed for a shot of this class before
       note_choice(c, true, known);
+    } else if (c->untimed) {
+      // no timing: the compiled default shape
     } else if (!(at && std::strcmp(at, "0") == 0) && c->n_steps >= 1) {
       // Each trial re-runs step 1 with traces and the DFT switched off: a
       // step reads one buffer set and overwrites the other with values that

@@ -49,7 +49,18 @@ struct Member {
   // its stream, oldest first.
   bool solo = false;
   std::vector<cudaEvent_t> ev;
+  int64_t seq = 0;      // admission order
 };
+
+// Solo members stepped at a time (the oldest admitted first; the others
+// wait): a few two-step chains keep the GPU busy, and every extra one only
+// adds streams and shares the device among more shots, which delays each.
+// FDTD2D_BATCH_SOLO_ACTIVE overrides it.
+int solo_active() {
+  const char* v = std::getenv("FDTD2D_BATCH_SOLO_ACTIVE");
+  const int k = v ? std::atoi(v) : 8;
+  return k > 0 ? k : 8;
+}
 
 // Grids of at least this many cells (2^21, about 1448^2) join a batch as
 // solo members (their own tensor-path launches fill the GPU); smaller ones
@@ -83,6 +94,7 @@ struct fdtd2d_batch {
   int64_t launches = 0;
   int last_cuda = 0;
   char name[64] = {0};
+  int64_t admitted = 0;                // admissions so far (Member::seq)
 };
 
 namespace {
@@ -231,8 +243,19 @@ int add_solo(fdtd2d_batch* b, const fdtd2d_setup* s, int64_t bytes, int32_t* sho
     b->m.emplace_back();
     slot = (int)b->m.size() - 1;
   }
+  // Its own streams; its kernel choice is timed at create while the batch
+  // has no device work in flight.  Timing trials run beside other shots'
+  // kernels measure nothing useful, and on a GB300 with some 150 shots in
+  // flight a trial kernel's bounded wait ran out; such an admission takes
+  // the class's stored choice or the default one.
+  bool busy = cudaStreamQuery(b->stream) == cudaErrorNotReady;
+  for (const Member& m : b->m)
+    if (m.live && m.solo && !busy)
+      busy = cudaStreamQuery(m.ctx->stream) == cudaErrorNotReady ||
+             (m.ctx->side && cudaStreamQuery(m.ctx->side) == cudaErrorNotReady);
+  cudaGetLastError();
   fdtd2d_ctx* c = nullptr;
-  const int rc = create_ctx(s, b->device, false, &c, true);   // its own streams, kernel choice timed
+  const int rc = create_ctx(s, b->device, false, &c, true, busy);
   if (rc) return rc;
   // the bytes it holds: two more field buffers on the two-step path
   if (c->tb) bytes += 2 * c->h.cells * 4 * store_bytes(c->h.store);
@@ -243,16 +266,26 @@ int add_solo(fdtd2d_batch* b, const fdtd2d_setup* s, int64_t bytes, int32_t* sho
   x.live = true;
   x.done = c->n_steps <= 0;
   x.solo = true;
+  x.seq = b->admitted++;
   b->used += bytes;
   *shot = slot;
   return FDTD2D_OK;
 }
 
-// Issue up to n more steps of every solo member on its own streams (the
-// host does not wait), keeping at most two run calls of each in flight.
+// Issue up to n more steps of the solo_active() oldest unfinished solo
+// members on their own streams (the host does not wait), keeping at most two
+// run calls of each in flight.
 int run_solo(fdtd2d_batch* b, int32_t n) {
-  for (Member& x : b->m) {
-    if (!x.live || !x.solo || x.done) continue;
+  // the solo_active() oldest unfinished solo members
+  std::vector<std::pair<int64_t, int>> order;
+  for (int k = 0; k < (int)b->m.size(); ++k) {
+    const Member& x = b->m[k];
+    if (x.live && x.solo && !x.done) order.push_back({x.seq, k});
+  }
+  std::sort(order.begin(), order.end());
+  if ((int)order.size() > solo_active()) order.resize(solo_active());
+  for (const auto& o : order) {
+    Member& x = b->m[o.second];
     fdtd2d_ctx* c = x.ctx;
     while (x.ev.size() >= 2) {
       const cudaError_t e = cudaEventSynchronize(x.ev.front());

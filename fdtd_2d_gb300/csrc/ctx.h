@@ -48,8 +48,13 @@ struct fdtd2d_ctx {
   // not timed here: forced, or the class's choice was remembered)
   float path_ms = 0.f;
   // how its kernel choices were made: 0 timed at create (or forced), 1 a
-  // choice kept by this process, 2 a choice read from the persisted file
+  // choice kept by this process, 2 a choice read from the persisted file,
+  // 3 a default taken without timing (untimed create)
   int choice_src = 0;
+  // create without timing trials: a class not timed before takes the
+  // default kernel choice (a batch admitting a shot while its device work
+  // is in flight)
+  bool untimed = false;
   // persistent form (step_persist_kernel): many steps per cooperative
   // launch, its own units and barrier word
   bool persist = false;
@@ -90,8 +95,10 @@ namespace fdtd2d {
 // timing, and the batch adopts it (adopt_ctx) once its uploads are done.
 // solo = true makes a batch's solo member, which runs beside the batch's
 // kernel: never the persistent form, whose cooperative launch wants the
-// whole GPU.
-int create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out, bool solo = false);
+// whole GPU.  untimed = true: no create-time timing trials (a class not
+// timed before takes the default kernel choice).
+int create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ctx** out, bool solo = false,
+               bool untimed = false);
 // The checks fdtd2d_create makes on a setup before it allocates anything
 // (FDTD2D_OK, FDTD2D_ERR_INVALID or FDTD2D_ERR_RANGE).
 int validate_setup(const fdtd2d_setup* s);

@@ -237,7 +237,11 @@ const char *fdtd2d_kernel_name(const fdtd2d_ctx *ctx);
    kernel choice (two steps per pass where that wins), stepped from the same
    run calls; its budget share counts that path's two extra field buffers.
    The batch's kernel steps FP32 fields, so a shot with F16 or BF16 storage
-   is a solo member whatever its size. ---- */
+   is a solo member whatever its size.  At most 8 solo members step at a
+   time, the oldest admitted first (FDTD2D_BATCH_SOLO_ACTIVE overrides).  A
+   solo member admitted while the batch has device work in flight is not
+   timed at create: it takes its class's stored kernel choice, else the
+   default one. ---- */
 typedef struct fdtd2d_batch fdtd2d_batch;
 
 /* hbm_budget_bytes <= 0: 90 % of the device memory free now. */
@@ -318,7 +322,9 @@ void fdtd2d_clear_kernel_choices(void);
 /* How the kernel choices of this context's create were made: 0 timed at
    create (or forced by FDTD2D_* overrides), 1 a choice this process kept
    from an earlier shot of the class, 2 a choice read from the persisted
-   file.  No counterpart in the reference. */
+   file, 3 the default choice taken without timing (a batch's solo member
+   admitted while the batch had work in flight).  No counterpart in the
+   reference. */
 int fdtd2d_kernel_choice_source(const fdtd2d_ctx *ctx);
 int fdtd2d_step_kernel_time(fdtd2d_ctx *ctx, double *ms, int64_t *launches, int64_t *cells, int32_t *steps);
 
