@@ -39,6 +39,18 @@ int fail_cuda(fdtd2d_ctx* c, cudaError_t e) {
   return e == cudaErrorMemoryAllocation ? FDTD2D_ERR_NOMEM : FDTD2D_ERR_CUDA;
 }
 
+// The shot's device error word, read in the order of its stream.  The word
+// is allocated and zeroed on that (non-blocking) stream, and kernels on it
+// set it; a plain cudaMemcpy runs on the legacy default stream, which does
+// not wait for a non-blocking stream, and could read memory the pool handed
+// back from a freed shot before the zeroing has run.
+cudaError_t read_err(fdtd2d_ctx* c, int* err) {
+  *err = 0;
+  cudaError_t e = cudaMemcpyAsync(err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return e;
+}
+
 template <class T>
 cudaError_t dalloc(fdtd2d_ctx* c, T** p, size_t count) {
   *p = nullptr;
@@ -769,7 +781,7 @@ int setup_persist(fdtd2d_ctx* c, int device) {
     if (e1) cudaEventDestroy(e1);
     if (e != cudaSuccess) return fail_cuda(c, e);
     int derr = 0;
-    if (cudaMemcpy(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return FDTD2D_ERR_CUDA;
+    if (read_err(c, &derr) != cudaSuccess) return FDTD2D_ERR_CUDA;
     if (derr != kErrNone) return FDTD2D_ERR_TIMEOUT;
     use = ms / 16 < 0.9f * path;
     if (mode < 0) {
@@ -1034,7 +1046,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
     }
   }
   int derr = 0;
-  if (cudaMemcpy(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return FDTD2D_ERR_CUDA;
+  if (read_err(c, &derr) != cudaSuccess) return FDTD2D_ERR_CUDA;
   if (derr != kErrNone) return FDTD2D_ERR_TIMEOUT;
   if (!have) {
     KernelChoice ch;
@@ -1468,7 +1480,7 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
       int derr = 0;
-      CK(cudaMemcpy(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+      CK(read_err(c, &derr));
       if (derr != kErrNone) {
         fdtd2d_destroy(c);
         return FDTD2D_ERR_TIMEOUT;
@@ -1707,9 +1719,8 @@ double fdtd2d_stability(const fdtd2d_setup* s) {
 int fdtd2d_synchronize(fdtd2d_ctx* c) {
   if (!c) return FDTD2D_ERR_INVALID;
   cudaSetDevice(c->device);
-  cudaError_t e = cudaStreamSynchronize(c->stream);
   int err = 0;
-  if (e == cudaSuccess) e = cudaMemcpy(&err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaError_t e = read_err(c, &err);
   if (e != cudaSuccess) return fail_cuda(c, e);
   return err == kErrWaitTimeout ? FDTD2D_ERR_TIMEOUT : (err ? FDTD2D_ERR_CUDA : FDTD2D_OK);
 }

@@ -638,9 +638,19 @@ int retire(fdtd2d_server* s, int* n_done) {
     // A shot whose kernels gave up on a bounded wait has skipped work: its
     // results are not handed out (the batch kernel's error word for its
     // members, a solo member's own one), and the call reports the timeout.
+    // A solo member's word was allocated and zeroed on its own stream
+    // (stream-ordered, from the pool): it is read in that stream's order,
+    // which has completed.  The batch's word comes from cudaMalloc and a
+    // synchronous memset; reading it does not wait for the queued blocks.
     int derr = 0;
-    const int* ew = mem.solo ? c->d_err : b->d_misc + kErr;
-    if (cudaMemcpy(&derr, ew, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return fail(b, cudaGetLastError());
+    cudaError_t re;
+    if (mem.solo) {
+      re = cudaMemcpyAsync(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+      if (re == cudaSuccess) re = cudaStreamSynchronize(c->stream);
+    } else {
+      re = cudaMemcpy(&derr, b->d_misc + kErr, sizeof(int), cudaMemcpyDeviceToHost);
+    }
+    if (re != cudaSuccess) return fail(b, re);
     if (derr) return FDTD2D_ERR_TIMEOUT;
     Finished f;
     f.tag = x.tag;

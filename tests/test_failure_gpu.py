@@ -119,3 +119,26 @@ def test_server_pop_negative_sizes(gpu):
                                  tr.ctypes.data_as(C.POINTER(C.c_float)), -1)
         assert rc == 1 and tag.value == 7
         assert np.all(dft == 123.0) and np.all(tr == 5.0)
+
+
+def test_create_on_recycled_memory(gpu):
+    """Shots created on device memory the pool hands back from freed shots
+    start clean.  Each shot leaves its fields full of large nonzero values
+    before it is freed; the next shot of the same class (kernel choice
+    remembered, so no timing trial synchronises its stream) gets that memory
+    back.  Its error word is zeroed on its own stream and read in that
+    stream's order, so no spurious FDTD2D_ERR_TIMEOUT, and every shot gives
+    the first one's results."""
+    prob = _small(n_steps=20)
+    s = prob.setup
+    first = None
+    for k in range(12):
+        with F.Shot(prob, gpu) as shot:
+            shot.run(1, 20)
+            shot.synchronize()
+            out = (shot.dft(), shot.read_field(F.FIELD_EZ))
+            if first is None:
+                first = out
+            assert np.array_equal(out[0], first[0]) and np.array_equal(out[1], first[1]), k
+            for w in FIELDS:
+                shot.write_field(w, np.full(F.field_shape(w, s.nx, s.ny, s.npml), 3e33, np.float32))
