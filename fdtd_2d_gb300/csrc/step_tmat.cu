@@ -317,85 +317,6 @@ __device__ __forceinline__ float upd_e2(float ca, float e, float cb, float dhy, 
   else return upd_e(ca, e, cb, dhy, dex, dhx, dey, jz);
 }
 
-// ---- four-cell updates of the two-step kernel, packed in pairs for 16-bit
-// storage.  Blackwell's packed FP32 instructions (sub/mul/fma.rn.f32x2) round
-// each element as the scalar .rn instruction does, so a pair update gives
-// the bits of two scalar ones in half the instructions.  The 16-bit kernel,
-// bound by issue, uses them; the FP32 kernel, bound by DRAM, keeps the
-// scalar form (packed measured no faster there).
-using u64 = unsigned long long;
-__device__ __forceinline__ u64 pk2(float a, float b) {
-  u64 r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-  return r;
-}
-__device__ __forceinline__ void up2(u64 v, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v)); }
-__device__ __forceinline__ u64 sub2(u64 a, u64 b) {
-  u64 r;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ u64 mul2(u64 a, u64 b) {
-  u64 r;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ u64 fma2(u64 a, u64 b, u64 c) {
-  u64 r;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-  return r;
-}
-
-// hn[q] = upd_h(da, h[q], db, ea[q], eb[q], den), q = 0..3.
-template <bool kPacked>
-__device__ __forceinline__ void upd_h4(float (&hn)[4], float da, const float (&h)[4], float db, const float (&ea)[4],
-                                       const float (&eb)[4], float den) {
-  if constexpr (kPacked) {
-    const u64 da2 = pk2(da, da), db2 = pk2(db, db), dn2 = pk2(den, den);
-#pragma unroll
-    for (int p = 0; p < 4; p += 2) {
-      const u64 r = fma2(db2, mul2(sub2(pk2(ea[p], ea[p + 1]), pk2(eb[p], eb[p + 1])), dn2),
-                         mul2(da2, pk2(h[p], h[p + 1])));
-      up2(r, hn[p], hn[p + 1]);
-    }
-  } else {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) hn[q] = upd_h(da, h[q], db, ea[q], eb[q], den);
-  }
-}
-
-// jn[q] = upd_j(ja, jz[q], kp[q], e[q]), then en[q] = the Ez update of the
-// kernel's storage (upd_es in stored units for 16-bit storage, upd_e for
-// FP32) with dhy = hy[q] - hyl[q], dhx = hxp[q] - hx[q] and the new Jz.
-template <bool kScaled>
-__device__ __forceinline__ void upd_je4(float (&jn)[4], float (&en)[4], float ja, const float (&jz)[4],
-                                        const float (&kp)[4], const float (&e)[4], float ca, float cb,
-                                        const float (&hy)[4], const float (&hyl)[4], float dex, const float (&hxp)[4],
-                                        const float (&hx)[4], float dey, float rj) {
-  if constexpr (kScaled) {
-    const u64 ja2 = pk2(ja, ja), ca2 = pk2(ca, ca), cb2 = pk2(cb, cb), dx2 = pk2(dex, dex), dy2 = pk2(dey, dey),
-              rj2 = pk2(-rj, -rj);
-#pragma unroll
-    for (int p = 0; p < 4; p += 2) {
-      const u64 e2 = pk2(e[p], e[p + 1]);
-      float t0, t1;
-      up2(fma2(pk2(kp[p], kp[p + 1]), e2, mul2(ja2, pk2(jz[p], jz[p + 1]))), t0, t1);
-      jn[p] = kp[p] != 0.f ? t0 : jz[p];            // upd_j: plasma cells only
-      jn[p + 1] = kp[p + 1] != 0.f ? t1 : jz[p + 1];
-      const u64 dhy = sub2(pk2(hy[p], hy[p + 1]), pk2(hyl[p], hyl[p + 1]));
-      const u64 dhx = sub2(pk2(hxp[p], hxp[p + 1]), pk2(hx[p], hx[p + 1]));
-      const u64 curl = fma2(rj2, pk2(jn[p], jn[p + 1]), fma2(dhy, dx2, mul2(dhx, dy2)));
-      up2(fma2(cb2, curl, mul2(ca2, e2)), en[p], en[p + 1]);
-    }
-  } else {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      jn[q] = upd_j(ja, jz[q], kp[q], e[q]);
-      en[q] = upd_e(ca, e[q], cb, __fsub_rn(hy[q], hyl[q]), dex, __fsub_rn(hxp[q], hx[q]), dey, jn[q]);
-    }
-  }
-}
-
 template <bool kScaled>
 __device__ __forceinline__ void pts2(const DevShot& S, int p0, int p1, int i, int n, bool rec, float (&ez)[4],
                                      const float (&hx)[4], const float (&hy)[4], int xc, float& ezx) {
@@ -590,11 +511,13 @@ __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const in
 
       // ---- step n, row j
       float hxn[4], hyn[4], jzn[4], ezs_n[4];
-      upd_h4<kScaled>(hxn, da, hxo, db, ezc, ezn, dhy);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) hxn[q] = upd_h(da, hxo[q], db, ezc[q], ezn[q], dhy);
       float ezr_k = __shfl_down_sync(0xffffffffu, ezc[0], 1);
       if (lane == 31) ezr_k = e_0;
       const float ezr4[4] = {ezc[1], ezc[2], ezc[3], ezr_k};
-      upd_h4<kScaled>(hyn, da, hyo, db, ezr4, ezc, dhx);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) hyn[q] = upd_h(da, hyo[q], db, ezr4[q], ezc[q], dhx);
       // edge column: Hy at xc-1 and xc, then Hx, Jz, Ez at xc
       const float hyA = upd_h(da, hyoA, db, e_0, e_m, dhx);
       const float hyB = upd_h(da, hyoB, db, e_p, e_0, dhx);
@@ -604,7 +527,11 @@ __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const in
       const float jzE = upd_j(ja, jzoE, kpE, e_0);
       float ezE = upd_e2<kScaled>(ca, e_0, cb, __fsub_rn(hyB, hyA), dex, __fsub_rn(hxe_p, hxE), dey, jzE, rj);
       const float hyl4[4] = {hyl, hyn[0], hyn[1], hyn[2]};
-      upd_je4<kScaled>(jzn, ezs_n, ja, jzo, kp, ezc, ca, cb, hyn, hyl4, dex, hxp, hxn, dey, rj);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        jzn[q] = upd_j(ja, jzo[q], kp[q], ezc[q]);
+        ezs_n[q] = upd_e2<kScaled>(ca, ezc[q], cb, __fsub_rn(hyn[q], hyl4[q]), dex, __fsub_rn(hxp[q], hxn[q]), dey, jzn[q], rj);
+      }
       const bool own = j >= j0 && j < j1;
       pts2<kScaled>(S, p0, p1, i, n, own, ezs_n, hxn, hyn, xc, ezE);
       if (own) {
@@ -635,18 +562,25 @@ __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const in
       St::rt4(jzs, jzn);
       if (j > jb) {
         float hx2[4];
-        upd_h4<kScaled>(hx2, da, hx1, db, ez1, ezs, dhy);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) hx2[q] = upd_h(da, hx1[q], db, ez1[q], ezs[q], dhy);
         if (j > j0) {
           float rk = __shfl_down_sync(0xffffffffu, ez1[0], 1);
           if (lane == 31) rk = eze1;
           const float er4[4] = {ez1[1], ez1[2], ez1[3], rk};
           float hy2[4];
-          upd_h4<kScaled>(hy2, da, hy1, db, er4, ez1, dhx);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) hy2[q] = upd_h(da, hy1[q], db, er4[q], ez1[q], dhx);
           float hl = __shfl_up_sync(0xffffffffu, hy2[3], 1);
           if (lane == 0) hl = upd_h(da, hye1, db, ez1[0], eze1, dhx);
           const float hl4[4] = {hl, hy2[0], hy2[1], hy2[2]};
           float ez2[4], jz2[4];
-          upd_je4<kScaled>(jz2, ez2, ja, jz1, kp1, ez1, ca, cb, hy2, hl4, dex, hx2p, hx2, dey, rj);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            jz2[q] = upd_j(ja, jz1[q], kp1[q], ez1[q]);
+            ez2[q] = upd_e2<kScaled>(ca, ez1[q], cb, __fsub_rn(hy2[q], hl4[q]), dex, __fsub_rn(hx2p[q], hx2[q]), dey,
+                            jz2[q], rj);
+          }
           float unused = 0.f;
           pts2<kScaled>(S, q0, q1, i, n + 1, true, ez2, hx2, hy2, -1, unused);
           const int64_t o = (int64_t)(j - 1) * pitch + i;
