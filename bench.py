@@ -308,8 +308,8 @@ def run_batched(args, local: int) -> tuple[dict, float]:
            "note": "end to end from host setups: create/upload, all steps, traces + DFT read back; kernel "
                    "choices of every size class timed once before both passes. plain: one shot at a time "
                    "through the single-shot ABI; batch: grids of >= 2^21 cells as solo members (own "
-                   "streams, two-step tensor path, stream priority by size), the rest in one persistent "
-                   "launch per step in CUDA-graph blocks of 16"}
+                   "streams, two-step tensor path, at most 8 stepping at a time), the rest in one "
+                   "persistent launch per step in CUDA-graph blocks of 16"}
     if args.batch_storage != "f32":
         store = {"f16": F.STORE_F16, "bf16": F.STORE_BF16}[args.batch_storage]
         probs16 = [F.Problem.from_spec(**sp, storage=store) for sp in specs]
