@@ -177,6 +177,9 @@ def _lib():
         "fdtd2d_time_step_kernel": (C.c_int, [vp, C.c_int]),
         "fdtd2d_clear_kernel_choices": (None, []),
         "fdtd2d_kernel_choice_source": (C.c_int, [vp]),
+        "fdtd2d_state_bytes": (C.c_int64, [vp]),
+        "fdtd2d_save_state": (C.c_int, [vp, vp, C.c_int64]),
+        "fdtd2d_load_state": (C.c_int, [vp, vp, C.c_int64]),
         "fdtd2d_step_kernel_time": (C.c_int, [vp, _dp, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                               C.POINTER(C.c_int32)]),
         "fdtd2d_stability": (C.c_double, [C.POINTER(Setup)]),
@@ -375,6 +378,21 @@ class Shot:
     def kernel_name(self) -> str:
         """The step kernel this shot launches, with its launch shape."""
         return _lib().fdtd2d_kernel_name(self._h).decode()
+
+    def save_state(self) -> np.ndarray:
+        """Host image of the shot's state after its last step (fdtd2d_save_state)."""
+        n = int(_lib().fdtd2d_state_bytes(self._h))
+        if n < 0:
+            raise FdtdError(n, "fdtd2d_state_bytes")
+        buf = np.empty(n, np.uint8)
+        _check(_lib().fdtd2d_save_state(self._h, buf.ctypes.data, n), "fdtd2d_save_state")
+        return buf
+
+    def load_state(self, image: np.ndarray) -> None:
+        """Continue from a saved image (fdtd2d_load_state): the next run call
+        starts at the saved step + 1."""
+        img = np.ascontiguousarray(image, np.uint8)
+        _check(_lib().fdtd2d_load_state(self._h, img.ctypes.data, img.size), "fdtd2d_load_state")
 
     def choice_source(self) -> int:
         """How its kernel choices were made: 0 timed at create (or forced), 1

@@ -51,10 +51,18 @@ cudaError_t read_err(fdtd2d_ctx* c, int* err) {
   return e;
 }
 
+// Test parameter FDTD2D_TEST_FAIL_ALLOC=k (read at create): the k-th device
+// allocation a context makes reports cudaErrorMemoryAllocation without
+// allocating, so a test can walk every allocation of fdtd2d_create and check
+// that each failure comes back as FDTD2D_ERR_NOMEM with the context's other
+// memory released, or, where the library has a smaller form to fall back to
+// (the two-step path's extra buffers), that the shot still runs.  Normal runs
+// leave it unset.
 template <class T>
 cudaError_t dalloc(fdtd2d_ctx* c, T** p, size_t count) {
   *p = nullptr;
   if (count == 0) return cudaSuccess;
+  if (c->fail_alloc > 0 && ++c->n_alloc == c->fail_alloc) return cudaErrorMemoryAllocation;
   void* q = nullptr;
   // Stream-ordered allocation from the device's pool: a shot's memory is
   // released with cudaFreeAsync behind its last kernel, so retiring a batch
@@ -1115,6 +1123,7 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
   if (!c) return FDTD2D_ERR_NOMEM;
   c->device = device;
   c->untimed = untimed;
+  if (const char* v = std::getenv("FDTD2D_TEST_FAIL_ALLOC")) c->fail_alloc = std::atoi(v);
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) keep_pool_memory(device);
@@ -1921,8 +1930,10 @@ int write_field16(fdtd2d_ctx* c, int which, const float* host) {
     if (!view16(c, which, b, &v)) return FDTD2D_ERR_INVALID;
     std::vector<uint16_t> buf((size_t)v.rows * v.cols);
     for (size_t t = 0; t < buf.size(); ++t) buf[t] = to16(host[t] * v.isc, c->h.store);
-    e = cudaMemcpy2D(const_cast<uint16_t*>(v.base), (size_t)c->pitch * 2, buf.data(), (size_t)v.cols * 2,
-                     (size_t)v.cols * 2, v.rows, cudaMemcpyHostToDevice);
+    // in the shot stream's order, finished before the host buffer goes away
+    e = cudaMemcpy2DAsync(const_cast<uint16_t*>(v.base), (size_t)c->pitch * 2, buf.data(), (size_t)v.cols * 2,
+                          (size_t)v.cols * 2, v.rows, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   }
   if (e != cudaSuccess) return fail_cuda(c, e);
   return FDTD2D_OK;
@@ -1956,11 +1967,162 @@ int fdtd2d_write_field(fdtd2d_ctx* c, int which, const float* host) {
     if (which > FDTD2D_FIELD_JZ && b >= 2) break;   // psi: two buffers
     FieldView v;
     if (!field_view(c, which, b, &v)) return FDTD2D_ERR_INVALID;
-    e = cudaMemcpy2D(v.base, v.dpitch * 4, host, v.hpitch * 4, (size_t)v.cols * 4, v.rows,
-                     cudaMemcpyHostToDevice);
+    // In the shot stream's order: a plain cudaMemcpy2D from pageable memory
+    // may return before its DMA has landed, and the shot's kernels run on a
+    // non-blocking stream that would not wait for it.
+    e = cudaMemcpy2DAsync(v.base, v.dpitch * 4, host, v.hpitch * 4, (size_t)v.cols * 4, v.rows,
+                          cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   }
   if (e != cudaSuccess) return fail_cuda(c, e);
   return FDTD2D_OK;
+}
+
+// ---- Snapshot and restore of a shot's state ----------------------------------
+//
+// Host image layout: a StateHeader, then the twelve field arrays of
+// fdtd2d_read_field in FDTD2D_FIELD_* order (reference layouts, FP32 values;
+// 16-bit storage round-trips exactly, every stored value being an FP32 value
+// times a power of two), then the FP64 DFT sums (re, im per detector), the
+// detector traces of every step ([n_steps][n_det] and [n_steps][n_comp][3]),
+// the wave-front tracker's edge levels and rows ([n_rc], [n_steps][n_rc]) and
+// the line-probe rows, each present when the setup has it.
+
+namespace {
+
+struct StateHeader {
+  uint32_t magic, version;
+  int32_t nx, ny, npml, n_steps, store, step;
+  int32_t n_det, n_comp, record, dft, n_rc, line_n, line_first, line_last;
+  int64_t bytes;
+};
+constexpr uint32_t kStateMagic = 0x31534446u;   // "FDS1"
+
+int64_t field_count(const fdtd2d_ctx* c, int which) {
+  const int64_t nx = c->nx, ny = c->ny, P = c->npml;
+  switch (which) {
+    case FDTD2D_FIELD_EZ: case FDTD2D_FIELD_JZ: return nx * ny;
+    case FDTD2D_FIELD_HX: return (ny - 1) * nx;
+    case FDTD2D_FIELD_HY: return ny * (nx - 1);
+    case FDTD2D_FIELD_PSI_EZX_1: case FDTD2D_FIELD_PSI_EZX_2: return ny * P;
+    case FDTD2D_FIELD_PSI_EZY_1: case FDTD2D_FIELD_PSI_EZY_2: return P * nx;
+    case FDTD2D_FIELD_PSI_HYX_1: case FDTD2D_FIELD_PSI_HYX_2: return ny * (P - 1);
+    default: return (P - 1) * nx;   // FDTD2D_FIELD_PSI_HXY_1/_2
+  }
+}
+
+// The device arrays after the fields, as (device pointer, bytes) in image order.
+std::vector<std::pair<void*, size_t>> state_blocks(fdtd2d_ctx* c) {
+  std::vector<std::pair<void*, size_t>> b;
+  if (c->dft) b.push_back({c->h.dft, (size_t)c->n_det * sizeof(double2)});
+  if (c->record) {
+    b.push_back({c->h.trace, (size_t)c->n_steps * c->n_det * sizeof(float)});
+    b.push_back({c->h.ctrace, (size_t)c->n_steps * c->n_comp * 3 * sizeof(float)});
+  }
+  if (c->n_rc > 0) {
+    b.push_back({c->d_edge, (size_t)c->n_rc * sizeof(float)});
+    b.push_back({c->d_spd, (size_t)c->n_steps * c->n_rc * sizeof(int)});
+  }
+  if (c->line_n > 0)
+    b.push_back({c->d_line, (size_t)(c->line_last - c->line_first + 1) * c->line_n * sizeof(float)});
+  return b;
+}
+
+StateHeader state_header(fdtd2d_ctx* c) {
+  StateHeader h{};
+  h.magic = kStateMagic;
+  h.version = 1;
+  h.nx = c->nx; h.ny = c->ny; h.npml = c->npml; h.n_steps = c->n_steps; h.store = c->h.store;
+  h.step = c->step;
+  h.n_det = c->n_det; h.n_comp = c->n_comp; h.record = c->record; h.dft = c->dft ? 1 : 0;
+  h.n_rc = c->n_rc; h.line_n = c->line_n; h.line_first = c->line_first; h.line_last = c->line_last;
+  int64_t n = sizeof(StateHeader);
+  for (int w = 0; w <= FDTD2D_FIELD_PSI_HXY_2; ++w) n += field_count(c, w) * 4;
+  for (const auto& blk : state_blocks(c)) n += (int64_t)blk.second;
+  h.bytes = n;
+  return h;
+}
+
+// Every kernel of the shot, on both of its streams, has finished.
+cudaError_t quiesce(fdtd2d_ctx* c) {
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess && c->side) e = cudaStreamSynchronize(c->side);
+  return e;
+}
+
+int save_state_body(fdtd2d_ctx* c, void* buf, int64_t bytes) {
+  if (!c || !buf) return FDTD2D_ERR_INVALID;
+  const StateHeader h = state_header(c);
+  if (bytes < h.bytes) return FDTD2D_ERR_RANGE;
+  cudaSetDevice(c->device);
+  cudaError_t e = quiesce(c);
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  char* p = static_cast<char*>(buf);
+  std::memcpy(p, &h, sizeof h);
+  p += sizeof h;
+  for (int w = 0; w <= FDTD2D_FIELD_PSI_HXY_2; ++w) {
+    const int rc = fdtd2d_read_field(c, w, reinterpret_cast<float*>(p));
+    if (rc) return rc;
+    p += field_count(c, w) * 4;
+  }
+  for (const auto& blk : state_blocks(c)) {
+    e = cudaMemcpyAsync(p, blk.first, blk.second, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return fail_cuda(c, e);
+    p += blk.second;
+  }
+  return FDTD2D_OK;
+}
+
+int load_state_body(fdtd2d_ctx* c, const void* buf, int64_t bytes) {
+  if (!c || !buf) return FDTD2D_ERR_INVALID;
+  if (c->batch) return FDTD2D_ERR_STATE;   // a batch member's step is the batch's
+  const StateHeader want = state_header(c);
+  StateHeader h;
+  if (bytes < (int64_t)sizeof h) return FDTD2D_ERR_RANGE;
+  std::memcpy(&h, buf, sizeof h);
+  if (h.magic != kStateMagic || h.version != 1) return FDTD2D_ERR_INVALID;
+  // the same shot geometry, storage, detectors and probes, a step it can be at
+  if (h.nx != want.nx || h.ny != want.ny || h.npml != want.npml || h.n_steps != want.n_steps ||
+      h.store != want.store || h.n_det != want.n_det || h.n_comp != want.n_comp || h.record != want.record ||
+      h.dft != want.dft || h.n_rc != want.n_rc || h.line_n != want.line_n || h.line_first != want.line_first ||
+      h.line_last != want.line_last || h.bytes != want.bytes || h.step < 0 || h.step > h.n_steps)
+    return FDTD2D_ERR_INVALID;
+  if (bytes < h.bytes) return FDTD2D_ERR_RANGE;
+  cudaSetDevice(c->device);
+  cudaError_t e = quiesce(c);
+  if (e != cudaSuccess) return fail_cuda(c, e);
+  // the fields go into every buffer of the shot (fdtd2d_write_field), so the
+  // state is in place whatever slot the next step reads
+  c->step = h.step;
+  const char* p = static_cast<const char*>(buf) + sizeof h;
+  for (int w = 0; w <= FDTD2D_FIELD_PSI_HXY_2; ++w) {
+    const int rc = fdtd2d_write_field(c, w, reinterpret_cast<const float*>(p));
+    if (rc) return rc;
+    p += field_count(c, w) * 4;
+  }
+  for (const auto& blk : state_blocks(c)) {
+    e = cudaMemcpyAsync(blk.first, p, blk.second, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return fail_cuda(c, e);
+    p += blk.second;
+  }
+  return FDTD2D_OK;
+}
+
+}  // namespace
+
+int64_t fdtd2d_state_bytes(fdtd2d_ctx* c) {
+  if (!c) return FDTD2D_ERR_INVALID;
+  return state_header(c).bytes;
+}
+
+int fdtd2d_save_state(fdtd2d_ctx* c, void* buf, int64_t bytes) {
+  return abi_guard([&] { return save_state_body(c, buf, bytes); });
+}
+
+int fdtd2d_load_state(fdtd2d_ctx* c, const void* buf, int64_t bytes) {
+  return abi_guard([&] { return load_state_body(c, buf, bytes); });
 }
 
 int fdtd2d_check_finite(fdtd2d_ctx* c) {

@@ -88,6 +88,8 @@ struct fdtd2d_ctx {
   int line_n = 0, line_i0 = 0, line_j = 0, line_first = 0, line_last = -1;
   float* d_line = nullptr;
   std::vector<void*> allocs;
+  // test parameter: the fail_alloc-th device allocation fails (0: none)
+  int fail_alloc = 0, n_alloc = 0;
 };
 
 namespace fdtd2d {

@@ -192,6 +192,23 @@ int fdtd2d_read_dft(fdtd2d_ctx *ctx, double *re, double *im);
 int fdtd2d_read_field(fdtd2d_ctx *ctx, int which, float *host);
 int fdtd2d_write_field(fdtd2d_ctx *ctx, int which, const float *host);
 
+/* Snapshot and restore of a shot's state after its last step, for preempting
+   a long shot and resuming it later, here or in another process: the fields
+   and CPML psi arrays (reference layouts), the FP64 DFT sums, the detector
+   traces recorded so far, the wave-front tracker's and the line probe's
+   state, and the step number.  fdtd2d_state_bytes gives the size of the host
+   image; fdtd2d_save_state writes it (FDTD2D_ERR_RANGE if `bytes` is
+   smaller); fdtd2d_load_state makes a context created from the same setup
+   continue from it: its next run call starts at the saved step + 1 and gives
+   the bits the shot would have given without the stop.  An image of another
+   geometry, storage or detector set is FDTD2D_ERR_INVALID; a batch member is
+   FDTD2D_ERR_STATE.  Both wait for the shot's queued work.  No counterpart in
+   the reference (its field dumps, FDTD_2D_Full/kernel.cu:2173-2303, cannot
+   be restarted from). */
+int64_t fdtd2d_state_bytes(fdtd2d_ctx *ctx);
+int fdtd2d_save_state(fdtd2d_ctx *ctx, void *buf, int64_t bytes);
+int fdtd2d_load_state(fdtd2d_ctx *ctx, const void *buf, int64_t bytes);
+
 /* Device-side scan for NaN/Inf in Ez/Hx/Hy/Jz; FDTD2D_ERR_NONFINITE if any. */
 int fdtd2d_check_finite(fdtd2d_ctx *ctx);
 

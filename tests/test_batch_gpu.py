@@ -224,3 +224,31 @@ def test_serving_with_solo_members(gpu, monkeypatch):
     for k, (dft, tr) in enumerate(solo):
         assert np.array_equal(got[k]["dft"], dft), k
         assert np.array_equal(got[k]["det_ez"], tr), k
+
+
+def test_batch_kernel_members_of_mixed_sample_size(gpu):
+    """Members of the mixed-shot sample's size range that stay on the batch
+    kernel (sides 1024..2040, below the 2^21-cell solo threshold, aspect up
+    to 1:2, CPML 16..32, dx = lambda/20): each equals its solo run bitwise,
+    with a small shot beside them."""
+    specs = []
+    for k, (nx, ny, P, f) in enumerate(((1024, 1536, 16, 30e9), (2040, 1024, 32, 55e9), (1100, 1100, 24, 75e9))):
+        assert nx * ny < 1 << 21
+        dx = 299792458.0 / f / 20
+        specs.append(dict(nx=nx, ny=ny, npml=P, n_steps=120 + 17 * k, dx=dx, dy=dx, courant=0.95, profile=2,
+                          ne_peak=2e19, x_center=0.6 * nx, width=0.1 * nx, nu=2e9, n_elem=8, src_i=P + 32,
+                          src_j=ny // 2 - 20, src_di=0, src_dj=5, freq=f, steer_deg=15, pulse=1,
+                          pulse_width=0.1e-9, n_det=8, det_i=P + 32, det_j=ny // 2 - 20, det_di=0, det_dj=5,
+                          dft_freq=f))
+    probs = [F.Problem.from_spec(**sp) for sp in specs] + problems(1)
+    ref = [alone(p, gpu) for p in probs]
+    with F.Batch(gpu) as b:
+        ids = [b.add(p) for p in probs]
+        assert all(i is not None for i in ids)
+        while not all(b.finished(i) for i in ids):
+            b.run(40)
+        b.synchronize()
+        for k, i in enumerate(ids):
+            sh = b.shot(i)
+            assert not sh.kernel_name().startswith("step_tmat"), "a batch-kernel member"
+            assert_same(ref[k], snapshot(sh), f"member {k}")

@@ -142,3 +142,61 @@ def test_create_on_recycled_memory(gpu):
             assert np.array_equal(out[0], first[0]) and np.array_equal(out[1], first[1]), k
             for w in FIELDS:
                 shot.write_field(w, np.full(F.field_shape(w, s.nx, s.ny, s.npml), 3e33, np.float32))
+
+
+def _pool_used_bytes(device):
+    """Bytes in use in the device's default memory pool (cudaMemPoolAttrUsedMemCurrent),
+    through the CUDA runtime library, or None where it cannot be loaded."""
+    import ctypes.util
+
+    for name in ("libcudart.so.13", "libcudart.so", ctypes.util.find_library("cudart") or ""):
+        try:
+            rt = C.CDLL(name)
+            break
+        except OSError:
+            continue
+    else:
+        return None
+    pool = C.c_void_p()
+    if rt.cudaDeviceGetDefaultMemPool(C.byref(pool), device) != 0:
+        return None
+    used = C.c_uint64()
+    if rt.cudaMemPoolGetAttribute(pool, 7, C.byref(used)) != 0:   # cudaMemPoolAttrUsedMemCurrent
+        return None
+    return used.value
+
+
+def test_allocation_failures_in_create(gpu, monkeypatch):
+    """Each device allocation fdtd2d_create makes fails in turn (a test
+    parameter read at create makes the k-th report cudaErrorMemoryAllocation
+    without allocating).  Every failure returns FDTD2D_ERR_NOMEM and gives
+    back what the shot had allocated (the pool's bytes in use return to where
+    they were), except where the library has a smaller form to fall back to:
+    the two-step path's extra buffers, whose failure leaves a shot on the
+    one-step path with the same results.  Past the last allocation the shot
+    is created as usual."""
+    prob = F.Problem.from_spec(nx=1400, ny=260, npml=16, n_steps=24, src_i=300, src_j=100, det_i=302,
+                               det_j=100, x_lo=700, x_hi=1380)
+    with F.Shot(prob, gpu) as s:
+        s.run(1, 24)
+        ref = s.dft()
+    base = _pool_used_bytes(gpu)
+    nomem = in_a_row = 0
+    for k in range(1, 300):
+        monkeypatch.setenv("FDTD2D_TEST_FAIL_ALLOC", str(k))
+        try:
+            shot = F.Shot(prob, gpu)
+        except F.FdtdError as e:
+            assert e.status == F.ERR_NOMEM, (k, e)
+            nomem += 1
+            in_a_row = 0
+            if base is not None:
+                assert _pool_used_bytes(gpu) == base, k
+            continue
+        with shot:
+            shot.run(1, 24)
+            assert np.array_equal(shot.dft(), ref), k
+        in_a_row += 1
+        if in_a_row == 3:   # past the last allocation of create
+            break
+    assert in_a_row == 3 and nomem >= 8, (nomem, k)
