@@ -1122,6 +1122,7 @@ int fdtd2d::create_ctx(const fdtd2d_setup* s, int device, bool member, fdtd2d_ct
   fdtd2d_ctx* c = new (std::nothrow) fdtd2d_ctx();
   if (!c) return FDTD2D_ERR_NOMEM;
   c->device = device;
+  c->solo = solo;
   c->untimed = untimed;
   if (const char* v = std::getenv("FDTD2D_TEST_FAIL_ALLOC")) c->fail_alloc = std::atoi(v);
   cudaError_t e = cudaSetDevice(device);
@@ -2076,7 +2077,7 @@ int save_state_body(fdtd2d_ctx* c, void* buf, int64_t bytes) {
 
 int load_state_body(fdtd2d_ctx* c, const void* buf, int64_t bytes) {
   if (!c || !buf) return FDTD2D_ERR_INVALID;
-  if (c->batch) return FDTD2D_ERR_STATE;   // a batch member's step is the batch's
+  if (c->batch || c->solo) return FDTD2D_ERR_STATE;   // a batch member's step is the batch's
   const StateHeader want = state_header(c);
   StateHeader h;
   if (bytes < (int64_t)sizeof h) return FDTD2D_ERR_RANGE;

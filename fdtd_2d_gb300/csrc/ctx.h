@@ -17,6 +17,7 @@ struct fdtd2d_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool batch = false;       // member of a batch: stream borrowed, stepped by the batch
+  bool solo = false;        // a batch's solo member: own streams, stepped from the batch's run calls
   int nx = 0, ny = 0, pitch = 0, npml = 0, n_steps = 0;
   int n_det = 0, n_comp = 0, record = 0, medium = 0;
   bool dft = false;

@@ -95,3 +95,21 @@ def test_load_refuses_another_shot(gpu):
         with pytest.raises(F.FdtdError) as e:
             sb.load_state(image[:64])
         assert e.value.status in (F.ERR_RANGE, F.ERR_INVALID)
+
+
+def test_load_refuses_batch_members(gpu):
+    """A batch steps its members itself (the batch kernel's members and the
+    solo members alike): loading a state into one is FDTD2D_ERR_STATE."""
+    small = F.Problem.from_spec(nx=256, ny=192, n_steps=40, src_i=30, src_j=96, det_i=34, det_j=96)
+    big = F.Problem.from_spec(nx=1600, ny=1400, n_steps=40, src_i=40, src_j=700, det_i=42, det_j=700)
+    images = []
+    for p in (small, big):
+        with F.Shot(p, gpu) as s:
+            s.run(1, 10)
+            images.append(s.save_state())
+    with F.Batch(gpu) as b:
+        ids = [b.add(small), b.add(big)]   # the large one (2.24 M cells) joins as a solo member
+        for i, image in zip(ids, images):
+            with pytest.raises(F.FdtdError) as e:
+                b.shot(i).load_state(image)
+            assert e.value.status == F.ERR_STATE
