@@ -177,6 +177,7 @@ def _lib():
         "fdtd2d_time_step_kernel": (C.c_int, [vp, C.c_int]),
         "fdtd2d_clear_kernel_choices": (None, []),
         "fdtd2d_kernel_choice_source": (C.c_int, [vp]),
+        "fdtd2d_server_cancel": (C.c_int, [vp, C.c_int64]),
         "fdtd2d_state_bytes": (C.c_int64, [vp]),
         "fdtd2d_save_state": (C.c_int, [vp, vp, C.c_int64]),
         "fdtd2d_load_state": (C.c_int, [vp, vp, C.c_int64]),
@@ -563,6 +564,15 @@ class Server:
         if rc < 0:
             raise FdtdError(rc, "fdtd2d_server_step")
         return rc
+
+    def cancel(self, tag: int) -> int:
+        """Cancel the shots submitted under `tag` (fdtd2d_server_cancel);
+        returns how many were cancelled."""
+        n = _lib().fdtd2d_server_cancel(self._h, tag)
+        if n < 0:
+            raise FdtdError(n, "fdtd2d_server_cancel")
+        self._held.pop(tag, None)
+        return int(n)
 
     def counts(self) -> tuple[int, int, int]:
         q, r, f = C.c_int32(), C.c_int32(), C.c_int32()

@@ -829,6 +829,51 @@ int fdtd2d_server_pop(fdtd2d_server* s, int64_t* tag, int32_t* n_det, int32_t* n
   return 1;
 }
 
+static int fdtd2d_server_cancel_body(fdtd2d_server* s, int64_t tag);
+
+// The entry point: its body, below, runs behind abi_guard.
+int fdtd2d_server_cancel(fdtd2d_server* s, int64_t tag) {
+  return abi_guard([&] { return fdtd2d_server_cancel_body(s, tag); });
+}
+
+// Queued shots of the tag leave the queue; running ones are removed from the
+// batch (a batch-kernel member's memory is released behind the blocks already
+// queued for it, which the batch's stream orders before any reuse, and the
+// unit list is rebuilt before the next block; a solo member waits for its own
+// streams); finished ones not yet popped are dropped.
+static int fdtd2d_server_cancel_body(fdtd2d_server* s, int64_t tag) {
+  if (!s) return FDTD2D_ERR_INVALID;
+  cudaSetDevice(s->b->device);
+  int n = 0;
+  for (size_t q = 0; q < s->queue.size();) {
+    if (s->queue[q].tag == tag) {
+      s->queue.erase(s->queue.begin() + q);
+      ++n;
+    } else {
+      ++q;
+    }
+  }
+  for (size_t r = 0; r < s->running.size();) {
+    if (s->running[r].tag != tag) {
+      ++r;
+      continue;
+    }
+    const int rc = fdtd2d_batch_remove(s->b, s->running[r].slot);
+    if (rc) return rc;
+    s->running.erase(s->running.begin() + r);
+    ++n;
+  }
+  for (size_t f = 0; f < s->finished.size();) {
+    if (s->finished[f].tag == tag) {
+      s->finished.erase(s->finished.begin() + f);
+      ++n;
+    } else {
+      ++f;
+    }
+  }
+  return n;
+}
+
 int fdtd2d_server_counts(const fdtd2d_server* s, int32_t* queued, int32_t* running, int32_t* finished) {
   if (!s) return FDTD2D_ERR_INVALID;
   if (queued) *queued = (int32_t)s->queue.size();

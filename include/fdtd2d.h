@@ -305,6 +305,12 @@ int fdtd2d_server_step(fdtd2d_server *s);
 int fdtd2d_server_pop(fdtd2d_server *s, int64_t *tag, int32_t *n_det, int32_t *n_steps, double *dft,
                       int32_t max_det, float *trace, int64_t max_trace);
 int fdtd2d_server_counts(const fdtd2d_server *s, int32_t *queued, int32_t *running, int32_t *finished);
+/* Cancel the shots submitted under `tag`, wherever they are: queued ones
+   leave the queue, running ones stop being stepped and their device memory
+   is released (behind the kernels already queued for them), finished ones
+   not yet popped are dropped.  No result of a cancelled shot is popped.
+   Returns the number of shots cancelled (0 if none had the tag). */
+int fdtd2d_server_cancel(fdtd2d_server *s, int64_t tag);
 fdtd2d_batch *fdtd2d_server_batch(fdtd2d_server *s);
 int fdtd2d_server_destroy(fdtd2d_server *s);
 

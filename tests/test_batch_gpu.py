@@ -252,3 +252,48 @@ def test_batch_kernel_members_of_mixed_sample_size(gpu):
             sh = b.shot(i)
             assert not sh.kernel_name().startswith("step_tmat"), "a batch-kernel member"
             assert_same(ref[k], snapshot(sh), f"member {k}")
+
+
+def test_server_cancel(gpu):
+    """fdtd2d_server_cancel: a running batch-kernel member and a running solo
+    member cancelled mid-flight stop and never pop; a queued shot cancelled
+    before admission never runs; the others finish equal to their solo runs."""
+    probs = problems(4)
+    big = F.Problem.from_spec(nx=1600, ny=1400, n_steps=200, src_i=40, src_j=700, det_i=42, det_j=700,
+                              dft_freq=30e9)
+    ref = {k: alone(probs[k], gpu)["dft"] for k in (0, 2, 3)}
+    with F.Server(gpu, block_steps=16) as srv:
+        for k, p in enumerate(probs):
+            srv.submit(p, k)
+        srv.submit(big, 10)
+        srv.step()
+        srv.step()
+        assert srv.counts()[1] == 5            # all admitted and running
+        assert srv.cancel(1) == 1              # a batch-kernel member
+        assert srv.cancel(10) == 1             # the solo member
+        assert srv.cancel(99) == 0
+        got = {}
+        for _ in range(100000):
+            srv.step()
+            while (r := srv.pop()) is not None:
+                got[r["tag"]] = r["dft"]
+            if srv.counts() == (0, 0, 0):
+                break
+        assert sorted(got) == [0, 2, 3]
+        for k in got:
+            assert np.array_equal(got[k], ref[k]), k
+    # a queued shot: the budget holds one shot at a time
+    with F.Server(gpu, budget_bytes=probs[0].device_bytes() + 1024, block_steps=16) as srv:
+        srv.submit(probs[0], 0)
+        srv.submit(probs[0], 5)
+        srv.step()
+        assert srv.counts()[:2] == (1, 1)
+        assert srv.cancel(5) == 1
+        got = []
+        for _ in range(100000):
+            srv.step()
+            while (r := srv.pop()) is not None:
+                got.append(r["tag"])
+            if srv.counts() == (0, 0, 0):
+                break
+        assert got == [0]
