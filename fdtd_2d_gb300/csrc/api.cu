@@ -201,7 +201,10 @@ std::vector<int4> edge_units(int nx, int ny, int P, int ci0, int ci1, int ri0, i
   double total = 0;
   for (const Seg& g : segs) total += std::max(0, g.j1 - g.j0) * g.w;
   const int slots = std::max(1, ctas - (int)segs.size());   // room for every band's rounding up
-  const double per = std::max(4.0, total / slots);
+  // No floor above one row: at 1024^2 a floor of four rows held the whole
+  // path to 72.4 Gcell/s against 81.6 with one; from 2048^2 up the floor
+  // does not bind.
+  const double per = std::max(1.0, total / slots);
   std::vector<int4> u;
   for (const Seg& g : segs) {
     const int r = g.j1 - g.j0;
