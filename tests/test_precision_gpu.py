@@ -34,7 +34,9 @@ def array_shot(storage: int, **kw):
 
 
 @pytest.mark.parametrize("storage", [F.STORE_F16, F.STORE_BF16])
-def test_reduced_storage_against_oracle(gpu, storage):
+def test_reduced_storage_against_oracle(gpu, storage, monkeypatch):
+    # the one-row kernel (the two-step case is below)
+    monkeypatch.setenv("FDTD2D_TMAT", "0")
     prob = array_shot(storage)
     ref = O.Oracle(prob.setup_ptr)
     ref.run(1, prob.n_steps)
