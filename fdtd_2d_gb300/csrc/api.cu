@@ -427,7 +427,8 @@ struct PairPlan {
 // interior pass reads outside R).  Side stream: the band kernel's step n,
 // then, once the interior kernel is done, its step n+1, which so runs beside
 // the next pair's interior kernel.  Slots: state n-1 in a = (n-1)&1, state n
-// (band cells and R's ring) into b = n&1, state n+1 into slot 2; slot 3 holds
+// (band cells, and R's edge cells from the interior kernel's ring units)
+// into b = n&1, state n+1 into slot 2; slot 3 holds
 // the previous pair's state-n buffer, which that pair's band step n+1 may
 // still be reading.  h and m come back with state n+1 in slot a (= (n+1)&1),
 // the next pair's state-n buffer in slot b, the old state n-1 buffer in slot
@@ -447,7 +448,9 @@ cudaError_t issue_pair(fdtd2d_ctx* c, const PairPlan& p, DevShot& h, TensorMaps&
   t2.fb[a] = h.fb[2];
   cudaError_t x = cudaStreamWaitEvent(c->side, c->ev_t, 0);
   cudaEvent_t p0 = prof_mark(c, nullptr, 0, 2);
-  if (x == cudaSuccess) x = launch_step_tmat2(p.k, ti, tm, p.tu, p.ntu, n, p.tctas, c->d_ctr, c->d_err, c->stream);
+  if (x == cudaSuccess)
+    x = launch_step_tmat2(p.k, ti, tm, p.tu, p.ntu, n, make_int4(p.ci0, p.ci1, p.ri0, p.ri1), p.tctas, c->d_ctr,
+                          c->d_err, c->stream);
   if (p0) prof_mark(c, p0, (int64_t)(p.ci1 - p.ci0) * (p.ri1 - p.ri0), 2);
   if (x == cudaSuccess) x = cudaEventRecord(c->ev_t, c->stream);
   if (x == cudaSuccess) x = launch_step_tma(p.q, h, p.eu, p.neu, n, p.ectas, c->d_err, c->side);
@@ -940,6 +943,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   }
   int best_k = -1, best_q = -1, best_ectas = 0, best_l = 1;
   std::vector<int4> best_t, best_e;
+  int best_nring = 0;
   TensorMaps best_m{};
   const int quick_q[3] = {tma_shape_find(2, 2), tma_shape_find(4, 2), tma_shape_find(4, 3)};
   for (int k = 0; k < tmat_shape_count(); ++k) {
@@ -983,8 +987,20 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
                   std::min((lv == 1 ? 1 : 3) * std::max(1, tctas / nbt), (ri1 - ri0) / (2 * R)));
         if (lv == 2)
           for (int4& u : tu)
-            u.x = (u.z == ri0 ? kRingTop : 0) | (u.w == ri1 ? kRingBottom : 0) |
-                  (u.y == ci0 - lead ? kRingLeft | (lead / kCols) << 4 : 0) | (u.y + bt == ci1 ? kRingRight : 0);
+            u.x = (h.store == FDTD2D_STORE_F32
+                       ? (u.z == ri0 ? kRingTop : 0) | (u.w == ri1 ? kRingBottom : 0) |
+                             (u.y == ci0 - lead ? kRingLeft : 0) | (u.y + bt == ci1 ? kRingRight : 0)
+                       : 0) |
+                  (u.y == ci0 - lead ? (lead / kCols) << 4 : 0);
+        int nring = 0;
+        if (lv == 2 && h.store != FDTD2D_STORE_F32) {
+          // 16-bit storage: ring units first, step n of R's edge cells, 4 per thread
+          const int cells = 2 * (ci1 - ci0) + 2 * std::max(0, ri1 - ri0 - 2);
+          std::vector<int4> ru;
+          for (int t = 0; t < cells; t += 4 * kCols) ru.push_back(make_int4(kUnitRing, t, std::min(cells, t + 4 * kCols), 0));
+          nring = (int)ru.size();
+          tu.insert(tu.begin(), ru.begin(), ru.end());
+        }
         eu = edge_units(nx, ny, P, ci0, ci1, ri0, ri1, b1, ectas);
         int4 *dt = nullptr, *de = nullptr;
         cudaError_t e = cudaMallocAsync(&dt, tu.size() * sizeof(int4), c->stream);
@@ -1032,6 +1048,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
           best_l = lv;
           best_ectas = ectas;
           best_t = tu;
+          best_nring = nring;
           best_e = eu;
           best_m = maps;
           c->tmat_ctas = tctas1;
@@ -1081,6 +1098,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   c->tma_shape = best_q;          // the one-row kernel's shape on the CPML bands and rows
   c->grid_warps = best_ectas;
   c->n_tunits = (int)best_t.size();
+  c->n_ring = best_nring;
   c->n_eunits = (int)best_e.size();
   c->maps = best_m;
   int w, r, st;
@@ -1612,8 +1630,8 @@ static int run_body(fdtd2d_ctx* c, int32_t n_first, int32_t n_last) {
       e = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
       cudaEvent_t p0 = c->tb ? nullptr : prof_mark(c, nullptr, 0, 1);
       if (e == cudaSuccess)
-        e = launch_step_tmat(c->tmat_shape, c->h, c->maps, c->d_tunits, c->n_tunits, n, c->tmat_ctas, c->d_err,
-                             c->stream);
+        e = launch_step_tmat(c->tmat_shape, c->h, c->maps, c->d_tunits + c->n_ring, c->n_tunits - c->n_ring, n,
+                             c->tmat_ctas, c->d_err, c->stream);
       if (p0) prof_mark(c, p0, (int64_t)(c->reg[1] - c->reg[0]) * (c->reg[3] - c->reg[2]), 1);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_t, 0);
       if (e == cudaSuccess) e = cudaEventRecord(c->ev_t, c->stream);

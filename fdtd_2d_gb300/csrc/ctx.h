@@ -42,6 +42,7 @@ struct fdtd2d_ctx {
   int* d_ctr = nullptr;       // the two-step kernel's unit counter
   int4* d_tunits = nullptr;   // interior units (tensor kernel)
   int n_tunits = 0;
+  int n_ring = 0;             // ring units at the front of d_tunits (two-step form only)
   int4* d_eunits = nullptr;   // the rest (staged kernel)
   int n_eunits = 0;
   fdtd2d::TensorMaps maps{};

@@ -230,16 +230,21 @@ cudaError_t launch_step_tmat(int shape, const DevShot& shot, const TensorMaps& m
                              int n_units, int n_global, int max_ctas, int* err, cudaStream_t stream);
 
 // Two-step (temporally blocked) form of the same kernel: steps n and n+1 of
-// units (ring, c0, j0, j1) in one pass over state n-1, with n = n_global -
-// base_n.  The units tile a region R whose cells and 1-cell surround have no
-// CPML; each unit recomputes step n one cell around itself, and writes state
-// n+1 to slot 2 and, on the cells of R next to the rest of the grid (ring
-// flags kRing*), state n to slot 1.  CTAs take units in turn from *ctr,
+// units (flags, c0, j0, j1) in one pass over state n-1, with n = n_global -
+// base_n.  The units tile a region R = [ring.x, ring.y) x [ring.z, ring.w)
+// whose cells and 1-cell surround have no CPML; each unit recomputes step n
+// one cell around itself and writes state n+1 to slot 2 (bits 4-6 of flags:
+// the unit's leading warps left of R).  State n of R's edge cells goes to
+// slot 1, for the CPML-band kernel's step n+1: with FP32 storage from the
+// units next to them (flags kRing*), with 16-bit storage from ring units
+// (kUnitRing, t0, t1, 0: edge cells t0 .. t1-1, rows ring.z and ring.w-1,
+// then columns ring.x and ring.y-1).  CTAs take units in turn from *ctr,
 // which must be 0 at launch (launch_frame resets it).
-enum RingFlags : int { kRingTop = 1, kRingBottom = 2, kRingLeft = 4, kRingRight = 8 };
+enum UnitFlags : int { kRingTop = 1, kRingBottom = 2, kRingLeft = 4, kRingRight = 8, kUnitRing = 256 };
 int tmat2_resident_ctas(int shape, int store, int device);
 cudaError_t launch_step_tmat2(int shape, const DevShot& shot, const TensorMaps& maps, const int4* units,
-                              int n_units, int n_global, int max_ctas, int* ctr, int* err, cudaStream_t stream);
+                              int n_units, int n_global, int4 ring, int max_ctas, int* ctr, int* err,
+                              cudaStream_t stream);
 // Step n (n_global - base_n) of the 2-cell frame around R = [ci0, ci1) x
 // [ri0, ri1) (columns [ci0-2, ci1+2) x rows [ri0-2, ri1+2), minus R) from
 // slot (n-1)&1 into slot n&1, sources applied, detectors left to the CPML

@@ -363,7 +363,7 @@ __device__ __forceinline__ void pts2(const DevShot& S, int p0, int p1, int i, in
   }
 }
 
-// Two time steps of one unit (ring, c0, j0, j1) in one pass over state n-1
+// Two time steps of one unit (flags, c0, j0, j1) in one pass over state n-1
 // (slot 0).  Step n runs over rows j0-1 .. j1 and, per warp, one column
 // beyond each side of its 128 (lane 0 the left one, lane 31 the right one),
 // so that step n+1 over the warp's cells [i0, i0+128) x [j0, j1) needs
@@ -371,14 +371,16 @@ __device__ __forceinline__ void pts2(const DevShot& S, int p0, int p1, int i, in
 // row j.  Step-n values reach step n+1 as a store and reload would give
 // them (Sto::rt*), and every update is the one-step kernel's, operation for
 // operation, so the two steps give the bits of two one-step launches.
-// State n+1 goes to slot 2; state n of the unit's cells on R's edge rows and
-// columns (ring flags) to slot 1, where the CPML-band kernel's step n+1
-// reads it.
+// State n+1 goes to slot 2, and state n of R's edge rows and columns, which
+// the CPML-band kernel's step n+1 reads, to slot 1: with FP32 storage from
+// here (ring flags), with 16-bit storage from the ring units (ring_unit),
+// because stores of it in the unrolled 16-bit row loop, even when seldom
+// taken, slowed that form 13 %.
 template <class C>
 __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const int4 ud, int n, int* err) {
   using T = typename C::Elem;
   using St = Sto<T>;
-  const int ring = ud.x, c0 = ud.y, j0 = ud.z, j1 = ud.w;
+  const int c0 = ud.y, j0 = ud.z, j1 = ud.w;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t pitch = S.pitch;
   const bool has_kp = S.kp != nullptr;
@@ -405,12 +407,12 @@ __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const in
   const float rj = kScaled ? __fmul_rn(S.sc[3], iH) : 1.f;                         // sJ/sH
   const float rk = kScaled ? __fmul_rn(__fmul_rn(S.sc[4], sE), S.isc[3]) : 1.f;    // sK sE/sJ
 
-  // The first `idle` warps of a unit (bits 4-6 of its ring word) lie left of
+  // The first `idle` warps of a unit (bits 4-6 of its flags) lie left of
   // R: a region that is not a whole number of units wide starts with a unit
   // whose leading columns belong to the CPML-band kernel.  Those warps only
   // follow the stages (barrier waits and arrivals); their few preamble
   // loads read the first working warp's columns, which are in bounds.
-  const int idle = (ring >> 4) & 7;
+  const int idle = (ud.x >> 4) & 7;
   const bool act = warp >= idle;
   const int wl = act ? warp : idle;            // the warp whose columns this one addresses
   const int i0 = c0 + wl * kCols;              // this warp's first column
@@ -534,23 +536,27 @@ __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const in
       }
       const bool own = j >= j0 && j < j1;
       pts2<kScaled>(S, p0, p1, i, n, own, ezs_n, hxn, hyn, xc, ezE);
-      if (own) {
-        const int64_t o = (int64_t)j * pitch + i;
-        if (((ring & kRingTop) && j == j0) || ((ring & kRingBottom) && j == j1 - 1)) {
-          St::stcs4(ezm + o, ezs_n);
-          St::stcs4(hxm + o, hxn);
-          St::stcs4(hym + o, hyn);
-          St::stcs4(jzm + o, jzn);
-        } else if ((ring & kRingLeft) && warp == idle && lane == 0) {
-          St::st1(ezm + o, ezs_n[0]);
-          St::st1(hxm + o, hxn[0]);
-          St::st1(hym + o, hyn[0]);
-          St::st1(jzm + o, jzn[0]);
-        } else if ((ring & kRingRight) && warp == C::kWarps - 1 && lane == 31) {
-          St::st1(ezm + o + 3, ezs_n[3]);
-          St::st1(hxm + o + 3, hxn[3]);
-          St::st1(hym + o + 3, hyn[3]);
-          St::st1(jzm + o + 3, jzn[3]);
+      if constexpr (!kScaled) {
+        // FP32: state n of R's edge rows and columns (flags kRing*) to slot
+        // 1 from here; the 16-bit forms take it from the ring units
+        if (own) {
+          const int64_t o = (int64_t)j * pitch + i;
+          if (((ud.x & kRingTop) && j == j0) || ((ud.x & kRingBottom) && j == j1 - 1)) {
+            St::stcs4(ezm + o, ezs_n);
+            St::stcs4(hxm + o, hxn);
+            St::stcs4(hym + o, hyn);
+            St::stcs4(jzm + o, jzn);
+          } else if ((ud.x & kRingLeft) && warp == idle && lane == 0) {
+            St::st1(ezm + o, ezs_n[0]);
+            St::st1(hxm + o, hxn[0]);
+            St::st1(hym + o, hyn[0]);
+            St::st1(jzm + o, jzn[0]);
+          } else if ((ud.x & kRingRight) && warp == C::kWarps - 1 && lane == 31) {
+            St::st1(ezm + o + 3, ezs_n[3]);
+            St::st1(hxm + o + 3, hxn[3]);
+            St::st1(hym + o + 3, hyn[3]);
+            St::st1(jzm + o + 3, jzn[3]);
+          }
         }
       }
 
@@ -638,6 +644,62 @@ __device__ void tband2(const DevShot& S, const TensorMaps& M, TRing& R, const in
   }
 }
 
+// One cell (i, j) of step n outside the CPML: the one-step kernels' updates
+// of Hx, Hy (and the Hx, Hy the Ez update takes from the cells above and to
+// the left), Jz and Ez, operation for operation, from state n-1 in slot rd
+// into slot wr, sources applied.
+template <class T>
+__device__ __forceinline__ void frame_cell(const DevShot& S, int i, int j, int n, int rd, int wr) {
+  using St = Sto<T>;
+  const int64_t p = S.pitch, o = (int64_t)j * p + i;
+  const float sE = S.sc[0], sHx = S.sc[1], sHy = S.sc[2], sJ = S.sc[3], sK = S.sc[4];
+  const T* ez = field_ptr_t<T>(S, kEz, rd);
+  const T* hx = field_ptr_t<T>(S, kHx, rd);
+  const T* hy = field_ptr_t<T>(S, kHy, rd);
+  const T* jz = field_ptr_t<T>(S, kJz, rd);
+  const float e_c = St::ldg1(ez + o, sE), e_r = St::ldg1(ez + o + 1, sE), e_l = St::ldg1(ez + o - 1, sE);
+  const float e_d = St::ldg1(ez + o + p, sE), e_u = St::ldg1(ez + o - p, sE);
+  const float da = S.da, db = S.db;
+  const float hx_c = upd_h(da, St::ldg1(hx + o, sHx), db, e_c, e_d, __ldg(S.den_hy + j));
+  const float hx_u = upd_h(da, St::ldg1(hx + o - p, sHx), db, e_u, e_c, __ldg(S.den_hy + j - 1));
+  const float hy_c = upd_h(da, St::ldg1(hy + o, sHy), db, e_r, e_c, __ldg(S.den_hx + i));
+  const float hy_l = upd_h(da, St::ldg1(hy + o - 1, sHy), db, e_c, e_l, __ldg(S.den_hx + i - 1));
+  const float kp = S.kp ? St::ldg1(reinterpret_cast<const T*>(S.kp) + o, sK) : 0.f;
+  const float jz_n = upd_j(S.ja, St::ldg1(jz + o, sJ), kp, e_c);
+  float e = upd_e(S.ca, e_c, S.cb, __fsub_rn(hy_c, hy_l), __ldg(S.den_ex + i), __fsub_rn(hx_u, hx_c),
+                  __ldg(S.den_ey + j), jz_n);
+  for (int q = __ldg(S.row_start + j), q1 = __ldg(S.row_start + j + 1); q < q1; ++q) {
+    const int4 pt = __ldg(S.pts + q);
+    if (pt.y == kPointSource && pt.x == i) e = __fsub_rn(e, __ldg(S.src_val + (int64_t)n * S.n_src + pt.z));
+  }
+  St::st1(field_ptr_t<T>(S, kEz, wr) + o, e, S.isc[0]);
+  St::st1(field_ptr_t<T>(S, kHx, wr) + o, hx_c, S.isc[1]);
+  St::st1(field_ptr_t<T>(S, kHy, wr) + o, hy_c, S.isc[2]);
+  St::st1(field_ptr_t<T>(S, kJz, wr) + o, jz_n, S.isc[3]);
+}
+
+// A ring unit of the two-step kernel (kUnitRing, t0, t1, 0; 16-bit
+// storage): step n of R's edge cells t0 .. t1-1 (rows ri0 and ri1-1 over
+// columns [ci0, ci1), then columns ci0 and ci1-1 over the rows between; rg =
+// (ci0, ci1, ri0, ri1)) from slot 0 into slot 1, where the CPML-band
+// kernel's step n+1 and the frame kernel read them.
+template <class T>
+__device__ void ring_unit(const DevShot& S, const int4 rg, const int4 ud, int n, int nthreads) {
+  const int w = rg.y - rg.x, h = rg.w - rg.z - 2;
+  for (int t = ud.y + (int)threadIdx.x; t < ud.z; t += nthreads) {
+    int i, j;
+    if (t < 2 * w) {
+      i = rg.x + t % w;
+      j = t < w ? rg.z : rg.w - 1;
+    } else {
+      const int q = t - 2 * w;
+      j = rg.z + 1 + q % h;
+      i = q < h ? rg.x : rg.y - 1;
+    }
+    frame_cell<T>(S, i, j, n, 0, 1);
+  }
+}
+
 template <class C>
 __global__ void __launch_bounds__(C::kThreads, C::kMinBlocks)
 step_tmat_kernel(const __grid_constant__ DevShot S, const __grid_constant__ TensorMaps M,
@@ -668,7 +730,7 @@ step_tmat_kernel(const __grid_constant__ DevShot S, const __grid_constant__ Tens
 template <class C>
 __global__ void __launch_bounds__(C::kThreads, C::kMinBlocks2)
 step_tmat2_kernel(const __grid_constant__ DevShot S, const __grid_constant__ TensorMaps M,
-                  const int4* __restrict__ units, int n_units, int n_global, int* ctr, int* err) {
+                  const int4* __restrict__ units, int n_units, int n_global, int4 rg, int* ctr, int* err) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[C::kStages], empty[C::kStages];
   __shared__ int next;
@@ -694,42 +756,13 @@ step_tmat2_kernel(const __grid_constant__ DevShot S, const __grid_constant__ Ten
     const int u = next;
     __syncthreads();
     if (u >= n_units) return;
-    tband2<C>(S, M, R, __ldg(units + u), n, err);
+    const int4 ud = __ldg(units + u);
+    if (ud.x & kUnitRing) {
+      ring_unit<typename C::Elem>(S, rg, ud, n, C::kThreads);
+    } else {
+      tband2<C>(S, M, R, ud, n, err);
+    }
   }
-}
-
-// One frame cell (i, j) of step n: the one-step kernels' updates of Hx, Hy
-// (and the Hx, Hy the Ez update takes from the cells above and to the left),
-// Jz and Ez, operation for operation, from the stored state n-1.
-template <class T>
-__device__ __forceinline__ void frame_cell(const DevShot& S, int i, int j, int n) {
-  using St = Sto<T>;
-  const int par = (n - 1) & 1;
-  const int64_t p = S.pitch, o = (int64_t)j * p + i;
-  const float sE = S.sc[0], sHx = S.sc[1], sHy = S.sc[2], sJ = S.sc[3], sK = S.sc[4];
-  const T* ez = field_ptr_t<T>(S, kEz, par);
-  const T* hx = field_ptr_t<T>(S, kHx, par);
-  const T* hy = field_ptr_t<T>(S, kHy, par);
-  const T* jz = field_ptr_t<T>(S, kJz, par);
-  const float e_c = St::ldg1(ez + o, sE), e_r = St::ldg1(ez + o + 1, sE), e_l = St::ldg1(ez + o - 1, sE);
-  const float e_d = St::ldg1(ez + o + p, sE), e_u = St::ldg1(ez + o - p, sE);
-  const float da = S.da, db = S.db;
-  const float hx_c = upd_h(da, St::ldg1(hx + o, sHx), db, e_c, e_d, __ldg(S.den_hy + j));
-  const float hx_u = upd_h(da, St::ldg1(hx + o - p, sHx), db, e_u, e_c, __ldg(S.den_hy + j - 1));
-  const float hy_c = upd_h(da, St::ldg1(hy + o, sHy), db, e_r, e_c, __ldg(S.den_hx + i));
-  const float hy_l = upd_h(da, St::ldg1(hy + o - 1, sHy), db, e_c, e_l, __ldg(S.den_hx + i - 1));
-  const float kp = S.kp ? St::ldg1(reinterpret_cast<const T*>(S.kp) + o, sK) : 0.f;
-  const float jz_n = upd_j(S.ja, St::ldg1(jz + o, sJ), kp, e_c);
-  float e = upd_e(S.ca, e_c, S.cb, __fsub_rn(hy_c, hy_l), __ldg(S.den_ex + i), __fsub_rn(hx_u, hx_c),
-                  __ldg(S.den_ey + j), jz_n);
-  for (int q = __ldg(S.row_start + j), q1 = __ldg(S.row_start + j + 1); q < q1; ++q) {
-    const int4 pt = __ldg(S.pts + q);
-    if (pt.y == kPointSource && pt.x == i) e = __fsub_rn(e, __ldg(S.src_val + (int64_t)n * S.n_src + pt.z));
-  }
-  St::st1(field_ptr_t<T>(S, kEz, par ^ 1) + o, e, S.isc[0]);
-  St::st1(field_ptr_t<T>(S, kHx, par ^ 1) + o, hx_c, S.isc[1]);
-  St::st1(field_ptr_t<T>(S, kHy, par ^ 1) + o, hy_c, S.isc[2]);
-  St::st1(field_ptr_t<T>(S, kJz, par ^ 1) + o, jz_n, S.isc[3]);
 }
 
 template <class T>
@@ -752,12 +785,12 @@ __global__ void __launch_bounds__(256) frame_kernel(const __grid_constant__ DevS
       j = ri0 + q % h;
       i = r < 2 ? ci0 - 2 + r : ci1 + r - 2;
     }
-    frame_cell<T>(S, i, j, n);
+    frame_cell<T>(S, i, j, n, (n - 1) & 1, n & 1);
   }
 }
 
 using TKernelFn = void (*)(DevShot, TensorMaps, const int4*, int, int, int*);
-using TKernelFn2 = void (*)(DevShot, TensorMaps, const int4*, int, int, int*, int*);
+using TKernelFn2 = void (*)(DevShot, TensorMaps, const int4*, int, int, int4, int*, int*);
 
 struct TShape {
   int warps, rows, stages;
@@ -815,13 +848,14 @@ cudaError_t launch_step_tmat(int shape, const DevShot& shot, const TensorMaps& m
 }
 
 cudaError_t launch_step_tmat2(int shape, const DevShot& shot, const TensorMaps& maps, const int4* units,
-                              int n_units, int n_global, int max_ctas, int* ctr, int* err, cudaStream_t stream) {
+                              int n_units, int n_global, int4 ring, int max_ctas, int* ctr, int* err,
+                              cudaStream_t stream) {
   const TShape& e = kTShapes[shape];
   const int ctas = max_ctas < n_units ? max_ctas : n_units;
   if (ctas <= 0) return cudaSuccess;
   if (shot.sc[1] != shot.sc[2]) return cudaErrorInvalidValue;   // one H scale (stored-unit curl)
   const int st = shot.store;
-  e.fn2[st]<<<ctas, e.warps * 32, e.smem[st], stream>>>(shot, maps, units, n_units, n_global, ctr, err);
+  e.fn2[st]<<<ctas, e.warps * 32, e.smem[st], stream>>>(shot, maps, units, n_units, n_global, ring, ctr, err);
   return cudaGetLastError();
 }
 
