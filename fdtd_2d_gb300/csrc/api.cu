@@ -910,10 +910,15 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
     if (psi_trial) cudaFreeAsync(psi_trial, c->stream);
     return FDTD2D_ERR_CUDA;
   }
+  // Trials time `reps` steps (pairs: reps pairs, halved), about 0.6 ms of
+  // work at ~200 Gcell/s and at least 3: at 2048^2 three pairs (~0.1 ms)
+  // picked the one-step form for F16 at 155 Gcell/s where two steps per
+  // pass run at 179.
+  const int reps = (int)std::max<int64_t>(3, std::min<int64_t>(24, (int64_t)(0.6e-3 / (5e-12 * (double)nx * ny)) + 1));
   auto timed = [&](auto&& step) -> float {
     cudaError_t e = step();
     if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
-    for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = step();
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) e = step();
     if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
     if (e == cudaSuccess) e = cudaEventSynchronize(e1);
     float ms = -1.f;
@@ -926,7 +931,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
     cudaError_t e = pair();
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
     if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
-    for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = pair();
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) e = pair();
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_e, 0);
     if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
     if (e == cudaSuccess) e = cudaEventSynchronize(e1);
@@ -961,6 +966,11 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
     const int tctas2 = try2 ? tmat2_resident_ctas(k, h.store, device) : 0;
     for (int lv = 1; lv <= 2; ++lv) {
       if ((lv == 2 && !try2) || (lv == 1 && tb_mode == 1)) continue;
+      // Where two steps per pass can run, the quick search times only that
+      // form: forced runs of every tensor shape at 1024^2-3072^2, FP32 and
+      // F16, found it 5-60 % faster than one step per pass, and short trials
+      // of both forms picked the one-step form at 1024^2 and 2048^2.
+      if (lv == 1 && try2 && tb_mode < 0 && !full) continue;
       const int tctas = lv == 1 ? tctas1 : tctas2;
       // interior region: rows [ri0, ri1), columns [ci0, ci1) with ci0 the
       // first multiple of the one-row band at or past the CPML (two-step
@@ -1064,7 +1074,7 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (psi_trial) cudaFreeAsync(psi_trial, c->stream);
-  if (!have && best > 0.f && best < 1e29f) c->path_ms = best / 3;   // trials time 3 steps
+  if (!have && best > 0.f && best < 1e29f) c->path_ms = best / reps;   // trials time `reps` steps
   if (h.fb[2] && !(best_k >= 0 && best_l == 2)) {
     // the two-step form lost: give its buffers back
     for (int b = 2; b < 4; ++b) {
