@@ -1037,16 +1037,16 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
             return x;
           });
         } else if (e == cudaSuccess) {
-          // every trial pair starts from the state in slot (n1-1)&1, which no
-          // pair writes, and computes the same values into the other slots;
-          // psi goes to the scratch slab
+          // pairs as the run issues them, the field slots rotating from pair
+          // to pair (all at step n1: the values are not used), psi into the
+          // scratch slab; the shot's buffers are zeroed again after the trials
+          // (a trial that kept reading one slot and writing another measured
+          // within ~10 % of the run, enough to pick the wrong shape)
           const PairPlan pl{k, tctas, (int)tu.size(), dt, q, ectas, (int)eu.size(), de, ci0, ci1, ri0, ri1};
-          ms = timed2([&] {
-            DevShot t2 = t;
-            t2.psi = psi_trial;
-            TensorMaps m2 = maps;
-            return issue_pair(c, pl, t2, m2, n1);
-          });
+          DevShot t2 = t;
+          t2.psi = psi_trial;
+          TensorMaps m2 = maps;
+          ms = timed2([&] { return issue_pair(c, pl, t2, m2, n1); });
           if (ms >= 0) ms *= 0.5f;
         }
         if (dt) cudaFreeAsync(dt, c->stream);
@@ -1075,6 +1075,16 @@ int setup_tmat(fdtd2d_ctx* c, int device) {
   cudaEventDestroy(e1);
   if (psi_trial) cudaFreeAsync(psi_trial, c->stream);
   if (!have && best > 0.f && best < 1e29f) c->path_ms = best / reps;   // trials time `reps` steps
+  // the trials wrote the shot's field buffers and psi: back to their state
+  // at create, all zero
+  if (!have) {
+    const size_t fbytes = (size_t)h.cells * 4 * store_bytes(h.store);
+    cudaError_t e = cudaSuccess;
+    for (int b = 0; b < 4 && e == cudaSuccess; ++b)
+      if (h.fb[b]) e = cudaMemsetAsync(h.fb[b], 0, fbytes, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h.psi, 0, ((size_t)h.psi_buf * 2 + 1024) * sizeof(float), c->stream);
+    if (e != cudaSuccess) return fail_cuda(c, e);
+  }
   if (h.fb[2] && !(best_k >= 0 && best_l == 2)) {
     // the two-step form lost: give its buffers back
     for (int b = 2; b < 4; ++b) {
