@@ -538,10 +538,15 @@ std::string device_ident(int device) {
 }
 
 // "<device>|<class fields>|<what and overrides>" (the last part holds '|'s)
+// The version of the timing that made a choice: a file entry of another
+// version is not used (choices made by an earlier candidate set or trial
+// method are timed again).
+constexpr int kChoiceVersion = 2;
+
 std::string key_text(const ChoiceKey& k) {
-  char b[96];
-  std::snprintf(b, sizeof b, "|%d|%d|%d|%d|%d|", std::get<1>(k), std::get<2>(k), std::get<3>(k), std::get<4>(k),
-                std::get<5>(k));
+  char b[112];
+  std::snprintf(b, sizeof b, "|v%d|%d|%d|%d|%d|%d|", kChoiceVersion, std::get<1>(k), std::get<2>(k), std::get<3>(k),
+                std::get<4>(k), std::get<5>(k));
   return device_ident(std::get<0>(k)) + b + clean(std::get<6>(k));
 }
 
@@ -566,8 +571,9 @@ void load_choices(int device) {   // g_choice_mu held
     if (!g_file.count(key)) g_file[key] = ch;
     // entries of this device go to the lookup table
     if (key.compare(0, id.size() + 1, id + "|") != 0) continue;
-    int f1, f2, f3, f4, f5, used = 0;
-    if (std::sscanf(key.c_str() + id.size(), "|%d|%d|%d|%d|%d|%n", &f1, &f2, &f3, &f4, &f5, &used) != 5 || !used)
+    int ver, f1, f2, f3, f4, f5, used = 0;
+    if (std::sscanf(key.c_str() + id.size(), "|v%d|%d|%d|%d|%d|%d|%n", &ver, &f1, &f2, &f3, &f4, &f5, &used) != 6 ||
+        !used || ver != kChoiceVersion)
       continue;
     const ChoiceKey ck{device, f1, f2, f3, f4, f5, key.substr(id.size() + used)};
     if (!g_choice.count(ck)) g_choice[ck] = ch;

@@ -334,8 +334,9 @@ int fdtd2d_time_step_kernel(fdtd2d_ctx *ctx, int on);
 
 /* Forget the kernel choices fdtd2d_create keeps per shot class (the next
    shot of every class is timed again).  The choices are also persisted in a
-   JSON file keyed by the device's name, SM count and compute capability and
-   the shot class: $FDTD2D_TUNE_CACHE, else
+   JSON file keyed by the device's name, SM count and compute capability, the
+   version of the timing method (entries of another version are timed again)
+   and the shot class: $FDTD2D_TUNE_CACHE, else
    $XDG_CACHE_HOME/fdtd2d/kernel_choices.json, else
    $HOME/.cache/fdtd2d/kernel_choices.json (FDTD2D_TUNE_CACHE=0: memory
    only).  A process reads the file at the first shot of a device, so a shot

@@ -44,5 +44,10 @@ def test_choices_persist_across_processes(gpu, tmp_path):
     second = _run(env)
     assert second[0][0] == "2"           # a new process reads the file
     assert second[0][1] == first[0][1]   # and makes the same choice
+    # an entry written by another version of the timing is not used
+    text = cache.read_text()
+    assert "|v2|" in text
+    cache.write_text(text.replace("|v2|", "|v1|"))
+    assert _run(env)[0][0] == "0"
     env["FDTD2D_TUNE_CACHE"] = "0"       # memory only: timed again
     assert _run(env)[0][0] == "0"
