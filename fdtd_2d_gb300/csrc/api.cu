@@ -182,16 +182,17 @@ void add_units(std::vector<int4>& u, int ca, int cb, int band, int ra, int rb, i
 // [ci1, nx) on every row, and over [ci0, ci1) on rows [0, ri0) and [ri1,
 // ny - 1).  Each band's rows are cut into strips of about equal cost (a row
 // of the CPML row strips costs about 1.5 plain rows, a row of a band that
-// holds an x strip about 1.3) so that the strips fill `ctas` CTAs in one
-// wave: the band kernel's step between two interior passes runs alone, and
-// its time is that of its longest CTA.
+// holds an x strip about 2: with 1.3 the x-strip bands' strips finished last,
+// 0.2-1.5 % slower on the 2048^2 and 8192^2 shots) so that the strips fill
+// `ctas` CTAs in one wave: the band kernel's step between two interior
+// passes runs alone, and its time is that of its longest CTA.
 std::vector<int4> edge_units(int nx, int ny, int P, int ci0, int ci1, int ri0, int ri1, int band, int ctas) {
   struct Seg {
     int c0, j0, j1;
     double w;
   };
   std::vector<Seg> segs;
-  auto xw = [&](int c) { return (c == 0 || c + band - 1 >= nx - P) ? 1.3 : 1.0; };
+  auto xw = [&](int c) { return (c == 0 || c + band - 1 >= nx - P) ? 2.0 : 1.0; };
   for (int c = ci0; c < ci1; c += band) {
     segs.push_back({c, 0, ri0, 1.5});
     segs.push_back({c, ri1, ny - 1, 1.5});
